@@ -1,0 +1,242 @@
+// C entry points over the reference's own CPU functions and kernel bodies,
+// compiled from the reference sources by oracle/build_ref.sh into
+// oracle/_ref/libref.so.  Used only to pin the oracle (test infrastructure);
+// the kernels run as host loops over thread ids (see inc/cuda_runtime_api.h).
+#include <cuda_runtime_api.h>  // the host stand-in in oracle/ref/inc
+
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <algorithm>
+#include <vector>
+#include <unistd.h>
+
+#include "cuda_objects.cuh"
+#include "dipole_kernals.cuh"
+#include "fields.h"
+#include "trove_functions.h"
+#include "../oracle.h"
+
+// Zero-filled array allocations: the reference's threej table leaves slots it
+// never reads with a nonzero weight uninitialised; zeroing keeps its kernels'
+// 0*slot products finite.
+void* operator new[](size_t n) {
+  void* p = std::calloc(n ? n : 1, 1);
+  if (!p) throw std::bad_alloc();
+  return p;
+}
+void operator delete[](void* p) noexcept { std::free(p); }
+void operator delete[](void* p, size_t) noexcept { std::free(p); }
+
+gi_ref_dim3 blockIdx, blockDim, threadIdx, gridDim;
+double s[1];  // backs the reference's `extern __shared__ double s[]` (unused kernels)
+extern intensity_info int_info;
+
+namespace {
+
+struct RefBasis {
+  cuda_bset_contrT c;
+  TO_bset_contrT t;
+  std::vector<double*> irr;
+  std::vector<int*> nper;
+  int* ijterms = nullptr;
+};
+
+void make_basis(const or_basis* b, int nrep, RefBasis& rb) {
+  std::memset(&rb.c, 0, sizeof(rb.c));
+  std::memset(&rb.t, 0, sizeof(rb.t));
+  rb.t.jval = b->jval;
+  rb.t.Maxsymcoeffs = b->Maxsymcoeffs;
+  rb.t.Maxcontracts = b->Maxcontracts;
+  rb.t.max_deg_size = b->max_deg_size;
+  rb.t.mat_size = b->mat_size;
+  rb.t.irr = new TO_PTrepresT[nrep];
+  rb.nper.resize(nrep);
+  for (int g = 0; g < nrep; g++) {
+    rb.nper[g] = new int[b->Maxsymcoeffs];
+    for (int ic = 0; ic < b->Maxsymcoeffs; ic++) rb.nper[g][ic] = b->Nsym[g + ic * nrep];
+    rb.t.irr[g].N = rb.nper[g];
+    rb.t.irr[g].repres = const_cast<double*>(b->repres[g]);
+  }
+  compute_ijterms(rb.t, &rb.ijterms, nrep);
+  rb.irr.resize(nrep);
+  for (int g = 0; g < nrep; g++) rb.irr[g] = const_cast<double*>(b->repres[g]);
+  rb.c.jval = b->jval;
+  rb.c.Maxsymcoeffs = b->Maxsymcoeffs;
+  rb.c.max_deg_size = b->max_deg_size;
+  rb.c.Maxcontracts = b->Maxcontracts;
+  rb.c.icontr2icase = const_cast<int*>(b->icontr2icase);
+  rb.c.iroot_correlat_j0 = const_cast<int*>(b->iroot_correlat_j0);
+  rb.c.k = const_cast<int*>(b->k);
+  rb.c.ktau = const_cast<int*>(b->ktau);
+  rb.c.irr_repres = rb.irr.data();
+  rb.c.N = const_cast<int*>(b->Nsym);
+  rb.c.Ntotal = const_cast<int*>(b->Ntotal);
+  rb.c.ijterms = rb.ijterms;
+}
+
+void free_basis(RefBasis& rb, int nrep) {
+  for (int g = 0; g < nrep; g++) delete[] rb.nper[g];
+  delete[] rb.t.irr;
+  delete[] rb.ijterms;
+}
+
+void set_info(int nrep, const int* degen, int jmax, int N, int dimenmax) {
+  intensity_info ii;
+  ii.sym_nrepres = nrep;
+  ii.sym_degen = const_cast<int*>(degen);
+  ii.jmax = jmax + 1;  // as cuda_host.cu:913
+  ii.dip_stride_1 = N;
+  ii.dip_stride_2 = N * N;
+  ii.dimenmax = dimenmax;
+  ii.sq2 = 1.0 / std::sqrt(2.0);
+  copy_intensity_info(&ii);
+}
+
+void one_thread_grid() {
+  blockIdx = {0, 0, 0};
+  threadIdx = {0, 0, 0};
+  blockDim = {1, 1, 1};
+  gridDim = {1, 1, 1};
+}
+
+void fill_job(const or_job* j, FintensityJob& f, std::vector<int*>& keep) {
+  std::memset((void*)&f, 0, sizeof(f));
+  f.ZPE = j->ZPE;
+  for (int i = 0; i < 2; i++) {
+    f.erange_lower[i] = j->erange_lower[i];
+    f.erange_upper[i] = j->erange_upper[i];
+    f.freq_window[i] = j->freq_window[i];
+    f.jvals[i] = j->jvals[i];
+  }
+  f.erange[0] = std::min(f.erange_lower[0], f.erange_upper[0]);
+  f.erange[1] = std::max(f.erange_lower[1], f.erange_upper[1]);
+  f.q_stat = j->q_stat;
+  f.temperature = j->temperature;
+  f.molec.nmodes = j->nmodes;
+  f.molec.sym_nrepres = j->nrep;
+  f.molec.sym_degen = const_cast<int*>(j->degen);
+  f.molec.sym_type = j->sym_type;
+  f.gns = const_cast<double*>(j->gns);
+  f.isym_pairs = const_cast<int*>(j->isym_pairs);
+  f.igamma_pair = new int[j->nrep];
+  keep.push_back(f.igamma_pair);
+  f.reduced = j->reduced != 0;
+  f.quanta_lower = new int*[2];
+  f.quanta_upper = new int*[2];
+  for (int i = 0; i < 2; i++) {
+    f.quanta_lower[i] = const_cast<int*>(j->quanta_lower) + i * j->nmodes;
+    f.quanta_upper[i] = const_cast<int*>(j->quanta_upper) + i * j->nmodes;
+  }
+  f.isym_do = new bool[j->nrep];
+  for (int g = 0; g < j->nrep; g++) f.isym_do[g] = !(j->gns[g] <= 0.00000001);
+}
+
+void drop_job(FintensityJob& f, std::vector<int*>& keep) {
+  for (int* p : keep) delete[] p;
+  delete[] f.quanta_lower;
+  delete[] f.quanta_upper;
+  delete[] f.isym_do;
+}
+
+}  // namespace
+
+extern "C" {
+
+double ref_fakt(double a) { return fakt(a); }
+double ref_three_j(int j1, int j2, int j3, int k1, int k2, int k3) {
+  return three_j(j1, j2, j3, k1, k2, k3);
+}
+
+void ref_precompute_threej(int jmax, double* out) {
+  double* t = nullptr;
+  precompute_threej(&t, jmax);
+  std::memcpy(out, t, sizeof(double) * (size_t)(jmax + 1) * (jmax + 1) * 9);
+  delete[] t;
+}
+
+void ref_compute_ijterms(const or_basis* b, int nrep, int* out) {
+  RefBasis rb;
+  make_basis(b, nrep, rb);
+  std::memcpy(out, rb.ijterms, sizeof(int) * (size_t)b->Maxsymcoeffs * nrep);
+  free_basis(rb, nrep);
+}
+
+// device_correlate_vectors (dipole_kernals.cu:38-71), one host call per root.
+void ref_correlate(const or_basis* b, int nrep, const int* degen, int ideg, int gamma,
+                   const double* vsym, double* vprim) {
+  RefBasis rb;
+  make_basis(b, nrep, rb);
+  set_info(nrep, degen, b->jval, 1, b->Maxcontracts);
+  one_thread_grid();
+  for (int r = 0; r < b->Maxcontracts; r++) {
+    blockIdx.x = (unsigned)r;
+    device_correlate_vectors(&rb.c, ideg, gamma, vsym, vprim);
+  }
+  free_basis(rb, nrep);
+}
+
+// device_compute_1st_half_ls_flipped_dipole (dipole_kernals.cu:162-227) with a
+// one-thread grid, so its grid-stride loop covers every final root.
+// dip_flipped is the layout read_dipole_flipped produces.
+void ref_half_ls_flipped(const or_basis* bI, const or_basis* bF, int nrep, const int* degen,
+                         int N, const double* dip_flipped, int jmax, const double* threej,
+                         const double* vprim, double* half_ls) {
+  RefBasis ri, rf;
+  make_basis(bI, nrep, ri);
+  make_basis(bF, nrep, rf);
+  int dmax = std::max(bI->Maxcontracts, bF->Maxcontracts);
+  set_info(nrep, degen, jmax, N, dmax);
+  one_thread_grid();
+  device_compute_1st_half_ls_flipped_dipole(&ri.c, &rf.c, const_cast<double*>(dip_flipped),
+                                            const_cast<double*>(vprim),
+                                            const_cast<double*>(threej), half_ls);
+  free_basis(ri, nrep);
+  free_basis(rf, nrep);
+}
+
+// read_dipole_flipped (trove_functions.cpp:113-205) on a j0_extfield.chk in dir.
+int ref_read_dipole_flipped(const char* dir, int N, double* out) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof(cwd))) return -1;
+  if (chdir(dir) != 0) return -2;
+  TO_bset_contrT b;
+  std::memset((void*)&b, 0, sizeof(b));
+  b.Maxcontracts = N;
+  double* d = nullptr;
+  size_t sz = 0;
+  read_dipole_flipped(b, &d, sz);
+  int rc = chdir(cwd);
+  (void)rc;
+  std::memcpy(out, d, sz);
+  delete[] d;
+  return (int)(sz / sizeof(double));
+}
+
+// Filters (trove_functions.cpp:1041-1072, 1432-1510) on one level pair.
+// Writes [lower(I), upper(F), intensity(I,F), indF-free] and igamma pairs.
+int ref_filters(const or_job* j, int jI, double EI, int gI, const int* qI, int jF, double EF,
+                int gF, const int* qF, int* out, int* igamma_pair) {
+  FintensityJob f;
+  std::vector<int*> keep;
+  fill_job(j, f, keep);
+  find_igamma_pair(f);
+  for (int g = 0; g < j->nrep; g++) igamma_pair[g] = f.igamma_pair[g];
+  out[0] = energy_filter_lower(f, jI, EI, const_cast<int*>(qI));
+  out[1] = energy_filter_upper(f, jF, EF, const_cast<int*>(qF));
+  out[2] = intensity_filter(f, jI, jF, EI, EF, gI, gF, const_cast<int*>(qI), const_cast<int*>(qF));
+  drop_job(f, keep);
+  return 0;
+}
+
+int ref_degeneracy_filter(const or_job* j, int gI, int gF, int idegI, int idegF) {
+  FintensityJob f;
+  std::vector<int*> keep;
+  fill_job(j, f, keep);
+  int r = degeneracy_filter(f, gI, gF, idegI, idegF);
+  drop_job(f, keep);
+  return r;
+}
+
+}  // extern "C"
