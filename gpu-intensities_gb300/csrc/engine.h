@@ -1,0 +1,166 @@
+// Internal declarations of the GB300 line-intensity engine (host side).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "../../include/gi.h"
+
+namespace gi {
+
+// ------------------------------------------------------------------ memory
+template <class T>
+struct DevArray {
+  T* p = nullptr;
+  size_t n = 0;
+  DevArray() = default;
+  DevArray(const DevArray&) = delete;
+  DevArray& operator=(const DevArray&) = delete;
+  DevArray(DevArray&& o) noexcept : p(o.p), n(o.n) { o.p = nullptr; o.n = 0; }
+  DevArray& operator=(DevArray&& o) noexcept {
+    if (this != &o) { reset(); p = o.p; n = o.n; o.p = nullptr; o.n = 0; }
+    return *this;
+  }
+  ~DevArray() { reset(); }
+  void reset() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    reset();
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc(reinterpret_cast<void**>(&p), count * sizeof(T));
+    if (e == cudaSuccess) n = count; else p = nullptr;
+    return e;
+  }
+  cudaError_t upload(const T* h, size_t count) {
+    cudaError_t e = alloc(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
+  }
+  cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
+  // grow-only workspace
+  cudaError_t reserve(size_t count) { return count <= n ? cudaSuccess : alloc(count); }
+};
+
+inline int round_up(int x, int m) { return (x + m - 1) / m * m; }
+
+// ------------------------------------------------------------------ inputs
+// One rotational/vibrational coupling term of the half line strength:
+//   h[rF] += coef * Z_c[slotI][v(rF)]   (per final (k, tau) "key").
+struct StencilTerm {
+  int32_t slotI;
+  int32_t c;
+  double coef;
+};
+
+struct Basis {
+  int J = 0, D = 0, ncase = 0, max_deg = 0, mat_size = 0;
+  std::vector<int32_t> icontr2icase, iroot, k, ktau, Nsym, Ntotal, ijterms;
+  std::vector<std::vector<double>> repres;  // per gamma
+  // derived
+  std::vector<int32_t> root_key;    // 2k + tau (tau = ktau & 1)
+  std::vector<int32_t> slot_of_key; // [2J+2] -> slot or -1
+  int nslot = 0;
+  std::vector<int32_t> case_ptr, case_roots;  // CSR: roots of each case
+  std::vector<std::vector<int32_t>> s_case;   // per gamma: case of symmetrised s
+  // device copies
+  DevArray<int32_t> d_root_v, d_root_key, d_root_lam, d_root_case, d_case_ptr, d_case_roots;
+  std::vector<DevArray<int32_t>> d_s_case, d_case_iterm, d_case_nelem;
+  std::vector<DevArray<double>> d_rep;
+  // (slot, v) -> roots CSR; depends on the dipole size N
+  int y_N = -1;
+  DevArray<int32_t> d_yptr, d_yroot;
+};
+
+struct Block {
+  int J = 0, gamma = 0, nsize = 0, nvec = 0, ld = 0;  // ld: padded row stride
+  DevArray<double> d_vecs;                              // [nvec][ld], zero padded
+  std::vector<double> energies;
+  std::vector<int32_t> quanta;                          // [nvec][nmodes+1]
+  DevArray<double> d_energies;
+};
+
+struct Level {
+  int J, gamma, rec, ndeg, krot, taurot;
+  double energy;
+};
+
+struct Ctx {
+  int device = 0;
+  size_t budget = 0;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::string err;
+
+  int sym_type = 0, nrep = 0;
+  std::vector<int32_t> degen;
+  bool have_params = false;
+  gi_params params{};
+
+  int N = 0, Kp = 0;          // dipole size and padded row stride
+  DevArray<double> d_mu;      // [3][N rows f][Kp]: row f holds mu_c(:, f)
+
+  std::map<int, std::unique_ptr<Basis>> bases;
+  std::map<std::pair<int, int>, std::unique_ptr<Block>> blocks;
+
+  int threej_jmax = -1;
+  bool threej_user = false;
+  std::vector<double> threej;
+
+  // results of the last run
+  std::vector<Level> levels;
+  std::vector<gi_line> lines;
+  DevArray<gi_line> d_lines;
+  bool lines_on_device = false;
+  int64_t nlines = 0;
+  gi_stats stats{};
+
+  // workspaces
+  DevArray<double> w_y, w_z, w_h, w_t;
+  DevArray<unsigned long long> w_counter;
+  DevArray<int32_t> w_ivec, w_int;
+  DevArray<uint8_t> w_upper;
+  DevArray<StencilTerm> w_stencil;
+  DevArray<int32_t> w_stencil_n, w_levelI, w_levelF;
+};
+
+// ------------------------------------------------------------------ kernels
+struct EpiParams {
+  int jI, jF, ndegI, ndegF, reduced, combo_mask;
+  double gns, zpe, beta, q_stat, fw0, fw1, thresh_S, thresh_I;
+  double A_coef, intens_cm_mol, avogno;
+};
+
+cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int nI, int ndeg,
+                           const Basis& b, int gamma, int degen, int N, int Kp, double* Y,
+                           cudaStream_t s);
+cudaError_t launch_build_h(const double* Z, size_t zstride_c, int ldz, int nslotI, int ndegI,
+                           int nI, const Basis& bF, int gammaF, int degF, int nsizeF, int ldh,
+                           const StencilTerm* st, const int32_t* st_n, int st_max, double* H,
+                           cudaStream_t s);
+cudaError_t launch_half_ls_prim(const double* Z, size_t zstride_c, int ldz, const Basis& bF,
+                                const StencilTerm* st, const int32_t* st_n, int st_max,
+                                double* h, cudaStream_t s);
+cudaError_t launch_epilogue(const double* T, int ldt, int nI, int nF, const int32_t* levelI,
+                            const double* EI, const int32_t* levelF, const double* EF,
+                            const uint8_t* upper_ok, const EpiParams& p, gi_line* out,
+                            unsigned long long* counter, long long cap, cudaStream_t s);
+// C[z][n*ldc + m] = sum_k A[z][m*lda + k] * B[n*ldb + k]; K multiple of 16.
+cudaError_t gemm_fp64_nt(const double* A, int lda, size_t strideA, const double* B, int ldb,
+                         double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch,
+                         cudaStream_t s);
+
+// ------------------------------------------------------------------ host math
+double three_j(int j1, int j2, int j3, int k1, int k2, int k3);
+void precompute_threej(int jmax, std::vector<double>& out);
+
+}  // namespace gi

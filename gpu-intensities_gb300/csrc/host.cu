@@ -1,0 +1,889 @@
+// Host side of the GB300 line-intensity engine: the C ABI (include/gi.h),
+// level table and line filters, block-pair planner and the run loop.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+
+#include "engine.h"
+#include "split.h"
+
+namespace gi {
+
+// ------------------------------------------------------------------ errors
+static gi_status fail(Ctx* c, gi_status s, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return s;
+}
+
+#define GI_CUDA(c, call)                                                                   \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail((c), e_ == cudaErrorMemoryAllocation ? GI_ERR_NOMEM : GI_ERR_CUDA,       \
+                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
+  } while (0)
+
+// ------------------------------------------------------------------ 3j
+// Scaled factorial a!/10^a and Wigner 3j symbol computed the way TROVE's
+// three_j does it (trove_functions.cpp:322-399): Racah's sum over products of
+// the scaled factorials, with the same operation order, so the table agrees
+// bit for bit with the reference's precompute_threej.
+static int nint(double a) { return a >= 0.0 ? (int)(a + 0.5) : (int)(a - 0.5); }
+
+static double fakt(double a) {
+  if (std::fabs(a) < 1e-24) return 1.0;
+  if (a < 0.0) return NAN;
+  const int ic = nint(a);
+  const double ax = a / 10.0;
+  double f = ax;
+  for (int i = 1; i < ic; i++) f *= (ax - (double)i * 0.1);
+  return f;
+}
+
+double three_j(int j1, int j2, int j3, int k1, int k2, int k3) {
+  const double a = j1, b = j2, c = j3, al = k1, be = k2, ga = k3;
+  if (c > a + b || c < std::fabs(a - b)) return 0.0;
+  if (a < 0.0 || b < 0.0 || c < 0.0) return 0.0;
+  if (a < std::fabs(al) || b < std::fabs(be) || c < std::fabs(ga)) return 0.0;
+  if (-1.0 * ga != al + be) return 0.0;
+  const double delta =
+      std::sqrt(fakt(a + b - c) * fakt(a + c - b) * fakt(b + c - a) / fakt(a + b + c + 1.0));
+  const double t1 = fakt(a + al) * fakt(a - al);
+  const double t2 = fakt(b - be) * fakt(b + be);
+  const double t3 = fakt(c + ga) * fakt(c - ga);
+  const double term = std::sqrt((2.0 * c + 1.0) * t1 * t2 * t3);
+  const int nmin = nint(std::max(std::max(a + be - c, b - c - al), 0.0));
+  const int nmax = nint(std::min(std::min(a - al, b + be), a + b - c));
+  double sum = 0.0;
+  for (int n = nmin; n <= nmax; n++) {
+    const double dn = n;
+    const double t4 = fakt(a - al - dn) * fakt(c - b + al + dn);
+    const double t5 = fakt(b + be - dn) * fakt(c - a - be + dn);
+    const double t6 = fakt(dn) * fakt(a + b - c - dn);
+    sum += std::pow(-1.0, n) / (t4 * t5 * t6);
+  }
+  const double clebsh = delta * term * sum / std::sqrt(10.0);
+  const double minus = (nint(a - b - ga) % 2 == 0) ? 1.0 : -1.0;
+  return minus * clebsh / std::sqrt(2.0 * c + 1.0);
+}
+
+// Table threej[jI + kI*J1 + (dJ+1)*J1^2 + (dK+1)*3*J1^2], J1 = jmax+1, holding
+// three_j(jI, 1, jF, kI, kF-kI, -kF) for |dJ|,|dK| <= 1 (trove_functions.cpp:899-925).
+void precompute_threej(int jmax, std::vector<double>& out) {
+  const int J1 = jmax + 1;
+  out.assign((size_t)J1 * J1 * 9, 0.0);
+  for (int jI = 0; jI <= jmax; jI++)
+    for (int jF = std::max(jI - 1, 0); jF <= std::min(jI + 1, jmax); jF++)
+      for (int kI = 0; kI <= jI; kI++)
+        for (int kF = std::max(kI - 1, 0); kF <= std::min(kI + 1, jF); kF++)
+          out[jI + kI * J1 + (jF - jI + 1) * J1 * J1 + (kF - kI + 1) * J1 * J1 * 3] =
+              three_j(jI, 1, jF, kI, kF - kI, -kF);
+}
+
+// ------------------------------------------------------------------ constants
+// CGS constants and prefactors of the reference (cuda_host.cu:12-18).
+struct Phys {
+  double pi, planck, avogno, vellgt, boltz, A_coef, intens_cm_mol;
+  Phys() {
+    pi = 4.0 * std::atan2(1.0, 1.0);
+    planck = 6.62606896e-27;
+    avogno = 6.0221415e23;
+    vellgt = 2.99792458e10;
+    boltz = 1.380658e-16;
+    A_coef = 64.0 * std::pow(10.0, -36.0) * std::pow(pi, 4.0) /
+             (3.0 * 6.62606896 * std::pow(10.0, -27.0));
+    intens_cm_mol = 8.0 * std::pow(10.0, -36.0) * std::pow(pi, 3.0) * avogno /
+                    (3.0 * planck * vellgt);
+  }
+};
+
+// ------------------------------------------------------------------ basis
+static gi_status derive_basis(Ctx* c, Basis& b) {
+  const int D = b.D, nrep = c->nrep;
+  b.root_key.resize(D);
+  int kmax = 0;
+  for (int r = 0; r < D; r++) {
+    const int ic = b.icontr2icase[r], lam = b.icontr2icase[r + D];
+    if (ic < 0 || ic >= b.ncase) return fail(c, GI_ERR_ARG, "basis J=%d: icontr2icase[%d]=%d out of range", b.J, r, ic);
+    if (lam < 0 || lam >= b.mat_size) return fail(c, GI_ERR_ARG, "basis J=%d: lambda %d of root %d >= mat_size", b.J, lam, r);
+    if (b.k[r] < 0 || b.k[r] > b.J) return fail(c, GI_ERR_ARG, "basis J=%d: k[%d]=%d outside 0..J", b.J, r, b.k[r]);
+    if (b.iroot[r] < 0) return fail(c, GI_ERR_ARG, "basis J=%d: negative iroot_correlat_j0", b.J);
+    b.root_key[r] = 2 * b.k[r] + (b.ktau[r] & 1);
+    kmax = std::max(kmax, b.k[r]);
+  }
+  b.slot_of_key.assign(2 * b.J + 2, -1);
+  b.nslot = 0;
+  for (int key = 0; key < 2 * b.J + 2; key++) {
+    bool any = false;
+    for (int r = 0; r < D && !any; r++) any = b.root_key[r] == key;
+    if (any) b.slot_of_key[key] = b.nslot++;
+  }
+  // ijterms (trove_functions.cpp:927-966) and Ntotal consistency
+  b.ijterms.assign((size_t)b.ncase * nrep, 0);
+  for (int g = 0; g < nrep; g++) {
+    int n = 0;
+    for (int it = 0; it < b.ncase; it++) {
+      b.ijterms[it + (size_t)g * b.ncase] = n;
+      const int ne = b.Nsym[g + (size_t)it * nrep];
+      if (ne < 0) return fail(c, GI_ERR_ARG, "basis J=%d: negative N", b.J);
+      n += ne;
+    }
+    if (n != b.Ntotal[g])
+      return fail(c, GI_ERR_ARG, "basis J=%d: Ntotal[%d]=%d but N sums to %d", b.J, g, b.Ntotal[g], n);
+  }
+  // roots of each case (CSR)
+  b.case_ptr.assign(b.ncase + 1, 0);
+  for (int r = 0; r < D; r++) b.case_ptr[b.icontr2icase[r] + 1]++;
+  for (int i = 0; i < b.ncase; i++) b.case_ptr[i + 1] += b.case_ptr[i];
+  b.case_roots.assign(D, 0);
+  {
+    std::vector<int> fill(b.case_ptr.begin(), b.case_ptr.end() - 1);
+    for (int r = 0; r < D; r++) b.case_roots[fill[b.icontr2icase[r]]++] = r;
+  }
+  // symmetrised index -> case, per gamma
+  b.s_case.assign(nrep, {});
+  for (int g = 0; g < nrep; g++) {
+    b.s_case[g].assign(std::max(b.Ntotal[g], 1), 0);
+    for (int it = 0; it < b.ncase; it++) {
+      const int s0 = b.ijterms[it + (size_t)g * b.ncase];
+      const int ne = b.Nsym[g + (size_t)it * nrep];
+      for (int j = 0; j < ne; j++) b.s_case[g][s0 + j] = it;
+    }
+  }
+  // device copies
+  std::vector<int32_t> root_lam(D), root_case(D);
+  for (int r = 0; r < D; r++) {
+    root_case[r] = b.icontr2icase[r];
+    root_lam[r] = b.icontr2icase[r + D];
+  }
+  GI_CUDA(c, b.d_root_v.upload(b.iroot));
+  GI_CUDA(c, b.d_root_key.upload(b.root_key));
+  GI_CUDA(c, b.d_root_lam.upload(root_lam));
+  GI_CUDA(c, b.d_root_case.upload(root_case));
+  GI_CUDA(c, b.d_case_ptr.upload(b.case_ptr));
+  GI_CUDA(c, b.d_case_roots.upload(b.case_roots));
+  b.d_s_case.clear();
+  b.d_case_iterm.clear();
+  b.d_case_nelem.clear();
+  b.d_rep.clear();
+  for (int g = 0; g < nrep; g++) {
+    b.d_s_case.emplace_back();
+    GI_CUDA(c, b.d_s_case.back().upload(b.s_case[g]));
+    std::vector<int32_t> it(b.ncase), ne(b.ncase);
+    for (int i = 0; i < b.ncase; i++) {
+      it[i] = b.ijterms[i + (size_t)g * b.ncase];
+      ne[i] = b.Nsym[g + (size_t)i * nrep];
+    }
+    b.d_case_iterm.emplace_back();
+    GI_CUDA(c, b.d_case_iterm.back().upload(it));
+    b.d_case_nelem.emplace_back();
+    GI_CUDA(c, b.d_case_nelem.back().upload(ne));
+    b.d_rep.emplace_back();
+    GI_CUDA(c, b.d_rep.back().upload(b.repres[g]));
+  }
+  b.y_N = -1;
+  return GI_OK;
+}
+
+// (slot, v) -> roots, once the dipole size N is known.
+static gi_status ensure_ycsr(Ctx* c, Basis& b) {
+  if (b.y_N == c->N) return GI_OK;
+  const int N = c->N;
+  std::vector<int32_t> ptr((size_t)b.nslot * N + 1, 0), roots(b.D);
+  for (int r = 0; r < b.D; r++) {
+    if (b.iroot[r] >= N)
+      return fail(c, GI_ERR_ARG, "basis J=%d: iroot_correlat_j0[%d]=%d >= N=%d", b.J, r, b.iroot[r], N);
+    ptr[(size_t)b.slot_of_key[b.root_key[r]] * N + b.iroot[r] + 1]++;
+  }
+  for (size_t i = 0; i + 1 < ptr.size(); i++) ptr[i + 1] += ptr[i];
+  std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
+  for (int r = 0; r < b.D; r++) roots[fill[(size_t)b.slot_of_key[b.root_key[r]] * N + b.iroot[r]]++] = r;
+  GI_CUDA(c, b.d_yptr.upload(ptr));
+  GI_CUDA(c, b.d_yroot.upload(roots));
+  b.y_N = N;
+  return GI_OK;
+}
+
+// ------------------------------------------------------------------ stencil
+// Terms of the half line strength for a final key (kF, tauF) towards the
+// initial basis of J=jI (dipole_kernals.cu:191-223): coefficient
+// (-1)^sigmaF (-1)^(sigmaI+kI) L f3j s and dipole component c.
+static void build_stencil(const Basis& bI, const Basis& bF, const std::vector<double>& threej,
+                          int tj_jmax, std::vector<StencilTerm>& st, std::vector<int32_t>& st_n) {
+  const int J1 = tj_jmax + 1;
+  const int jI = bI.J, jF = bF.J;
+  const double sq2 = 1.0 / std::sqrt(2.0);
+  const int nkey = 2 * jF + 2;
+  st.assign((size_t)nkey * 6, StencilTerm{0, 0, 0.0});
+  st_n.assign(nkey, 0);
+  for (int keyF = 0; keyF < nkey; keyF++) {
+    const int kF = keyF >> 1, tauF = keyF & 1;
+    const int sigF = (kF % 3) * tauF;
+    const double sgnF = (sigF & 1) ? -1.0 : 1.0;
+    for (int kI = std::max(kF - 1, 0); kI <= std::min(kF + 1, jI); kI++)
+      for (int tauI = 0; tauI < 2; tauI++) {
+        const int slot = bI.slot_of_key[2 * kI + tauI];
+        if (slot < 0) continue;
+        const int sigI = (kI % 3) * tauI;
+        const double sgnI = ((sigI + kI) & 1) ? -1.0 : 1.0;
+        const double f3j = threej[jI + kI * J1 + (jF - jI + 1) * J1 * J1 + (kF - kI + 1) * J1 * J1 * 3];
+        int comp;
+        double L;
+        if (kF == kI) {
+          comp = 2;
+          L = (double)(tauF - tauI);
+        } else if (tauF != tauI) {
+          comp = 0;
+          L = (double)((tauF - tauI) * (kF - kI));
+        } else {
+          comp = 1;
+          L = -1.0;
+        }
+        const double s = (kI != kF && kI * kF != 0) ? sq2 : 1.0;
+        const double coef = sgnF * (sgnI * L * f3j * s);
+        if (coef == 0.0) continue;
+        st[(size_t)keyF * 6 + st_n[keyF]++] = StencilTerm{slot, comp, coef};
+      }
+  }
+}
+
+// ------------------------------------------------------------------ job plan
+struct BlockPlan {
+  Block* blk = nullptr;
+  std::vector<int32_t> level_of_rec;   // -1: not a level
+  std::vector<uint8_t> lower_ok, upper_ok;
+  std::vector<int32_t> ivec;           // records passing the lower filter
+  int nupper = 0;
+};
+
+struct PairPlan {
+  BlockPlan* I;
+  BlockPlan* F;
+  int combo_mask;
+  size_t st_off;  // into the job stencil array (in keys*6 units)
+};
+
+struct Filters {
+  const Ctx* c;
+  double zpe;
+  int jmin, jmax;
+  bool lower(int J, double E, const int32_t* q) const {
+    const gi_params& p = c->params;
+    for (int i = 0; i < p.nmodes; i++) {
+      if (q[i + 1] < p.quanta_lower[0][i] || q[i + 1] > p.quanta_lower[1][i]) return false;
+    }
+    return J >= jmin && J <= jmax && (E - zpe) >= p.erange_lower[0] && (E - zpe) <= p.erange_lower[1];
+  }
+  bool upper(int J, double E, const int32_t* q) const {
+    const gi_params& p = c->params;
+    for (int i = 0; i < p.nmodes; i++) {
+      if (q[i + 1] < p.quanta_upper[0][i] || q[i + 1] > p.quanta_upper[1][i]) return false;
+    }
+    return J >= jmin && J <= jmax && (E - zpe) >= p.erange_upper[0] && (E - zpe) <= p.erange_upper[1];
+  }
+};
+
+static bool isym_do(const Ctx* c, int g) { return !(c->params.gns[g] <= 0.00000001); }
+
+// degeneracy_filter (trove_functions.cpp:1495-1510)
+static bool degeneracy_ok(const Ctx* c, int gI, int gF, int dI, int dF) {
+  if (c->degen[gI] == 1 || c->degen[gF] == 1) return true;
+  if (!c->params.reduced) return true;
+  if (c->sym_type == 2 || c->sym_type == 3) return dI == 1 && dF == 0;
+  return true;
+}
+
+static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
+  auto t_start = std::chrono::steady_clock::now();
+  if (c->nrep == 0) return fail(c, GI_ERR_STATE, "gi_set_symmetry not called");
+  if (!c->have_params) return fail(c, GI_ERR_STATE, "gi_set_params not called");
+  if (c->N == 0) return fail(c, GI_ERR_STATE, "gi_set_dipole not called");
+  if (c->bases.empty()) return fail(c, GI_ERR_STATE, "no basis set");
+  const gi_params& P = c->params;
+  const int nrep = c->nrep;
+  if (P.nmodes < 0 || P.nmodes > GI_MAX_MODES) return fail(c, GI_ERR_ARG, "nmodes out of range");
+  if (P.precision != GI_PREC_FP64 && P.precision != GI_PREC_SPLIT)
+    return fail(c, GI_ERR_ARG, "unknown precision %d", P.precision);
+
+  std::vector<int> jlist;
+  for (auto& kv : c->bases) jlist.push_back(kv.first);
+  const int jmin = jlist.front(), jmax = jlist.back();
+  for (auto& kv : c->blocks) {
+    auto it = c->bases.find(kv.first.first);
+    if (it == c->bases.end()) return fail(c, GI_ERR_STATE, "block J=%d has no basis", kv.first.first);
+    if (kv.second->nsize != it->second->Ntotal[kv.first.second])
+      return fail(c, GI_ERR_ARG, "block (J=%d, gamma=%d): nsize %d != Ntotal %d", kv.first.first,
+                  kv.first.second, kv.second->nsize, it->second->Ntotal[kv.first.second]);
+  }
+  for (auto& kv : c->bases) {
+    gi_status s = ensure_ycsr(c, *kv.second);
+    if (s != GI_OK) return s;
+  }
+
+  // igamma pairs (trove_functions.cpp:1041-1072)
+  std::vector<int> igamma_pair(nrep);
+  for (int gI = 0; gI < nrep; gI++) {
+    int n = 0;
+    igamma_pair[gI] = gI;
+    for (int gF = 0; gF < nrep; gF++)
+      if (gI != gF && P.isym_pairs[gI] == P.isym_pairs[gF]) {
+        igamma_pair[gI] = gF;
+        if (++n > 1) return fail(c, GI_ERR_ARG, "selection rules do not come in pairs");
+      }
+    if (P.gns[gI] != P.gns[igamma_pair[gI]])
+      return fail(c, GI_ERR_ARG, "selection rules do not agree with gns");
+  }
+
+  // ZPE: while negative, every J=0 Gamma=0 record replaces it (trove_functions.cpp:1200-1201)
+  double zpe = P.ZPE;
+  {
+    auto it = c->blocks.find({0, 0});
+    if (zpe < 0 && c->bases.count(0) && isym_do(c, 0) && it != c->blocks.end())
+      for (double e : it->second->energies)
+        if (zpe < 0) zpe = e;
+  }
+  const double er0 = std::min(P.erange_lower[0], P.erange_upper[0]);
+  const double er1 = std::max(P.erange_lower[1], P.erange_upper[1]);
+  Filters F{c, zpe, jmin, jmax};
+
+  // level table (trove_functions.cpp:1129-1414): filter, then stable sort by energy
+  std::map<std::pair<int, int>, BlockPlan> plans;
+  struct Lv { int J, g, rec; double E; };
+  std::vector<Lv> lv;
+  for (int J : jlist)
+    for (int g = 0; g < nrep; g++) {
+      auto it = c->blocks.find({J, g});
+      if (it == c->blocks.end()) continue;
+      BlockPlan& bp = plans[{J, g}];
+      bp.blk = it->second.get();
+      bp.level_of_rec.assign(bp.blk->nvec, -1);
+      bp.lower_ok.assign(bp.blk->nvec, 0);
+      bp.upper_ok.assign(bp.blk->nvec, 0);
+      if (!isym_do(c, g)) continue;
+      for (int r = 0; r < bp.blk->nvec; r++) {
+        const double E = bp.blk->energies[r];
+        if ((E - zpe) >= er0 && (E - zpe) <= er1) lv.push_back({J, g, r, E});
+      }
+    }
+  std::stable_sort(lv.begin(), lv.end(), [](const Lv& a, const Lv& b) { return a.E < b.E; });
+  c->levels.clear();
+  c->levels.reserve(lv.size());
+  const int nq = P.nmodes + 1;
+  for (size_t l = 0; l < lv.size(); l++) {
+    BlockPlan& bp = plans[{lv[l].J, lv[l].g}];
+    bp.level_of_rec[lv[l].rec] = (int32_t)l;
+    const int32_t* q = bp.blk->quanta.data() + (size_t)lv[l].rec * nq;
+    int krot = 0, taurot = lv[l].J % 2;
+    if (q[0] >= 1) { krot = (q[0] + 1) / 2; taurot = (q[0] + 1) % 2; }
+    c->levels.push_back(Level{lv[l].J, lv[l].g, lv[l].rec, c->degen[lv[l].g], krot, taurot, lv[l].E});
+  }
+  for (auto& kv : plans) {
+    BlockPlan& bp = kv.second;
+    for (int r = 0; r < bp.blk->nvec; r++) {
+      if (bp.level_of_rec[r] < 0) continue;
+      const int32_t* q = bp.blk->quanta.data() + (size_t)r * nq;
+      const double E = bp.blk->energies[r];
+      bp.lower_ok[r] = F.lower(bp.blk->J, E, q);
+      bp.upper_ok[r] = F.upper(bp.blk->J, E, q);
+      if (bp.lower_ok[r]) bp.ivec.push_back(r);
+      if (bp.upper_ok[r]) bp.nupper++;
+    }
+  }
+
+  // 3j table
+  if (!c->threej_user || c->threej_jmax < jmax) {
+    precompute_threej(jmax, c->threej);
+    c->threej_jmax = jmax;
+    c->threej_user = false;
+  }
+
+  // block pairs and their stencils (intensity_filter block-level rules,
+  // trove_functions.cpp:1452-1464)
+  std::vector<PairPlan> pairs;
+  std::vector<StencilTerm> st_all;
+  std::vector<int32_t> stn_all;
+  std::map<std::pair<int, int>, size_t> st_off;
+  for (auto& kv : plans) {
+    BlockPlan& I = kv.second;
+    const int JI = I.blk->J, gI = I.blk->gamma;
+    if (I.ivec.empty() || !(P.gns[gI] > 0.0)) continue;
+    for (int JF = JI - 1; JF <= JI + 1; JF++) {
+      if (!c->bases.count(JF)) continue;
+      if (JI + JF < 1) continue;
+      if (JI == jmin && JF == jmin) continue;
+      const int gF = igamma_pair[gI];
+      if (P.isym_pairs[gI] != P.isym_pairs[gF]) continue;
+      auto fit = plans.find({JF, gF});
+      if (fit == plans.end() || fit->second.nupper == 0) continue;
+      int mask = 0;
+      for (int dF = 0; dF < c->degen[gF]; dF++) {
+        if (P.reduced && dF != 0) continue;
+        for (int dI = 0; dI < c->degen[gI]; dI++)
+          if (degeneracy_ok(c, gI, gF, dI, dF)) mask |= 1 << (dI + 2 * dF);
+      }
+      if (!st_off.count({JI, JF})) {
+        std::vector<StencilTerm> st;
+        std::vector<int32_t> stn;
+        build_stencil(*c->bases[JI], *c->bases[JF], c->threej, c->threej_jmax, st, stn);
+        st_off[{JI, JF}] = stn_all.size();
+        st_all.insert(st_all.end(), st.begin(), st.end());
+        stn_all.insert(stn_all.end(), stn.begin(), stn.end());
+      }
+      pairs.push_back(PairPlan{&I, &fit->second, mask, st_off[{JI, JF}]});
+    }
+  }
+  GI_CUDA(c, c->w_stencil.upload(st_all));
+  GI_CUDA(c, c->w_stencil_n.upload(stn_all));
+
+  Phys ph;
+  const double beta = ph.planck * ph.vellgt / (ph.boltz * P.temperature);
+
+  // capacities
+  size_t cap_total = 0;
+  for (auto& pp : pairs) cap_total += (size_t)pp.I->ivec.size() * pp.F->nupper;
+  c->lines_on_device = (flags & GI_RUN_LINES_ON_DEVICE) != 0;
+
+  // per-block device side arrays (levels, energies, upper flags) - uploaded once
+  std::map<BlockPlan*, std::pair<size_t, size_t>> farr;  // offsets into w_int / w_upper
+  std::vector<int32_t> h_int;
+  std::vector<uint8_t> h_upper;
+  for (auto& kv : plans) {
+    BlockPlan& bp = kv.second;
+    farr[&bp] = {h_int.size(), h_upper.size()};
+    h_int.insert(h_int.end(), bp.level_of_rec.begin(), bp.level_of_rec.end());
+    h_upper.insert(h_upper.end(), bp.upper_ok.begin(), bp.upper_ok.end());
+  }
+  GI_CUDA(c, c->w_int.upload(h_int));
+  GI_CUDA(c, c->w_upper.upload(h_upper));
+  GI_CUDA(c, c->w_counter.reserve(1));
+  GI_CUDA(c, cudaMemsetAsync(c->w_counter.p, 0, sizeof(unsigned long long), c->stream));
+
+  // line buffer: the whole job on the device
+  GI_CUDA(c, c->d_lines.reserve(std::max<size_t>(cap_total, 1)));
+
+  // workspace: per initial block (chunked to the budget)
+  const int N = c->N, Kp = c->Kp;
+  size_t ws_limit = c->budget ? c->budget / 2 : ((size_t)24 << 30);
+  c->stats = gi_stats{};
+  int launches = 0;
+  double fl_half = 0.0, fl_final = 0.0;
+  int64_t npairs_checked = 0;
+
+  GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  std::vector<int32_t> h_ivec, h_lvI;
+  std::vector<double> h_EI;
+  for (auto& kv : plans) {
+    BlockPlan& I = kv.second;
+    std::vector<PairPlan*> mine;
+    for (auto& pp : pairs)
+      if (pp.I == &I) mine.push_back(&pp);
+    if (mine.empty()) continue;
+    const Basis& bI = *c->bases[I.blk->J];
+    const int ndegI = c->degen[I.blk->gamma];
+    const int nslot = bI.nslot;
+    // bytes per initial vector: Y + 3 Z columns, plus H and T of the widest pair
+    size_t per_vec = (size_t)ndegI * nslot * Kp * 8 * 4;
+    for (auto* pp : mine) {
+      const int ndegF = c->degen[pp->F->blk->gamma];
+      per_vec += (size_t)ndegI * ndegF * (pp->F->blk->ld + round_up(pp->F->blk->nvec, 2)) * 8;
+    }
+    int chunk = (int)std::max<size_t>(1, ws_limit / per_vec);
+    chunk = std::min<int>(chunk, (int)I.ivec.size());
+    for (int i0 = 0; i0 < (int)I.ivec.size(); i0 += chunk) {
+      const int nI = std::min(chunk, (int)I.ivec.size() - i0);
+      h_ivec.assign(I.ivec.begin() + i0, I.ivec.begin() + i0 + nI);
+      h_lvI.resize(nI);
+      h_EI.resize(nI);
+      for (int i = 0; i < nI; i++) {
+        h_lvI[i] = I.level_of_rec[h_ivec[i]];
+        h_EI[i] = I.blk->energies[h_ivec[i]];
+      }
+      // small per-chunk tables (synchronous upload keeps the host arrays valid)
+      GI_CUDA(c, cudaStreamSynchronize(c->stream));
+      GI_CUDA(c, c->w_ivec.reserve((size_t)nI * 2));
+      GI_CUDA(c, cudaMemcpy(c->w_ivec.p, h_ivec.data(), sizeof(int32_t) * nI, cudaMemcpyHostToDevice));
+      GI_CUDA(c, cudaMemcpy(c->w_ivec.p + nI, h_lvI.data(), sizeof(int32_t) * nI, cudaMemcpyHostToDevice));
+      GI_CUDA(c, c->w_t.reserve(1));
+      DevArray<double> d_EI;
+      GI_CUDA(c, d_EI.upload(h_EI));
+
+      const int ncolY = nI * ndegI * nslot;
+      GI_CUDA(c, c->w_y.reserve((size_t)ncolY * Kp));
+      GI_CUDA(c, c->w_z.reserve((size_t)3 * ncolY * Kp));
+      GI_CUDA(c, launch_build_y(I.blk->d_vecs.p, I.blk->ld, c->w_ivec.p, nI, ndegI, bI,
+                                I.blk->gamma, c->degen[I.blk->gamma], N, Kp, c->w_y.p, c->stream));
+      launches++;
+      const size_t zc = (size_t)ncolY * Kp;
+      if (P.precision == GI_PREC_SPLIT) {
+        gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, ncolY, &launches);
+        if (s != GI_OK) return s;
+      } else {
+        GI_CUDA(c, gemm_fp64_nt(c->d_mu.p, Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp, zc, N,
+                                ncolY, Kp, 3, c->stream));
+        launches++;
+      }
+      fl_half += 2.0 * 3.0 * N * (double)N * ncolY;
+
+      for (auto* pp : mine) {
+        BlockPlan& Fp = *pp->F;
+        const Block& fb = *Fp.blk;
+        const Basis& bF = *c->bases[fb.J];
+        const int ndegF = c->degen[fb.gamma];
+        const int ldh = fb.ld;
+        const int ncolH = nI * ndegI * ndegF;
+        const int ldt = round_up(fb.nvec, 2);
+        GI_CUDA(c, c->w_h.reserve((size_t)ncolH * ldh));
+        GI_CUDA(c, c->w_t.reserve((size_t)ncolH * ldt));
+        GI_CUDA(c, launch_build_h(c->w_z.p, zc, Kp, nslot, ndegI, nI, bF, fb.gamma, ndegF,
+                                  fb.nsize, ldh, c->w_stencil.p + pp->st_off * 6,
+                                  c->w_stencil_n.p + pp->st_off, 6, c->w_h.p, c->stream));
+        launches++;
+        if (P.precision == GI_PREC_SPLIT) {
+          gi_status s = split_gemm_final(c, fb.d_vecs.p, fb.ld, fb.nvec, c->w_h.p, ldh, ncolH,
+                                         c->w_t.p, ldt, &launches);
+          if (s != GI_OK) return s;
+        } else {
+          GI_CUDA(c, gemm_fp64_nt(fb.d_vecs.p, fb.ld, 0, c->w_h.p, ldh, c->w_t.p, ldt, 0, fb.nvec,
+                                  ncolH, ldh, 1, c->stream));
+          launches++;
+        }
+        fl_final += 2.0 * fb.nsize * (double)fb.nvec * ncolH;
+        EpiParams ep{};
+        ep.jI = I.blk->J;
+        ep.jF = fb.J;
+        ep.ndegI = ndegI;
+        ep.ndegF = ndegF;
+        ep.reduced = P.reduced;
+        ep.combo_mask = pp->combo_mask;
+        ep.gns = P.gns[I.blk->gamma];
+        ep.zpe = zpe;
+        ep.beta = beta;
+        ep.q_stat = P.q_stat;
+        ep.fw0 = P.freq_window[0];
+        ep.fw1 = P.freq_window[1];
+        ep.thresh_S = P.thresh_linestrength;
+        ep.thresh_I = P.thresh_intensity;
+        ep.A_coef = ph.A_coef;
+        ep.intens_cm_mol = ph.intens_cm_mol;
+        ep.avogno = ph.avogno;
+        const auto off = farr[&Fp];
+        GI_CUDA(c, launch_epilogue(c->w_t.p, ldt, nI, fb.nvec, c->w_ivec.p + nI, d_EI.p,
+                                   c->w_int.p + off.first, fb.d_energies.p, c->w_upper.p + off.second,
+                                   ep, c->d_lines.p, c->w_counter.p, (long long)c->d_lines.n,
+                                   c->stream));
+        launches++;
+        npairs_checked += (int64_t)nI * Fp.nupper;
+      }
+    }
+  }
+  GI_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  unsigned long long count = 0;
+  GI_CUDA(c, cudaMemcpyAsync(&count, c->w_counter.p, sizeof(count), cudaMemcpyDeviceToHost, c->stream));
+  GI_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (count > c->d_lines.n) return fail(c, GI_ERR_DEVICE, "line buffer overflow (%llu lines)", count);
+  c->nlines = (int64_t)count;
+  if (!c->lines_on_device) {
+    c->lines.resize(count);
+    if (count)
+      GI_CUDA(c, cudaMemcpy(c->lines.data(), c->d_lines.p, sizeof(gi_line) * count, cudaMemcpyDeviceToHost));
+  }
+  float ms = 0.f;
+  GI_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  c->stats.nlines = c->nlines;
+  c->stats.npairs_checked = npairs_checked;
+  c->stats.nblock_pairs = (int32_t)pairs.size();
+  c->stats.nlevels = (int32_t)c->levels.size();
+  c->stats.zpe = zpe;
+  c->stats.seconds_gpu = ms * 1e-3;
+  c->stats.flops_halfls = fl_half;
+  c->stats.flops_final = fl_final;
+  c->stats.kernel_launches = launches;
+  c->stats.seconds_total =
+      std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+  *nlines_out = c->nlines;
+  return GI_OK;
+}
+
+}  // namespace gi
+
+// ====================================================================== C ABI
+using namespace gi;
+
+extern "C" {
+
+const char* gi_status_string(gi_status s) {
+  switch (s) {
+    case GI_OK: return "ok";
+    case GI_ERR_ARG: return "invalid argument";
+    case GI_ERR_CUDA: return "CUDA error";
+    case GI_ERR_NOMEM: return "out of memory";
+    case GI_ERR_STATE: return "call out of order";
+    case GI_ERR_BUDGET: return "over the HBM budget";
+    case GI_ERR_NOTFOUND: return "not found";
+    case GI_ERR_DEVICE: return "device-side check failed";
+  }
+  return "unknown status";
+}
+
+gi_status gi_create(gi_ctx** out, int device, size_t hbm_budget_bytes) {
+  if (!out) return GI_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GI_ERR_CUDA;
+  if (device < 0 || device >= ndev) return GI_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return GI_ERR_CUDA;
+  Ctx* c = new Ctx();
+  c->device = device;
+  c->budget = hbm_budget_bytes;
+  cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    delete c;
+    return GI_ERR_CUDA;
+  }
+  *out = reinterpret_cast<gi_ctx*>(c);
+  return GI_OK;
+}
+
+gi_status gi_destroy(gi_ctx* h) {
+  if (!h) return GI_OK;
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  split_release(c);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return GI_OK;
+}
+
+const char* gi_last_error(const gi_ctx* h) {
+  return h ? reinterpret_cast<const Ctx*>(h)->err.c_str() : "null context";
+}
+
+gi_status gi_set_symmetry(gi_ctx* h, int sym_type) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return GI_ERR_ARG;
+  switch (sym_type) {
+    case 1: c->degen = {1, 1, 1, 1}; break;
+    case 2: c->degen = {1, 1, 2}; break;
+    case 3: c->degen = {1, 1, 2, 1, 1, 2}; break;
+    default: return fail(c, GI_ERR_ARG, "symmetry %d not implemented", sym_type);
+  }
+  if (!c->bases.empty() && (int)c->degen.size() != c->nrep)
+    return fail(c, GI_ERR_STATE, "symmetry changed after bases were set");
+  c->sym_type = sym_type;
+  c->nrep = (int)c->degen.size();
+  return GI_OK;
+}
+
+gi_status gi_set_params(gi_ctx* h, const gi_params* p) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !p) return GI_ERR_ARG;
+  if (p->nmodes < 0 || p->nmodes > GI_MAX_MODES) return fail(c, GI_ERR_ARG, "nmodes out of range");
+  if (!(p->temperature > 0.0)) return fail(c, GI_ERR_ARG, "temperature must be positive");
+  c->params = *p;
+  c->have_params = true;
+  return GI_OK;
+}
+
+gi_status gi_set_dipole(gi_ctx* h, int N, const double* mu) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || N <= 0 || !mu) return GI_ERR_ARG;
+  cudaSetDevice(c->device);
+  const int Kp = round_up(N, 64);
+  std::vector<double> hbuf((size_t)3 * N * Kp, 0.0);
+  for (int comp = 0; comp < 3; comp++)
+    for (int f = 0; f < N; f++)
+      std::memcpy(&hbuf[((size_t)comp * N + f) * Kp], mu + (size_t)comp * N * N + (size_t)f * N,
+                  sizeof(double) * N);
+  GI_CUDA(c, c->d_mu.upload(hbuf));
+  c->N = N;
+  c->Kp = Kp;
+  split_invalidate(c);
+  return GI_OK;
+}
+
+gi_status gi_set_basis(gi_ctx* h, int J, int D, int ncase, int max_deg_size, int mat_size,
+                       const int32_t* icontr2icase, const int32_t* iroot_correlat_j0,
+                       const int32_t* k, const int32_t* ktau, const int32_t* Nsym,
+                       const int32_t* Ntotal, const double* const* repres) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return GI_ERR_ARG;
+  if (c->nrep == 0) return fail(c, GI_ERR_STATE, "gi_set_symmetry must precede gi_set_basis");
+  if (J < 0 || D <= 0 || ncase <= 0 || mat_size <= 0 || !icontr2icase || !iroot_correlat_j0 ||
+      !k || !ktau || !Nsym || !Ntotal || !repres)
+    return fail(c, GI_ERR_ARG, "gi_set_basis: bad arguments for J=%d", J);
+  cudaSetDevice(c->device);
+  auto b = std::make_unique<Basis>();
+  b->J = J;
+  b->D = D;
+  b->ncase = ncase;
+  b->max_deg = max_deg_size;
+  b->mat_size = mat_size;
+  b->icontr2icase.assign(icontr2icase, icontr2icase + 2 * (size_t)D);
+  b->iroot.assign(iroot_correlat_j0, iroot_correlat_j0 + D);
+  b->k.assign(k, k + D);
+  b->ktau.assign(ktau, ktau + D);
+  b->Nsym.assign(Nsym, Nsym + (size_t)c->nrep * ncase);
+  b->Ntotal.assign(Ntotal, Ntotal + c->nrep);
+  for (int g = 0; g < c->nrep; g++) {
+    const size_t n = (size_t)std::max(Ntotal[g], 0) * c->degen[g] * mat_size;
+    if (n && !repres[g]) return fail(c, GI_ERR_ARG, "repres[%d] missing", g);
+    b->repres.emplace_back(repres[g], repres[g] + n);
+  }
+  gi_status s = derive_basis(c, *b);
+  if (s != GI_OK) return s;
+  c->bases[J] = std::move(b);
+  return GI_OK;
+}
+
+gi_status gi_set_threej(gi_ctx* h, int jmax, const double* threej) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || jmax < 0 || !threej) return GI_ERR_ARG;
+  c->threej.assign(threej, threej + (size_t)(jmax + 1) * (jmax + 1) * 9);
+  c->threej_jmax = jmax;
+  c->threej_user = true;
+  return GI_OK;
+}
+
+gi_status gi_set_block(gi_ctx* h, int J, int gamma, int nsize, int nvec, const double* vecs,
+                       const double* energies, const int32_t* quanta) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return GI_ERR_ARG;
+  if (!c->have_params) return fail(c, GI_ERR_STATE, "gi_set_params must precede gi_set_block");
+  if (gamma < 0 || gamma >= c->nrep || nsize < 0 || nvec < 0 || (nsize == 0 && nvec > 0) ||
+      (nvec > 0 && (!vecs || !energies || !quanta)))
+    return fail(c, GI_ERR_ARG, "gi_set_block: bad arguments for (J=%d, gamma=%d)", J, gamma);
+  cudaSetDevice(c->device);
+  auto b = std::make_unique<Block>();
+  b->J = J;
+  b->gamma = gamma;
+  b->nsize = nsize;
+  b->nvec = nvec;
+  b->ld = round_up(nsize, 64);
+  b->energies.assign(energies, energies + nvec);
+  const int nq = c->params.nmodes + 1;
+  b->quanta.assign(quanta, quanta + (size_t)nvec * nq);
+  GI_CUDA(c, b->d_vecs.alloc((size_t)std::max(nvec, 1) * b->ld));
+  GI_CUDA(c, cudaMemset(b->d_vecs.p, 0, sizeof(double) * b->d_vecs.n));
+  if (nvec)
+    GI_CUDA(c, cudaMemcpy2D(b->d_vecs.p, sizeof(double) * b->ld, vecs, sizeof(double) * nsize,
+                            sizeof(double) * nsize, nvec, cudaMemcpyHostToDevice));
+  GI_CUDA(c, b->d_energies.upload(b->energies));
+  c->blocks[{J, gamma}] = std::move(b);
+  return GI_OK;
+}
+
+gi_status gi_run(gi_ctx* h, int flags, int64_t* nlines) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !nlines) return GI_ERR_ARG;
+  cudaSetDevice(c->device);
+  c->err.clear();
+  return run_job(c, flags, nlines);
+}
+
+gi_status gi_get_lines(gi_ctx* h, int64_t offset, int64_t count, gi_line* out) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || offset < 0 || count < 0 || (count && !out)) return GI_ERR_ARG;
+  if (offset + count > c->nlines) return fail(c, GI_ERR_ARG, "line range past the end");
+  if (!count) return GI_OK;
+  if (c->lines_on_device) {
+    GI_CUDA(c, cudaMemcpy(out, c->d_lines.p + offset, sizeof(gi_line) * count, cudaMemcpyDeviceToHost));
+  } else {
+    std::memcpy(out, c->lines.data() + offset, sizeof(gi_line) * count);
+  }
+  return GI_OK;
+}
+
+gi_status gi_num_levels(gi_ctx* h, int32_t* n) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !n) return GI_ERR_ARG;
+  *n = (int32_t)c->levels.size();
+  return GI_OK;
+}
+
+gi_status gi_get_levels(gi_ctx* h, int32_t cap, gi_level* out) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || cap < 0 || (cap && !out)) return GI_ERR_ARG;
+  const int n = std::min<int>(cap, (int)c->levels.size());
+  for (int i = 0; i < n; i++) {
+    const Level& l = c->levels[i];
+    out[i] = gi_level{l.J, l.gamma, l.rec, l.ndeg, l.krot, l.taurot, l.energy};
+  }
+  return GI_OK;
+}
+
+gi_status gi_get_stats(gi_ctx* h, gi_stats* out) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !out) return GI_ERR_ARG;
+  *out = c->stats;
+  return GI_OK;
+}
+
+gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const double* vsym,
+                     double* half_ls) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || !vsym || !half_ls) return GI_ERR_ARG;
+  if (c->N == 0) return fail(c, GI_ERR_STATE, "gi_set_dipole not called");
+  auto iI = c->bases.find(jI), iF = c->bases.find(jF);
+  if (iI == c->bases.end() || iF == c->bases.end()) return fail(c, GI_ERR_NOTFOUND, "no basis for J");
+  if (gammaI < 0 || gammaI >= c->nrep || ideg < 0 || ideg >= c->degen[gammaI])
+    return fail(c, GI_ERR_ARG, "bad gamma/ideg");
+  if (std::abs(jI - jF) > 1) return fail(c, GI_ERR_ARG, "|jI - jF| > 1");
+  cudaSetDevice(c->device);
+  Basis& bI = *iI->second;
+  Basis& bF = *iF->second;
+  gi_status s = ensure_ycsr(c, bI);
+  if (s != GI_OK) return s;
+  s = ensure_ycsr(c, bF);
+  if (s != GI_OK) return s;
+  const int jmax = std::max(jI, jF);
+  if (c->threej_jmax < jmax) {
+    precompute_threej(jmax, c->threej);
+    c->threej_jmax = jmax;
+    c->threej_user = false;
+  }
+  std::vector<StencilTerm> st;
+  std::vector<int32_t> stn;
+  build_stencil(bI, bF, c->threej, c->threej_jmax, st, stn);
+  const int nsize = bI.Ntotal[gammaI], ld = round_up(nsize, 64), ndeg = c->degen[gammaI];
+  DevArray<double> v, y, z, hh;
+  DevArray<int32_t> iv;
+  DevArray<StencilTerm> dst;
+  DevArray<int32_t> dstn;
+  int32_t zero = 0;
+  GI_CUDA(c, v.alloc(ld));
+  GI_CUDA(c, cudaMemset(v.p, 0, sizeof(double) * ld));
+  GI_CUDA(c, cudaMemcpy(v.p, vsym, sizeof(double) * nsize, cudaMemcpyHostToDevice));
+  GI_CUDA(c, iv.upload(&zero, 1));
+  GI_CUDA(c, dst.upload(st));
+  GI_CUDA(c, dstn.upload(stn));
+  const int ncol = ndeg * bI.nslot;
+  GI_CUDA(c, y.alloc((size_t)ncol * c->Kp));
+  GI_CUDA(c, z.alloc((size_t)3 * ncol * c->Kp));
+  GI_CUDA(c, hh.alloc(bF.D));
+  GI_CUDA(c, launch_build_y(v.p, ld, iv.p, 1, ndeg, bI, gammaI, ndeg, c->N, c->Kp, y.p, c->stream));
+  const size_t zc = (size_t)ncol * c->Kp;
+  GI_CUDA(c, gemm_fp64_nt(c->d_mu.p, c->Kp, (size_t)c->N * c->Kp, y.p, c->Kp, z.p, c->Kp, zc, c->N,
+                          ncol, c->Kp, 3, c->stream));
+  GI_CUDA(c, launch_half_ls_prim(z.p + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF, dst.p,
+                                 dstn.p, 6, hh.p, c->stream));
+  GI_CUDA(c, cudaStreamSynchronize(c->stream));
+  GI_CUDA(c, cudaMemcpy(half_ls, hh.p, sizeof(double) * bF.D, cudaMemcpyDeviceToHost));
+  return GI_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,323 @@
+// Gather/scatter, stencil, epilogue and FP64 DMMA GEMM kernels of the
+// line-intensity engine (sm_103a).
+//
+// Factorisation of the reference's half line strength
+// (dipole_kernals.cu:162-227).  With keyI = 2kI+tauI, the reference sums
+//   h[rF] = sgnF * sum_rI [|kI-kF|<=1] R(keyI,keyF) * mu_c(icontrI, icontrF) * vI[rI]
+// where R (sign, L, 3j, 1/sqrt2) and the component c depend only on the two
+// keys.  Grouping the initial roots by key gives
+//   Y[slotI][v] = sum_{rI: key=slotI, icontrI=v} vI[rI]            (k_build_y)
+//   Z_c[slotI][f] = sum_v mu_c(v, f) Y[slotI][v]                    (a GEMM)
+//   h[rF] = sum_{terms of keyF} coef * Z_c[slotI][icontrF(rF)]      (k_build_h)
+// and the reference's per-final-vector correlate + Ddot (cuda_host.cu:1301-1317)
+// becomes a GEMM against H projected back onto the symmetrised basis:
+//   H[s] = sum_lambda repres_F[s, idegF, lambda] * h[root(case(s), lambda)].
+#include <cuda_runtime.h>
+
+#include "engine.h"
+
+namespace gi {
+
+// ------------------------------------------------------------------ Y build
+// One thread per (slot, v) element of one column (i, d).  Fuses the
+// symmetrised -> primitive transform (dipole_kernals.cu:38-71) with the
+// scatter of primitive roots onto their (key, J=0 index) position.
+__global__ void k_build_y(const double* __restrict__ vecs, int ld, const int32_t* __restrict__ ivec,
+                          int ndeg, const int32_t* __restrict__ yptr,
+                          const int32_t* __restrict__ yroot, const int32_t* __restrict__ root_case,
+                          const int32_t* __restrict__ root_lam,
+                          const int32_t* __restrict__ case_iterm,
+                          const int32_t* __restrict__ case_nelem, const double* __restrict__ rep,
+                          int Ntot, int degen, int nslot, int N, int Kp, double* __restrict__ Y) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const int col = blockIdx.y;  // i * ndeg + d
+  const int i = col / ndeg, d = col - i * ndeg;
+  if (e >= nslot * Kp) return;
+  const int slot = e / Kp, v = e - slot * Kp;
+  double acc = 0.0;
+  if (v < N) {
+    const double* vs = vecs + (size_t)ivec[i] * ld;
+    const int q = slot * N + v;
+    for (int p = yptr[q]; p < yptr[q + 1]; ++p) {
+      const int r = yroot[p];
+      const int c = root_case[r], lam = root_lam[r];
+      const int it = case_iterm[c], ne = case_nelem[c];
+      const double* rr = rep + (size_t)d * Ntot + (size_t)lam * degen * Ntot;
+      for (int j = 0; j < ne; ++j) acc = fma(vs[it + j], rr[it + j], acc);
+    }
+  }
+  Y[((size_t)col * nslot + slot) * Kp + v] = acc;
+}
+
+cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int nI, int ndeg,
+                           const Basis& b, int gamma, int degen, int N, int Kp, double* Y,
+                           cudaStream_t s) {
+  if (nI == 0) return cudaSuccess;
+  dim3 grid((b.nslot * Kp + 255) / 256, nI * ndeg);
+  k_build_y<<<grid, 256, 0, s>>>(vecs, ld, ivec, ndeg, b.d_yptr.p, b.d_yroot.p, b.d_root_case.p,
+                                 b.d_root_lam.p, b.d_case_iterm[gamma].p,
+                                 b.d_case_nelem[gamma].p, b.d_rep[gamma].p, b.Ntotal[gamma],
+                                 degen, b.nslot, N, Kp, Y);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ H build
+// One thread per symmetrised final function s of one initial column (i, dI);
+// writes H for every final degenerate component dF.
+template <int NDEGF>
+__global__ void k_build_h(const double* __restrict__ Z, size_t zc, int ldz, int nslotI, int ndegI,
+                          const int32_t* __restrict__ s_case, const int32_t* __restrict__ case_ptr,
+                          const int32_t* __restrict__ case_roots,
+                          const int32_t* __restrict__ root_v, const int32_t* __restrict__ root_key,
+                          const int32_t* __restrict__ root_lam, const double* __restrict__ rep,
+                          int Ntot, const StencilTerm* __restrict__ st,
+                          const int32_t* __restrict__ st_n, int st_max, int nsizeF, int ldh,
+                          double* __restrict__ H) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int colI = blockIdx.y;  // i * ndegI + dI
+  if (s >= ldh) return;
+  double acc[NDEGF];
+#pragma unroll
+  for (int d = 0; d < NDEGF; ++d) acc[d] = 0.0;
+  if (s < nsizeF) {
+    const double* zcol = Z + (size_t)colI * nslotI * ldz;
+    const int cs = s_case[s];
+    for (int p = case_ptr[cs]; p < case_ptr[cs + 1]; ++p) {
+      const int r = case_roots[p];
+      const int v = root_v[r], key = root_key[r], lam = root_lam[r];
+      double h = 0.0;
+      const int nt = st_n[key];
+      for (int t = 0; t < nt; ++t) {
+        const StencilTerm term = st[key * st_max + t];
+        h = fma(term.coef, zcol[(size_t)term.c * zc + (size_t)term.slotI * ldz + v], h);
+      }
+#pragma unroll
+      for (int d = 0; d < NDEGF; ++d)
+        acc[d] = fma(rep[s + (size_t)d * Ntot + (size_t)lam * NDEGF * Ntot], h, acc[d]);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < NDEGF; ++d) H[((size_t)colI * NDEGF + d) * ldh + s] = acc[d];
+}
+
+cudaError_t launch_build_h(const double* Z, size_t zstride_c, int ldz, int nslotI, int ndegI,
+                           int nI, const Basis& bF, int gammaF, int degF, int nsizeF, int ldh,
+                           const StencilTerm* st, const int32_t* st_n, int st_max, double* H,
+                           cudaStream_t s) {
+  if (nI == 0) return cudaSuccess;
+  dim3 grid((ldh + 255) / 256, nI * ndegI);
+  if (degF == 1)
+    k_build_h<1><<<grid, 256, 0, s>>>(Z, zstride_c, ldz, nslotI, ndegI, bF.d_s_case[gammaF].p,
+                                      bF.d_case_ptr.p, bF.d_case_roots.p, bF.d_root_v.p,
+                                      bF.d_root_key.p, bF.d_root_lam.p, bF.d_rep[gammaF].p,
+                                      bF.Ntotal[gammaF], st, st_n, st_max, nsizeF, ldh, H);
+  else if (degF == 2)
+    k_build_h<2><<<grid, 256, 0, s>>>(Z, zstride_c, ldz, nslotI, ndegI, bF.d_s_case[gammaF].p,
+                                      bF.d_case_ptr.p, bF.d_case_roots.p, bF.d_root_v.p,
+                                      bF.d_root_key.p, bF.d_root_lam.p, bF.d_rep[gammaF].p,
+                                      bF.Ntotal[gammaF], st, st_n, st_max, nsizeF, ldh, H);
+  else
+    return cudaErrorInvalidValue;
+  return cudaGetLastError();
+}
+
+// Primitive-space half line strength of one column (the reference's half_ls
+// buffer, dipole_kernals.cu:223-224).
+__global__ void k_half_ls_prim(const double* __restrict__ Z, size_t zc, int ldz,
+                               const int32_t* __restrict__ root_v,
+                               const int32_t* __restrict__ root_key,
+                               const StencilTerm* __restrict__ st, const int32_t* __restrict__ st_n,
+                               int st_max, int D, double* __restrict__ h) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= D) return;
+  const int v = root_v[r], key = root_key[r];
+  double acc = 0.0;
+  for (int t = 0; t < st_n[key]; ++t) {
+    const StencilTerm term = st[key * st_max + t];
+    acc = fma(term.coef, Z[(size_t)term.c * zc + (size_t)term.slotI * ldz + v], acc);
+  }
+  h[r] = acc;
+}
+
+cudaError_t launch_half_ls_prim(const double* Z, size_t zstride_c, int ldz, const Basis& bF,
+                                const StencilTerm* st, const int32_t* st_n, int st_max,
+                                double* h, cudaStream_t s) {
+  k_half_ls_prim<<<(bF.D + 255) / 256, 256, 0, s>>>(Z, zstride_c, ldz, bF.d_root_v.p,
+                                                    bF.d_root_key.p, st, st_n, st_max, bF.D, h);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ epilogue
+// Degeneracy sum, S, A_if, I(T), frequency window and thresholds
+// (cuda_host.cu:1376-1408), then a warp-aggregated append of kept lines.
+__global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF,
+                           const int32_t* __restrict__ levelI, const double* __restrict__ EI,
+                           const int32_t* __restrict__ levelF, const double* __restrict__ EF,
+                           const uint8_t* __restrict__ upper_ok, EpiParams p,
+                           gi_line* __restrict__ out, unsigned long long* counter,
+                           long long cap) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = blockIdx.y;
+  bool keep = false;
+  gi_line L;
+  if (f < nF && upper_ok[f]) {
+    const double ei = EI[i], ef = EF[f];
+    const double nu = ef - ei;
+    if (nu >= p.fw0 && nu <= p.fw1) {
+      double t[4] = {0.0, 0.0, 0.0, 0.0};
+      for (int dF = 0; dF < p.ndegF; ++dF)
+        for (int dI = 0; dI < p.ndegI; ++dI)
+          if (p.combo_mask & (1 << (dI + 2 * dF)))
+            t[dI + 2 * dF] = T[((size_t)(i * p.ndegI + dI) * p.ndegF + dF) * ldt + f];
+      double ls = 0.0;
+      for (int dF = 0; dF < p.ndegF; ++dF)
+        for (int dI = 0; dI < p.ndegI; ++dI) ls += t[dI + 2 * dF] * t[dI + 2 * dF];
+      ls /= (double)p.ndegI;
+      if (p.reduced && p.ndegF != 1 && p.ndegI != 1) ls *= (double)p.ndegI;
+      const double anu = fabs(nu);
+      const double boltz_fc =
+          anu * exp(-(ei - p.zpe) * p.beta) * (1.0 - exp(-anu * p.beta)) / p.q_stat;
+      const double A = p.A_coef * (double)(2 * p.jI + 1) * ls * (anu * anu * anu);
+      const double S = ls * p.gns * (double)((2 * p.jI + 1) * (2 * p.jF + 1));
+      const double In = S * p.intens_cm_mol * boltz_fc;
+      keep = (S >= p.thresh_S) && (In / p.avogno >= p.thresh_I);
+      L.level_i = levelI[i];
+      L.level_f = levelF[f];
+      L.ndeg_i = p.ndegI;
+      L.ndeg_f = p.ndegF;
+      L.nu = nu;
+      L.S = S;
+      L.A = A;
+      L.I = In;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) L.t[q] = t[q];
+    }
+  }
+  const unsigned mask = __ballot_sync(0xffffffffu, keep);
+  if (mask == 0) return;
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  unsigned long long base = 0;
+  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (keep) {
+    const unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
+    if ((long long)pos < cap) out[pos] = L;
+  }
+}
+
+cudaError_t launch_epilogue(const double* T, int ldt, int nI, int nF, const int32_t* levelI,
+                            const double* EI, const int32_t* levelF, const double* EF,
+                            const uint8_t* upper_ok, const EpiParams& p, gi_line* out,
+                            unsigned long long* counter, long long cap, cudaStream_t s) {
+  if (nI == 0 || nF == 0) return cudaSuccess;
+  dim3 grid((nF + 127) / 128, nI);
+  k_epilogue<<<grid, 128, 0, s>>>(T, ldt, nI, nF, levelI, EI, levelF, EF, upper_ok, p, out,
+                                  counter, cap);
+  return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ FP64 GEMM
+// C[z][n*ldc + m] = sum_k A[z][m*lda + k] * B[n*ldb + k] on the FP64 tensor
+// pipe (mma.sync m8n8k4 .f64).  64x64 tile, 4 warps of 32x32, K step 16,
+// cp.async double buffering.  K is a multiple of 16 and lda/ldb are even
+// (the engine pads every K dimension), so each 16-byte copy is aligned.
+namespace {
+constexpr int GBM = 64, GBN = 64, GBK = 16, GPAD = 2;
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, bool valid) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  const int n = valid ? 16 : 0;
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(gmem), "r"(n));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+}  // namespace
+
+__global__ void __launch_bounds__(128)
+    k_gemm_fp64_nt(const double* __restrict__ A, int lda, size_t strideA,
+                   const double* __restrict__ B, int ldb, double* __restrict__ C, int ldc,
+                   size_t strideC, int M, int Nc, int K) {
+  __shared__ __align__(16) double As[2][GBM][GBK + GPAD];
+  __shared__ __align__(16) double Bs[2][GBN][GBK + GPAD];
+  A += (size_t)blockIdx.z * strideA;
+  C += (size_t)blockIdx.z * strideC;
+  const int m0 = blockIdx.y * GBM, n0 = blockIdx.x * GBN;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+  const int g = lane >> 2, tq = lane & 3;
+
+  double acc[4][4][2];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b][0] = acc[a][b][1] = 0.0;
+
+  auto load = [&](int st, int k0) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int q = tid + 128 * j;
+      const int row = q >> 3, cp = (q & 7) * 2;
+      const int am = m0 + row, bn = n0 + row;
+      const bool va = am < M, vb = bn < Nc;
+      cp_async16(&As[st][row][cp], A + (size_t)(va ? am : 0) * lda + k0 + cp, va);
+      cp_async16(&Bs[st][row][cp], B + (size_t)(vb ? bn : 0) * ldb + k0 + cp, vb);
+    }
+    cp_async_commit();
+  };
+
+  const int nk = K / GBK;
+  load(0, 0);
+  for (int kt = 0; kt < nk; ++kt) {
+    const int st = kt & 1;
+    if (kt + 1 < nk) {
+      load(st ^ 1, (kt + 1) * GBK);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < GBK; kk += 4) {
+      double af[4], bf[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) af[a] = As[st][wm + a * 8 + g][kk + tq];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) bf[b] = Bs[st][wn + b * 8 + g][kk + tq];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+          asm volatile(
+              "mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};\n"
+              : "+d"(acc[a][b][0]), "+d"(acc[a][b][1])
+              : "d"(af[a]), "d"(bf[b]));
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+#pragma unroll
+      for (int e = 0; e < 2; ++e) {
+        const int m = m0 + wm + a * 8 + g;
+        const int n = n0 + wn + b * 8 + tq * 2 + e;
+        if (m < M && n < Nc) C[(size_t)n * ldc + m] = acc[a][b][e];
+      }
+}
+
+cudaError_t gemm_fp64_nt(const double* A, int lda, size_t strideA, const double* B, int ldb,
+                         double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch,
+                         cudaStream_t s) {
+  if (M <= 0 || Nc <= 0 || batch <= 0) return cudaSuccess;
+  if (K <= 0 || K % GBK != 0 || (lda & 1) || (ldb & 1)) return cudaErrorInvalidValue;
+  dim3 grid((Nc + GBN - 1) / GBN, (M + GBM - 1) / GBM, batch);
+  k_gemm_fp64_nt<<<grid, 128, 0, s>>>(A, lda, strideA, B, ldb, C, ldc, strideC, M, Nc, K);
+  return cudaGetLastError();
+}
+
+}  // namespace gi

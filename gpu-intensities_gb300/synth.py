@@ -405,3 +405,56 @@ def workload(name: str, seed: int = 1, **kw) -> Problem:
     if name == "c3v_small":
         return make_c3v(seed, kw.pop("N", 60), kw.pop("jlist", [0, 1, 2, 3]), name=name, **kw)
     raise KeyError(name)
+
+
+# ---------------------------------------------------------------- persistence
+def save(prob: Problem, path: str) -> None:
+    """Write a Problem to one .npz file (no pickling)."""
+    d = {"sym_type": prob.sym_type, "N": prob.N, "mu": prob.mu, "name": prob.name}
+    p = prob.params
+    for f in dataclasses.fields(Params):
+        v = getattr(p, f.name)
+        if v is not None:
+            d["param_" + f.name] = np.asarray(v)
+    for J, b in prob.bases.items():
+        for f in dataclasses.fields(Basis):
+            if f.name == "repres":
+                for g, r in enumerate(b.repres):
+                    d[f"basis{J}_repres{g}"] = r
+            else:
+                d[f"basis{J}_{f.name}"] = np.asarray(getattr(b, f.name))
+    for (J, g), b in prob.blocks.items():
+        d[f"block{J}_{g}_vecs"] = b.vecs
+        d[f"block{J}_{g}_energies"] = b.energies
+        d[f"block{J}_{g}_quanta"] = b.quanta
+    np.savez_compressed(path, **d)
+
+
+def load(path: str) -> Problem:
+    z = np.load(path)
+    sym = int(z["sym_type"])
+    nrep = len(SYM_INFO[sym]["degen"])
+    kw = {}
+    for f in dataclasses.fields(Params):
+        key = "param_" + f.name
+        if key in z:
+            v = z[key]
+            kw[f.name] = (tuple(v.tolist()) if v.ndim == 1 else v) if v.ndim else v.item()
+    params = Params(**kw)
+    bases, blocks = {}, {}
+    Js = sorted({int(k[5:].split("_")[0]) for k in z.files if k.startswith("basis")})
+    for J in Js:
+        vals = {}
+        for f in dataclasses.fields(Basis):
+            if f.name == "repres":
+                vals["repres"] = [z[f"basis{J}_repres{g}"] for g in range(nrep)]
+            else:
+                a = z[f"basis{J}_{f.name}"]
+                vals[f.name] = int(a) if a.ndim == 0 else a
+        bases[J] = Basis(**vals)
+    for k in z.files:
+        if k.startswith("block") and k.endswith("_vecs"):
+            J, g = map(int, k[5:-5].split("_"))
+            blocks[(J, g)] = Block(J, g, z[k], z[f"block{J}_{g}_energies"],
+                                   z[f"block{J}_{g}_quanta"])
+    return Problem(sym, int(z["N"]), z["mu"], bases, blocks, params, name=str(z["name"]))

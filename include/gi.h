@@ -1,0 +1,176 @@
+/*
+ * gi.h - C ABI of the GB300 line-intensity engine.
+ *
+ * One context drives one GPU.  The caller hands over the same inputs the
+ * reference reads from TROVE checkpoints (vibrational dipole, per-J basis
+ * tables, per-(J,Gamma) eigenvector blocks with energies and quanta) and the
+ * parameters of its input deck; the engine returns the same lines (S, A_if,
+ * I(T) and the transition moments) after the same filters.
+ *
+ * Conventions
+ *   - Every call returns a gi_status; nothing exits the process.  The text of
+ *     the last failure is available from gi_last_error().
+ *   - All buffers are caller-owned; setters copy what they need (to device
+ *     memory) before returning, so the caller may free its arrays afterwards.
+ *   - A context is used from one host thread at a time.
+ *   - Indices are 0-based unless stated.  Symmetry indices gamma follow the
+ *     reference's order for the group (e.g. C2V(M): A1, A2, B1, B2).
+ *
+ * Reference interfaces replaced (file:line in the reference project):
+ *   gi_create/gi_destroy   dipole_initialise_gpu + device teardown
+ *                          (cuda_host.cu:900-993, 1501-1503)
+ *   gi_set_symmetry        read_symmetry (fields.cpp:11-115)
+ *   gi_set_params          read_intensities / read_fields (fields.cpp:145-282)
+ *   gi_set_dipole          read_dipole_flipped + its upload
+ *                          (trove_functions.cpp:113-205, cuda_host.cu:983)
+ *   gi_set_basis           bset_contr_factory + correlate_index +
+ *                          compute_ijterms + copy_bset_contr_to_gpu
+ *                          (trove_functions.cpp:401-858, 927-966; cuda_host.cu:186-366)
+ *   gi_set_threej          precompute_threej + copy_threej_to_gpu
+ *                          (trove_functions.cpp:899-925; cuda_host.cu:379-383)
+ *   gi_set_block           read_eigenvalues + the eigenvector fread/H2D
+ *                          (trove_functions.cpp:1075-1429; cuda_host.cu:1196-1199, 1262-1273)
+ *   gi_run                 dipole_do_intensities_async_omp
+ *                          (cuda_host.cu:995-1506; declared cuda_host.cuh:19)
+ *   gi_half_ls             do_1st_half_ls: device_correlate_vectors +
+ *                          device_compute_1st_half_ls_flipped_dipole
+ *                          (cuda_host.cu:767-780; dipole_kernals.cu:38-71, 162-227)
+ *   gi_line / gi_level     the printed line and level record
+ *                          (cuda_host.cu:1444-1473; trove_objects.h:113-127)
+ */
+#ifndef GI_H
+#define GI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  GI_OK = 0,
+  GI_ERR_ARG = 1,       /* invalid argument or inconsistent tables */
+  GI_ERR_CUDA = 2,      /* CUDA runtime or kernel error */
+  GI_ERR_NOMEM = 3,     /* device or pinned host allocation failed */
+  GI_ERR_STATE = 4,     /* call out of order (e.g. run before inputs) */
+  GI_ERR_BUDGET = 5,    /* the job does not fit the context's HBM budget */
+  GI_ERR_NOTFOUND = 6,  /* unknown J / block / job id */
+  GI_ERR_DEVICE = 7     /* a device-side check failed (status read back) */
+} gi_status;
+
+typedef enum { GI_PREC_FP64 = 0, GI_PREC_SPLIT = 1 } gi_precision;
+
+typedef struct gi_ctx gi_ctx;
+
+#define GI_MAX_REP 8
+#define GI_MAX_MODES 16
+
+/* The INTENSITY block of the reference's input deck (fields.h:176-210). */
+typedef struct {
+  double temperature;      /* K */
+  double q_stat;           /* partition function */
+  double ZPE;              /* cm^-1; < 0: the first J=0, Gamma=0 record energy */
+  double erange_lower[2];  /* E-ZPE window of initial levels */
+  double erange_upper[2];  /* E-ZPE window of final levels */
+  double freq_window[2];   /* nu = E_F - E_I window */
+  double gns[GI_MAX_REP];  /* nuclear-spin weights; <= 1e-8 disables the symmetry */
+  int32_t isym_pairs[GI_MAX_REP]; /* SELECTION */
+  int32_t nmodes;
+  int32_t quanta_lower[2][GI_MAX_MODES]; /* [0]=min, [1]=max of quanta[1..nmodes] */
+  int32_t quanta_upper[2][GI_MAX_MODES];
+  int32_t reduced;         /* SYMMETRY REDUCED */
+  int32_t precision;       /* gi_precision */
+  int32_t split_slices;    /* bf16 slices per FP64 operand in GI_PREC_SPLIT (0: default) */
+  int32_t reserved;
+  double thresh_linestrength; /* keep lines with S >= this (Debye^2) */
+  double thresh_intensity;    /* keep lines with I >= this (cm/molecule) */
+} gi_params;
+
+/* One output line (cuda_host.cu:1444-1473).  level_i/level_f index the
+   energy-sorted level table (gi_get_levels). */
+typedef struct {
+  int32_t level_i, level_f;
+  int32_t ndeg_i, ndeg_f;
+  double nu;   /* E_F - E_I, cm^-1 */
+  double S;    /* line strength, Debye^2 */
+  double A;    /* Einstein A, 1/s */
+  double I;    /* absorption intensity, cm/mol (as the reference prints) */
+  double t[4]; /* transition moments, Debye: t[ideg_i + 2*ideg_f] */
+} gi_line;
+
+/* One level (TO_PTeigen, trove_objects.h:113-127). */
+typedef struct {
+  int32_t J, gamma;
+  int32_t rec;        /* 0-based record (vector) index within its block */
+  int32_t ndeg;
+  int32_t krot, taurot;
+  double energy;      /* absolute, cm^-1 */
+} gi_level;
+
+typedef struct {
+  int64_t nlines;          /* lines returned */
+  int64_t npairs_checked;  /* (i, f) pairs that passed the block-level rules */
+  int32_t nblock_pairs;
+  int32_t nlevels;
+  double zpe;
+  double seconds_total;    /* wall time of the last gi_run */
+  double seconds_gpu;      /* device time of the last gi_run (CUDA events) */
+  double flops_halfls;     /* algorithmic FP64 flops of the half line strength */
+  double flops_final;      /* algorithmic FP64 flops of the final contraction */
+  int32_t kernel_launches; /* kernels launched by the last gi_run */
+  int32_t reserved;
+} gi_stats;
+
+/* Context ---------------------------------------------------------------- */
+gi_status gi_create(gi_ctx** out, int device, size_t hbm_budget_bytes);
+gi_status gi_destroy(gi_ctx* ctx);
+const char* gi_last_error(const gi_ctx* ctx);
+const char* gi_status_string(gi_status s);
+
+/* Inputs ------------------------------------------------------------------ */
+/* sym_type: 1 C2V(M), 2 C3V(M), 3 D3H(M) as in the reference deck. */
+gi_status gi_set_symmetry(gi_ctx* ctx, int sym_type);
+gi_status gi_set_params(gi_ctx* ctx, const gi_params* p);
+/* mu: [3][N*N] doubles in the checkpoint's record order, mu_c(i,f) at
+   c*N*N + i + f*N (c = x, y, z). */
+gi_status gi_set_dipole(gi_ctx* ctx, int N, const double* mu);
+/* The per-J contracted basis (TO_bset_contrT):
+     icontr2icase[2*D]:   [r] = case, [r+D] = lambda (degenerate component)
+     iroot_correlat_j0[D], k[D], ktau[D] (= 2k+tau)
+     Nsym[nrep*ncase]:    N[g + case*nrep]
+     Ntotal[nrep]
+     repres[g]:           Ntotal[g]*degen[g]*mat_size doubles,
+                          (s, ideg, lambda) at s + ideg*Ntot + lambda*degen*Ntot */
+gi_status gi_set_basis(gi_ctx* ctx, int J, int D, int ncase, int max_deg_size, int mat_size,
+                       const int32_t* icontr2icase, const int32_t* iroot_correlat_j0,
+                       const int32_t* k, const int32_t* ktau, const int32_t* Nsym,
+                       const int32_t* Ntotal, const double* const* repres);
+/* Optional: a 3j table laid out as precompute_threej(jmax); by default the
+   engine computes the same table itself. */
+gi_status gi_set_threej(gi_ctx* ctx, int jmax, const double* threej);
+/* One (J, gamma) block: vecs[nvec][nsize] (record irec = row irec-1),
+   energies[nvec], quanta[nvec][nmodes+1] (quanta[0] = rotational index). */
+gi_status gi_set_block(gi_ctx* ctx, int J, int gamma, int nsize, int nvec, const double* vecs,
+                       const double* energies, const int32_t* quanta);
+
+/* Run ---------------------------------------------------------------------- */
+#define GI_RUN_LINES_ON_DEVICE 1 /* keep lines in device memory (no D2H) */
+/* Computes every line of the job (all loaded J; |dJ| <= 1; the reference's
+   filters).  *nlines receives the count. */
+gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);
+gi_status gi_get_lines(gi_ctx* ctx, int64_t offset, int64_t count, gi_line* out);
+gi_status gi_num_levels(gi_ctx* ctx, int32_t* n);
+gi_status gi_get_levels(gi_ctx* ctx, int32_t cap, gi_level* out);
+gi_status gi_get_stats(gi_ctx* ctx, gi_stats* out);
+
+/* Kernel-level drop-in for do_1st_half_ls: half line strength of one initial
+   vector vsym (nsize doubles of block (jI, gammaI)), degenerate component
+   ideg, towards the J=jF basis; half_ls receives D_F doubles. */
+gi_status gi_half_ls(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF, const double* vsym,
+                     double* half_ls);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GI_H */

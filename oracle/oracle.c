@@ -486,3 +486,32 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
 }
 
 void or_free(void* p) { free(p); }
+
+/* Filters of one level pair with the job's ZPE as given (for pinning against
+   the reference's energy_filter_lower/upper and intensity_filter). */
+int or_filter_pair(const or_job* job, int jI, double EI, int gI, const int32_t* qI, int jF,
+                   double EF, int gF, const int32_t* qF, int32_t* out, int32_t* igamma_pair) {
+  or_ctx x;
+  x.job = job;
+  x.zpe = job->ZPE;
+  for (int a = 0; a < job->nrep; a++) {
+    int n = 0;
+    x.igamma_pair[a] = a;
+    for (int b = 0; b < job->nrep; b++)
+      if (a != b && job->isym_pairs[a] == job->isym_pairs[b]) {
+        x.igamma_pair[a] = b;
+        if (++n > 1) return -2;
+      }
+    igamma_pair[a] = x.igamma_pair[a];
+  }
+  or_level I = {0, jI, gI, 0, job->degen[gI], EI, qI};
+  or_level F = {0, jF, gF, 0, job->degen[gF], EF, qF};
+  out[0] = filt_lower(&x, jI, EI, qI);
+  out[1] = filt_upper(&x, jF, EF, qF);
+  out[2] = filt_intensity(&x, &I, &F);
+  return 0;
+}
+
+int or_degeneracy_filter(const or_job* job, int gI, int gF, int idegI, int idegF) {
+  return filt_degeneracy(job, gI, gF, idegI, idegF);
+}

@@ -113,8 +113,15 @@ double or_dot(const double* x, const double* y, int n);
 int or_run(const or_job* job, or_line** out, size_t* nout);
 void or_free(void* p);
 
-/* Resolved ZPE and level count of a job (read_eigenvalues first pass). */
+/* Resolved ZPE of a job (read_eigenvalues first pass). */
 double or_resolve_zpe(const or_job* job);
+
+/* Filters of one level pair, ZPE taken as given: out = [energy_filter_lower(I),
+   energy_filter_upper(F), intensity_filter(I,F)] (trove_functions.cpp:1432-1464). */
+int or_filter_pair(const or_job* job, int jI, double EI, int gI, const int32_t* qI, int jF,
+                   double EF, int gF, const int32_t* qF, int32_t* out, int32_t* igamma_pair);
+/* degeneracy_filter (trove_functions.cpp:1495-1510). */
+int or_degeneracy_filter(const or_job* job, int gI, int gF, int idegI, int idegF);
 
 #ifdef __cplusplus
 }

@@ -99,6 +99,9 @@ def lib():
         L.or_free.argtypes = [C.c_void_p]
         L.or_resolve_zpe.restype = C.c_double
         L.or_resolve_zpe.argtypes = [C.POINTER(or_job)]
+        L.or_filter_pair.argtypes = [C.POINTER(or_job), C.c_int, C.c_double, C.c_int, i32p,
+                                     C.c_int, C.c_double, C.c_int, i32p, i32p, i32p]
+        L.or_degeneracy_filter.argtypes = [C.POINTER(or_job), C.c_int, C.c_int, C.c_int, C.c_int]
         _lib = L
     return _lib
 

@@ -1,0 +1,108 @@
+"""Engine (CUDA, through the C ABI) against the CPU oracle: identical line
+selection and per-line accuracy in FP64."""
+import numpy as np
+import pytest
+
+from paritylib import compare
+
+pytestmark = pytest.mark.gpu
+
+
+def run_engine(pkg, prob, **kw):
+    with pkg.Engine(0) as eng:
+        eng.load(prob, **kw)
+        eng.run()
+        return pkg.keyed(eng.lines(), eng.levels()), eng.stats(), eng.levels()
+
+
+@pytest.mark.parametrize("case", ["c2v", "c3v", "c3v_reduced"])
+def test_lines_match_oracle(pkg, synth, oracle, case):
+    if case == "c2v":
+        prob = synth.make_c2v(11, 30, [0, 1, 2, 3], nvec_max=8)
+    else:
+        prob = synth.make_c3v(12, 24, [0, 1, 2, 3], nvec_max=8, reduced=case.endswith("reduced"))
+    got, st, _ = run_engine(pkg, prob)
+    ref = oracle.run_all(prob)
+    res = compare(got, ref)
+    assert res["n"] > 100
+    print(case, res, st["kernel_launches"])
+
+
+def test_small_workload_full(pkg, synth, oracle):
+    """Every eigenvector of the CPU-sized workload (N=200, J=0..2)."""
+    prob = synth.workload("c2v_small", seed=1)
+    got, st, _ = run_engine(pkg, prob)
+    ref = oracle.run_all(prob)
+    res = compare(got, ref)
+    assert res["n"] == 360000
+    print(res)
+
+
+def test_half_ls_matches_oracle(pkg, synth, oracle):
+    for prob in (synth.make_c2v(3, 16, [1, 2, 3], nvec_max=3),
+                 synth.make_c3v(4, 14, [1, 2, 3], nvec_max=3)):
+        with pkg.Engine(0) as eng:
+            eng.load(prob)
+            for (jI, gI), blk in sorted(prob.blocks.items()):
+                if blk.nvec == 0:
+                    continue
+                for jF in prob.jlist:
+                    if abs(jF - jI) > 1:
+                        continue
+                    for d in range(prob.degen[gI]):
+                        vprim = oracle.correlate(prob.bases[jI], prob.nrep, prob.degen, d, gI,
+                                                 blk.vecs[0])
+                        want = oracle.half_ls(prob.bases[jI], prob.bases[jF], prob.N, prob.mu,
+                                              max(prob.jlist), vprim)
+                        got = eng.half_ls(jI, gI, d, jF, blk.vecs[0], prob.bases[jF].Maxcontracts)
+                        assert np.abs(got - want).max() <= 1e-13 * np.abs(want).max()
+
+
+def test_empty_and_filtered(pkg, synth, oracle):
+    prob = synth.make_c2v(5, 20, [0, 1, 2], nvec_max=6)
+    # an empty block and a symmetry switched off by its spin weight
+    b = prob.blocks[(1, 2)]
+    prob.blocks[(1, 2)] = synth.Block(1, 2, b.vecs[:0], b.energies[:0], b.quanta[:0])
+    prob.params.gns = (1.0, 1.0, 0.0, 0.0)
+    got, _, _ = run_engine(pkg, prob)
+    ref = oracle.run_all(prob)
+    compare(got, ref)
+    assert len(ref) > 0 and np.all(ref["gammaI"] < 2)
+    # windows that select nothing
+    prob.params.erange_lower = (1e8, 2e8)
+    got, _, _ = run_engine(pkg, prob)
+    assert len(got) == 0 and len(oracle.run_all(prob)) == 0
+
+
+def test_windows_thresholds_zpe(pkg, synth, oracle):
+    prob = synth.make_c2v(6, 24, [0, 1, 2], nvec_max=10)
+    p = prob.params
+    p.ZPE = -1.0                      # taken from the first J=0, A1 record
+    p.freq_window = (-3000.0, 8000.0)  # emission and absorption
+    p.erange_lower = (0.0, 9000.0)
+    p.erange_upper = (500.0, 19000.0)
+    p.quanta_lower = np.array([[0, 1, 0], [7, 6, 7]], np.int32)
+    p.quanta_upper = np.array([[1, 0, 0], [7, 7, 5]], np.int32)
+    p.thresh_intensity = 1e-24
+    p.thresh_linestrength = 1e-3
+    got, st, _ = run_engine(pkg, prob)
+    ref = oracle.run_all(prob)
+    compare(got, ref)
+    assert abs(st["zpe"] - prob.blocks[(0, 0)].energies[0]) == 0.0
+    assert (ref["nu"] < 0).any() and len(ref) > 50
+
+
+def test_errors_are_reported(pkg, synth):
+    with pkg.Engine(0) as eng:
+        with pytest.raises(pkg.GiError) as e:
+            eng.run()
+        assert e.value.status == pkg.GI_ERR_STATE
+        prob = synth.make_c2v(1, 10, [0, 1], nvec_max=3)
+        eng.set_symmetry(prob.sym_type)
+        b = prob.bases[1]
+        bad = synth.Basis(**{**b.__dict__, "Ntotal": b.Ntotal + 1})
+        with pytest.raises(pkg.GiError) as e:
+            eng.set_basis(bad)
+        assert e.value.status == pkg.GI_ERR_ARG
+        with pytest.raises(pkg.GiError):
+            eng.set_symmetry(9)
