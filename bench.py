@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the GB300 line-intensity engine.
+
+Workload (default ``c2v_plain``): triatomic C2v, J = 0..10, Nvib = 2000,
+the lowest 1000 eigenvectors per (J, Gamma) under 15000 cm^-1, every
+dJ = 0, +-1 block pair; seeded synthetic inputs of those shapes (no TROVE
+checkpoints exist here).  One step = one whole intensity job over that
+input: every line S, A_if, I(T) after the reference's filters.
+
+Metric: linestrengths/s, counting lines that pass every filter before the
+intensity threshold (1e-30 cm/molecule; the post-threshold count is reported
+beside it).
+
+  value   inputs resident in HBM, lines kept on the device, wall time of K
+          steps bracketed by synchronize (and a barrier across ranks)
+  e2e     the same job through the C ABI from pinned host buffers: every step
+          uploads the dipole and every eigenvector block and reads all lines
+          back to host memory
+  --impl reference   the reference's algorithm on the host cores (the CPU
+          oracle port; the reference has no CPU implementation of the path)
+          on a bounded sample of the same workload
+
+Multi-GPU (torchrun): every rank runs an independent replica of the job with
+its own seed (no collective on the data path), value = all ranks' lines /
+max time ("weak" scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+import __graft_entry__ as G  # noqa: E402
+
+METRIC = "linestrengths/s"
+THRESH_I = 1e-30  # cm/molecule
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2v_plain")
+    ap.add_argument("--jmax", type=int, default=None, help="restrict J to 0..jmax")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+def make_problem(args, rank=0):
+    G.load_package()
+    from gpu_intensities_gb300 import synth
+    kw = {}
+    if args.jmax is not None:
+        kw["jlist"] = list(range(args.jmax + 1))
+    prob = synth.workload(args.workload, seed=args.seed + rank, **kw)
+    prob.params.thresh_intensity = THRESH_I
+    return prob
+
+
+def config_of(args, prob):
+    return {"workload": args.workload, "sym": "C2v" if prob.sym_type == 1 else "C3v",
+            "J": [min(prob.jlist), max(prob.jlist)], "Nvib": prob.N,
+            "nvec_max_per_block": max(b.nvec for b in prob.blocks.values()),
+            "levels": int(sum(b.nvec for b in prob.blocks.values())),
+            "precision": args.precision, "thresh_intensity_cm_per_molecule": THRESH_I,
+            "l2": "inputs (eigenvector blocks, 1.9 GB) larger than L2",
+            "seed": args.seed}
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.index)], stdout=subprocess.PIPE,
+                stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        rows = []
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]) if f[3] not in ("[N/A]",) else 0.0,
+                             f[5], f[6], f[7], f[8]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [r[0] for r in rows]
+        reasons = []
+        for i, name in ((3, "hw_slowdown"), (4, "hw_thermal_slowdown"),
+                        (5, "sw_thermal_slowdown"), (6, "sw_power_cap")):
+            if any(r[i].lower() == "active" for r in rows):
+                reasons.append(name)
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_sample(prob, nlow: int):
+    """Bounded sample of the workload for the oracle: the reference run over the
+    two highest J with only the nlow lowest initial levels kept (lower energy
+    window), every final level kept."""
+    O = G.load_oracle()
+    js = prob.jlist
+    pair = (js[-2], js[-1])
+    zpe = O.resolve_zpe(prob)
+    e = np.sort(np.concatenate([prob.blocks[(J, g)].energies for J in pair
+                                for g in range(prob.nrep) if (J, g) in prob.blocks]))
+    cut = float(e[min(nlow, len(e)) - 1]) - (zpe if zpe > 0 else 0.0)
+    saved = prob.params.erange_lower
+    prob.params.erange_lower = (saved[0], cut)
+    return O, pair, zpe, saved
+
+
+def run_cpu(prob, nlow: int, threads: int):
+    O, pair, zpe, saved = cpu_sample(prob, nlow)
+    try:
+        t = time.perf_counter()
+        lines = O.run_pair(prob, pair, zpe, nthreads=threads)
+        dt = time.perf_counter() - t
+    finally:
+        prob.params.erange_lower = saved
+    return len(lines), dt, pair
+
+
+def cpu_baseline(prob, nlow=8):
+    threads = os.cpu_count() or 1
+    n, dt, pair = run_cpu(prob, nlow, threads)
+    return {"value": n / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"oracle run over J={pair[0]},{pair[1]} restricted to the {nlow} lowest "
+                      f"initial levels ({n} lines in {dt:.1f} s)"}
+
+
+# ---------------------------------------------------------------- reference arm
+def main_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    prob = make_problem(args)
+    threads = os.cpu_count() or 1
+    nlow = 4
+    for _ in range(args.warmup):
+        run_cpu(prob, nlow, threads)
+    tot_n, tot_t = 0, 0.0
+    for _ in range(args.steps):
+        n, dt, pair = run_cpu(prob, nlow, threads)
+        tot_n += n
+        tot_t += dt
+    v = tot_n / tot_t
+    out = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC,
+           "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
+           "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": config_of(args, prob),
+           "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
+                            "sample": f"oracle (the reference's algorithm restated in C; the "
+                                      f"reference has no CPU path) over J={pair[0]},{pair[1]} "
+                                      f"with the {nlow} lowest initial levels per step"},
+           "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+    return 0
+
+
+# ---------------------------------------------------------------- our arm
+def main_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    pkg = G.load_package()
+    prob = make_problem(args, rank)
+    prec = pkg.GI_PREC_SPLIT if args.precision == "split" else pkg.GI_PREC_FP64
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    eng = pkg.Engine(local)
+    eng.load(prob, precision=prec)
+    for _ in range(args.warmup):
+        eng.run(lines_on_device=True)
+    torch.cuda.synchronize()
+    barrier()
+    stats = []
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng.run(lines_on_device=True)
+            stats.append(eng.stats())
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+    barrier()
+    dt = (t1 - t0) / args.steps
+    lines_pre = stats[-1]["nlines_filtered"]
+    lines_post = stats[-1]["nlines"]
+    launches = int(sum(s["kernel_launches"] for s in stats))
+
+    # roofline of the dominant kernel: one more step with per-kernel events
+    eng.run(lines_on_device=True, phase_timing=True)
+    ps = eng.stats()
+    sp = ps["seconds_phase"]
+    lp = ps["launches_phase"]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    if args.precision == "split":
+        dom = "halfls_gemm"
+        flops = ps["flops_tensor"]
+        peak = peaks.get("bf16_tflops", 1900.0)
+        tens_time = sp["halfls_gemm"] + sp["final_gemm"]
+        achieved = flops / tens_time / 1e12 if tens_time else 0.0
+        roof = {"bound": "tensor", "kernel": "split bf16 slice GEMMs (tcgen05)",
+                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"
+                if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s"}
+    else:
+        dom = "halfls_gemm"
+        fp64_peak = pkg.measure_fp64_peak(local)  # TFLOP/s, DMMA m8n8k4, measured live
+        achieved = ps["flops_halfls"] / sp[dom] / 1e12 if sp[dom] else 0.0
+        roof = {"bound": "tensor", "kernel": "k_gemm_fp64_nt (FP64 DMMA, half line strength)",
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": None,
+                "peak_source": "FP64 DMMA peak measured live by gi_measure_fp64_peak "
+                               "(of measured); MEASURED_PEAKS.json has no FP64 entry"}
+    roof["phase_seconds"] = {k: round(v, 6) for k, v in sp.items()}
+    roof["phase_launches"] = lp
+    roof["launch_avg_ms"] = 1e3 * sp[dom] / max(lp[dom], 1)
+
+    # end to end through the C ABI from pinned host buffers
+    e2e = None
+    if not args.no_e2e:
+        pin = {}
+        mu = torch.from_numpy(prob.mu).pin_memory()
+        for k, b in prob.blocks.items():
+            pin[k] = torch.from_numpy(np.ascontiguousarray(b.vecs)).pin_memory()
+        h2d = mu.numel() * 8 + sum(v.numel() * 8 for v in pin.values())
+        ne = args.e2e_steps or args.steps
+
+        def step():
+            eng.set_dipole(prob.N, mu.numpy())
+            for (J, g), b in sorted(prob.blocks.items()):
+                eng.set_block(J, g, pin[(J, g)].numpy(), b.energies, b.quanta)
+            return eng.run(lines_on_device=False)
+
+        step()
+        torch.cuda.synchronize()
+        barrier()
+        te0 = time.perf_counter()
+        for _ in range(ne):
+            n = step()
+        torch.cuda.synchronize()
+        te1 = time.perf_counter()
+        barrier()
+        st = eng.stats()
+        e2e = {"value": world * st["nlines_filtered"] / ((te1 - te0) / ne), "unit": METRIC,
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(n * 80 + 16),
+               "ms_per_step": 1e3 * (te1 - te0) / ne}
+
+    if world > 1:
+        t = torch.tensor([dt], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt = float(t.item())
+    out = None
+    if rank == 0:
+        out = {"metric": METRIC, "value": world * lines_pre / dt, "unit": METRIC,
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+               "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak",
+               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+               "config": config_of(args, prob),
+               "lines_per_step": lines_pre, "lines_above_threshold_per_step": lines_post,
+               "value_above_threshold": world * lines_post / dt,
+               "gpu_launches": launches, "roofline": roof, "e2e": e2e,
+               "clocks": clk.summary()}
+        if world == 1 and not args.no_cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline(prob)
+        print(json.dumps(out))
+    eng.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return main_reference(args)
+    return main_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -22,11 +22,14 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgi.so")
 HEADER = os.path.join(HERE, os.pardir, "include", "gi.h")
+HEADERS = [os.path.join(HERE, os.pardir, "include", h) for h in ("gi.h", "gi_probe.h")]
 
 GI_OK, GI_ERR_ARG, GI_ERR_CUDA, GI_ERR_NOMEM, GI_ERR_STATE, GI_ERR_BUDGET, GI_ERR_NOTFOUND, \
     GI_ERR_DEVICE = range(8)
 GI_PREC_FP64, GI_PREC_SPLIT = 0, 1
 GI_RUN_LINES_ON_DEVICE = 1
+GI_RUN_PHASE_TIMING = 2
+PHASES = ("correlate", "halfls_gemm", "stencil", "final_gemm", "epilogue", "slice")
 GI_MAX_REP, GI_MAX_MODES = 8, 16
 
 i32p = C.POINTER(C.c_int32)
@@ -54,10 +57,13 @@ LEVEL_DTYPE = np.dtype([("J", np.int32), ("gamma", np.int32), ("rec", np.int32),
 
 
 class gi_stats(C.Structure):
-    _fields_ = [("nlines", C.c_int64), ("npairs_checked", C.c_int64),
+    _fields_ = [("nlines", C.c_int64), ("nlines_filtered", C.c_int64),
+                ("npairs_checked", C.c_int64),
                 ("nblock_pairs", C.c_int32), ("nlevels", C.c_int32), ("zpe", C.c_double),
                 ("seconds_total", C.c_double), ("seconds_gpu", C.c_double),
                 ("flops_halfls", C.c_double), ("flops_final", C.c_double),
+                ("flops_tensor", C.c_double), ("bytes_correlate", C.c_double),
+                ("seconds_phase", C.c_double * 6), ("launches_phase", C.c_int32 * 6),
                 ("kernel_launches", C.c_int32), ("reserved", C.c_int32)]
 
 
@@ -71,8 +77,8 @@ _lib = None
 
 
 def header_functions():
-    """Names of the entry points include/gi.h declares."""
-    text = open(HEADER).read()
+    """Names of the entry points the headers in include/ declare."""
+    text = "".join(open(h).read() for h in HEADERS)
     return sorted(set(re.findall(r"^\s*(?:gi_status|const char\*)\s+(gi_\w+)\s*\(", text, re.M)))
 
 
@@ -113,11 +119,21 @@ def lib():
         L.gi_get_levels.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
         L.gi_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_stats)]
         L.gi_half_ls.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p]
+        L.gi_measure_fp64_peak.argtypes = [C.c_int, f64p]
         for name in header_functions():
             if name not in ("gi_last_error", "gi_status_string"):
                 getattr(L, name).restype = C.c_int
         _lib = L
     return _lib
+
+
+def measure_fp64_peak(device: int = 0) -> float:
+    """FP64 DMMA peak of the device in TFLOP/s (gi_measure_fp64_peak)."""
+    v = C.c_double(0.0)
+    st = lib().gi_measure_fp64_peak(device, C.byref(v))
+    if st != GI_OK:
+        raise GiError(st, "gi_measure_fp64_peak failed")
+    return v.value
 
 
 def _p(a: np.ndarray, t):
@@ -231,9 +247,10 @@ class Engine:
             self.set_block(J, g, b.vecs, b.energies, b.quanta)
 
     # run -----------------------------------------------------------------
-    def run(self, lines_on_device: bool = False) -> int:
+    def run(self, lines_on_device: bool = False, phase_timing: bool = False) -> int:
         n = C.c_int64(0)
-        flags = GI_RUN_LINES_ON_DEVICE if lines_on_device else 0
+        flags = (GI_RUN_LINES_ON_DEVICE if lines_on_device else 0) | \
+            (GI_RUN_PHASE_TIMING if phase_timing else 0)
         self._ck(self._L.gi_run(self._h, flags, C.byref(n)))
         return int(n.value)
 
@@ -257,7 +274,11 @@ class Engine:
     def stats(self) -> Dict[str, float]:
         s = gi_stats()
         self._ck(self._L.gi_get_stats(self._h, C.byref(s)))
-        return {f: getattr(s, f) for f, _ in gi_stats._fields_ if f != "reserved"}
+        out = {f: getattr(s, f) for f, _ in gi_stats._fields_
+               if f not in ("reserved", "seconds_phase", "launches_phase")}
+        out["seconds_phase"] = dict(zip(PHASES, list(s.seconds_phase)))
+        out["launches_phase"] = dict(zip(PHASES, list(s.launches_phase)))
+        return out
 
     def half_ls(self, jI: int, gammaI: int, ideg: int, jF: int, vsym: np.ndarray,
                 D_F: int) -> np.ndarray:

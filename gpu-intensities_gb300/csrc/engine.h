@@ -118,11 +118,30 @@ struct Ctx {
 
   // results of the last run
   std::vector<Level> levels;
-  std::vector<gi_line> lines;
+  gi_line* h_lines = nullptr;  // pinned staging of the last run's lines
+  size_t h_lines_cap = 0;
   DevArray<gi_line> d_lines;
   bool lines_on_device = false;
   int64_t nlines = 0;
   gi_stats stats{};
+
+  // per-phase device timing (GI_RUN_PHASE_TIMING)
+  struct PhaseRec {
+    int phase;
+    cudaEvent_t a, b;
+  };
+  bool timing = false;
+  std::vector<cudaEvent_t> ev_pool;
+  size_t ev_used = 0;
+  std::vector<PhaseRec> phase_recs;
+  cudaEvent_t take_event() {
+    if (ev_used == ev_pool.size()) {
+      cudaEvent_t e = nullptr;
+      if (cudaEventCreate(&e) != cudaSuccess) return nullptr;
+      ev_pool.push_back(e);
+    }
+    return ev_pool[ev_used++];
+  }
 
   // workspaces
   DevArray<double> w_y, w_z, w_h, w_t;
@@ -132,6 +151,22 @@ struct Ctx {
   DevArray<StencilTerm> w_stencil;
   DevArray<int32_t> w_stencil_n, w_levelI, w_levelF;
 };
+
+// Runs one launch group on the context's stream, counting it under `phase`
+// and, when timing is on, bracketing it with CUDA events.
+template <class F>
+cudaError_t timed(Ctx* c, int phase, F&& launch) {
+  c->stats.launches_phase[phase]++;
+  c->stats.kernel_launches++;
+  if (!c->timing) return launch();
+  cudaEvent_t a = c->take_event(), b = c->take_event();
+  if (!a || !b) return cudaErrorMemoryAllocation;
+  cudaEventRecord(a, c->stream);
+  cudaError_t e = launch();
+  cudaEventRecord(b, c->stream);
+  c->phase_recs.push_back({phase, a, b});
+  return e;
+}
 
 // ------------------------------------------------------------------ kernels
 struct EpiParams {

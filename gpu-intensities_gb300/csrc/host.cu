@@ -466,140 +466,183 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   }
   GI_CUDA(c, c->w_int.upload(h_int));
   GI_CUDA(c, c->w_upper.upload(h_upper));
-  GI_CUDA(c, c->w_counter.reserve(1));
-  GI_CUDA(c, cudaMemsetAsync(c->w_counter.p, 0, sizeof(unsigned long long), c->stream));
+  GI_CUDA(c, c->w_counter.reserve(2));
+  GI_CUDA(c, cudaMemsetAsync(c->w_counter.p, 0, 2 * sizeof(unsigned long long), c->stream));
 
   // line buffer: the whole job on the device
   GI_CUDA(c, c->d_lines.reserve(std::max<size_t>(cap_total, 1)));
 
-  // workspace: per initial block (chunked to the budget)
+  // workspace: per initial block, chunked to the budget; every per-chunk
+  // table is planned here and uploaded once, so the launch loop never waits
   const int N = c->N, Kp = c->Kp;
-  size_t ws_limit = c->budget ? c->budget / 2 : ((size_t)24 << 30);
-  c->stats = gi_stats{};
-  int launches = 0;
-  double fl_half = 0.0, fl_final = 0.0;
-  int64_t npairs_checked = 0;
-
-  GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  std::vector<int32_t> h_ivec, h_lvI;
+  const size_t ws_limit = c->budget ? c->budget / 2 : ((size_t)24 << 30);
+  struct Chunk {
+    BlockPlan* I;
+    std::vector<PairPlan*> pairs;
+    int nI;
+    size_t off;  // into the ivec/level and energy tables
+  };
+  std::vector<Chunk> chunks;
+  std::vector<int32_t> h_ivec;  // per chunk: nI record ids then nI level ids
   std::vector<double> h_EI;
+  size_t max_y = 1, max_z = 1, max_h = 1, max_t = 1;
   for (auto& kv : plans) {
     BlockPlan& I = kv.second;
     std::vector<PairPlan*> mine;
     for (auto& pp : pairs)
       if (pp.I == &I) mine.push_back(&pp);
     if (mine.empty()) continue;
-    const Basis& bI = *c->bases[I.blk->J];
     const int ndegI = c->degen[I.blk->gamma];
-    const int nslot = bI.nslot;
-    // bytes per initial vector: Y + 3 Z columns, plus H and T of the widest pair
+    const int nslot = c->bases[I.blk->J]->nslot;
     size_t per_vec = (size_t)ndegI * nslot * Kp * 8 * 4;
     for (auto* pp : mine) {
       const int ndegF = c->degen[pp->F->blk->gamma];
       per_vec += (size_t)ndegI * ndegF * (pp->F->blk->ld + round_up(pp->F->blk->nvec, 2)) * 8;
     }
-    int chunk = (int)std::max<size_t>(1, ws_limit / per_vec);
-    chunk = std::min<int>(chunk, (int)I.ivec.size());
+    int chunk = (int)std::min<size_t>(std::max<size_t>(1, ws_limit / per_vec), I.ivec.size());
     for (int i0 = 0; i0 < (int)I.ivec.size(); i0 += chunk) {
-      const int nI = std::min(chunk, (int)I.ivec.size() - i0);
-      h_ivec.assign(I.ivec.begin() + i0, I.ivec.begin() + i0 + nI);
-      h_lvI.resize(nI);
-      h_EI.resize(nI);
-      for (int i = 0; i < nI; i++) {
-        h_lvI[i] = I.level_of_rec[h_ivec[i]];
-        h_EI[i] = I.blk->energies[h_ivec[i]];
+      Chunk ch{&I, mine, std::min(chunk, (int)I.ivec.size() - i0), h_EI.size()};
+      for (int i = 0; i < ch.nI; i++) h_EI.push_back(I.blk->energies[I.ivec[i0 + i]]);
+      for (int i = 0; i < ch.nI; i++) h_ivec.push_back(I.ivec[i0 + i]);
+      for (int i = 0; i < ch.nI; i++) h_ivec.push_back(I.level_of_rec[I.ivec[i0 + i]]);
+      const size_t ncolY = (size_t)ch.nI * ndegI * nslot;
+      max_y = std::max(max_y, ncolY * Kp);
+      max_z = std::max(max_z, 3 * ncolY * Kp);
+      for (auto* pp : mine) {
+        const size_t ncolH = (size_t)ch.nI * ndegI * c->degen[pp->F->blk->gamma];
+        max_h = std::max(max_h, ncolH * pp->F->blk->ld);
+        max_t = std::max(max_t, ncolH * round_up(pp->F->blk->nvec, 2));
       }
-      // small per-chunk tables (synchronous upload keeps the host arrays valid)
-      GI_CUDA(c, cudaStreamSynchronize(c->stream));
-      GI_CUDA(c, c->w_ivec.reserve((size_t)nI * 2));
-      GI_CUDA(c, cudaMemcpy(c->w_ivec.p, h_ivec.data(), sizeof(int32_t) * nI, cudaMemcpyHostToDevice));
-      GI_CUDA(c, cudaMemcpy(c->w_ivec.p + nI, h_lvI.data(), sizeof(int32_t) * nI, cudaMemcpyHostToDevice));
-      GI_CUDA(c, c->w_t.reserve(1));
-      DevArray<double> d_EI;
-      GI_CUDA(c, d_EI.upload(h_EI));
+      chunks.push_back(std::move(ch));
+    }
+  }
+  // ivec/level tables are laid out [chunk: nI recs, nI levels]; energies [chunk: nI]
+  GI_CUDA(c, c->w_ivec.upload(h_ivec));
+  DevArray<double> d_EI;
+  GI_CUDA(c, d_EI.upload(h_EI));
+  GI_CUDA(c, c->w_y.reserve(max_y));
+  GI_CUDA(c, c->w_z.reserve(max_z));
+  GI_CUDA(c, c->w_h.reserve(max_h));
+  GI_CUDA(c, c->w_t.reserve(max_t));
+  if (P.precision == GI_PREC_SPLIT) {
+    gi_status s = split_prepare(c);
+    if (s != GI_OK) return s;
+  }
 
-      const int ncolY = nI * ndegI * nslot;
-      GI_CUDA(c, c->w_y.reserve((size_t)ncolY * Kp));
-      GI_CUDA(c, c->w_z.reserve((size_t)3 * ncolY * Kp));
-      GI_CUDA(c, launch_build_y(I.blk->d_vecs.p, I.blk->ld, c->w_ivec.p, nI, ndegI, bI,
-                                I.blk->gamma, c->degen[I.blk->gamma], N, Kp, c->w_y.p, c->stream));
-      launches++;
-      const size_t zc = (size_t)ncolY * Kp;
+  c->stats = gi_stats{};
+  c->timing = (flags & GI_RUN_PHASE_TIMING) != 0;
+  c->ev_used = 0;
+  c->phase_recs.clear();
+  double fl_half = 0.0, fl_final = 0.0, by_corr = 0.0;
+  int64_t npairs_checked = 0;
+
+  GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  for (const Chunk& ch : chunks) {
+    BlockPlan& I = *ch.I;
+    const Basis& bI = *c->bases[I.blk->J];
+    const int ndegI = c->degen[I.blk->gamma];
+    const int nslot = bI.nslot;
+    const int nI = ch.nI;
+    const int32_t* d_ivec = c->w_ivec.p + 2 * ch.off;
+    const int32_t* d_lvI = d_ivec + nI;
+    const double* d_ei = d_EI.p + ch.off;
+    const int ncolY = nI * ndegI * nslot;
+    GI_CUDA(c, timed(c, GI_PHASE_CORRELATE, [&] {
+              return launch_build_y(I.blk->d_vecs.p, I.blk->ld, d_ivec, nI, ndegI, bI,
+                                    I.blk->gamma, ndegI, N, Kp, c->w_y.p, c->stream);
+            }));
+    by_corr += 8.0 * ((double)nI * I.blk->nsize + (double)ncolY * Kp);
+    const size_t zc = (size_t)ncolY * Kp;
+    if (P.precision == GI_PREC_SPLIT) {
+      gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, ncolY);
+      if (s != GI_OK) return s;
+    } else {
+      GI_CUDA(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
+                return gemm_fp64_nt(c->d_mu.p, Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp,
+                                    zc, N, ncolY, Kp, 3, c->stream);
+              }));
+    }
+    fl_half += 2.0 * 3.0 * N * (double)N * ncolY;
+
+    for (auto* pp : ch.pairs) {
+      BlockPlan& Fp = *pp->F;
+      const Block& fb = *Fp.blk;
+      const Basis& bF = *c->bases[fb.J];
+      const int ndegF = c->degen[fb.gamma];
+      const int ldh = fb.ld;
+      const int ncolH = nI * ndegI * ndegF;
+      const int ldt = round_up(fb.nvec, 2);
+      GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
+                return launch_build_h(c->w_z.p, zc, Kp, nslot, ndegI, nI, bF, fb.gamma, ndegF,
+                                      fb.nsize, ldh, c->w_stencil.p + pp->st_off * 6,
+                                      c->w_stencil_n.p + pp->st_off, 6, c->w_h.p, c->stream);
+              }));
       if (P.precision == GI_PREC_SPLIT) {
-        gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, ncolY, &launches);
+        gi_status s = split_gemm_final(c, fb.d_vecs.p, fb.ld, fb.nvec, c->w_h.p, ldh, ncolH,
+                                       c->w_t.p, ldt);
         if (s != GI_OK) return s;
       } else {
-        GI_CUDA(c, gemm_fp64_nt(c->d_mu.p, Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp, zc, N,
-                                ncolY, Kp, 3, c->stream));
-        launches++;
+        GI_CUDA(c, timed(c, GI_PHASE_FINAL_GEMM, [&] {
+                  return gemm_fp64_nt(fb.d_vecs.p, fb.ld, 0, c->w_h.p, ldh, c->w_t.p, ldt, 0,
+                                      fb.nvec, ncolH, ldh, 1, c->stream);
+                }));
       }
-      fl_half += 2.0 * 3.0 * N * (double)N * ncolY;
-
-      for (auto* pp : mine) {
-        BlockPlan& Fp = *pp->F;
-        const Block& fb = *Fp.blk;
-        const Basis& bF = *c->bases[fb.J];
-        const int ndegF = c->degen[fb.gamma];
-        const int ldh = fb.ld;
-        const int ncolH = nI * ndegI * ndegF;
-        const int ldt = round_up(fb.nvec, 2);
-        GI_CUDA(c, c->w_h.reserve((size_t)ncolH * ldh));
-        GI_CUDA(c, c->w_t.reserve((size_t)ncolH * ldt));
-        GI_CUDA(c, launch_build_h(c->w_z.p, zc, Kp, nslot, ndegI, nI, bF, fb.gamma, ndegF,
-                                  fb.nsize, ldh, c->w_stencil.p + pp->st_off * 6,
-                                  c->w_stencil_n.p + pp->st_off, 6, c->w_h.p, c->stream));
-        launches++;
-        if (P.precision == GI_PREC_SPLIT) {
-          gi_status s = split_gemm_final(c, fb.d_vecs.p, fb.ld, fb.nvec, c->w_h.p, ldh, ncolH,
-                                         c->w_t.p, ldt, &launches);
-          if (s != GI_OK) return s;
-        } else {
-          GI_CUDA(c, gemm_fp64_nt(fb.d_vecs.p, fb.ld, 0, c->w_h.p, ldh, c->w_t.p, ldt, 0, fb.nvec,
-                                  ncolH, ldh, 1, c->stream));
-          launches++;
-        }
-        fl_final += 2.0 * fb.nsize * (double)fb.nvec * ncolH;
-        EpiParams ep{};
-        ep.jI = I.blk->J;
-        ep.jF = fb.J;
-        ep.ndegI = ndegI;
-        ep.ndegF = ndegF;
-        ep.reduced = P.reduced;
-        ep.combo_mask = pp->combo_mask;
-        ep.gns = P.gns[I.blk->gamma];
-        ep.zpe = zpe;
-        ep.beta = beta;
-        ep.q_stat = P.q_stat;
-        ep.fw0 = P.freq_window[0];
-        ep.fw1 = P.freq_window[1];
-        ep.thresh_S = P.thresh_linestrength;
-        ep.thresh_I = P.thresh_intensity;
-        ep.A_coef = ph.A_coef;
-        ep.intens_cm_mol = ph.intens_cm_mol;
-        ep.avogno = ph.avogno;
-        const auto off = farr[&Fp];
-        GI_CUDA(c, launch_epilogue(c->w_t.p, ldt, nI, fb.nvec, c->w_ivec.p + nI, d_EI.p,
-                                   c->w_int.p + off.first, fb.d_energies.p, c->w_upper.p + off.second,
-                                   ep, c->d_lines.p, c->w_counter.p, (long long)c->d_lines.n,
-                                   c->stream));
-        launches++;
-        npairs_checked += (int64_t)nI * Fp.nupper;
-      }
+      fl_final += 2.0 * fb.nsize * (double)fb.nvec * ncolH;
+      EpiParams ep{};
+      ep.jI = I.blk->J;
+      ep.jF = fb.J;
+      ep.ndegI = ndegI;
+      ep.ndegF = ndegF;
+      ep.reduced = P.reduced;
+      ep.combo_mask = pp->combo_mask;
+      ep.gns = P.gns[I.blk->gamma];
+      ep.zpe = zpe;
+      ep.beta = beta;
+      ep.q_stat = P.q_stat;
+      ep.fw0 = P.freq_window[0];
+      ep.fw1 = P.freq_window[1];
+      ep.thresh_S = P.thresh_linestrength;
+      ep.thresh_I = P.thresh_intensity;
+      ep.A_coef = ph.A_coef;
+      ep.intens_cm_mol = ph.intens_cm_mol;
+      ep.avogno = ph.avogno;
+      const auto off = farr[&Fp];
+      GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+                return launch_epilogue(c->w_t.p, ldt, nI, fb.nvec, d_lvI, d_ei,
+                                       c->w_int.p + off.first, fb.d_energies.p,
+                                       c->w_upper.p + off.second, ep, c->d_lines.p,
+                                       c->w_counter.p, (long long)c->d_lines.n, c->stream);
+              }));
+      npairs_checked += (int64_t)nI * Fp.nupper;
     }
   }
   GI_CUDA(c, cudaEventRecord(c->ev1, c->stream));
-  unsigned long long count = 0;
-  GI_CUDA(c, cudaMemcpyAsync(&count, c->w_counter.p, sizeof(count), cudaMemcpyDeviceToHost, c->stream));
+  unsigned long long counts[2] = {0, 0};
+  GI_CUDA(c, cudaMemcpyAsync(counts, c->w_counter.p, sizeof(counts), cudaMemcpyDeviceToHost, c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));
+  const unsigned long long count = counts[0];
   if (count > c->d_lines.n) return fail(c, GI_ERR_DEVICE, "line buffer overflow (%llu lines)", count);
   c->nlines = (int64_t)count;
-  if (!c->lines_on_device) {
-    c->lines.resize(count);
-    if (count)
-      GI_CUDA(c, cudaMemcpy(c->lines.data(), c->d_lines.p, sizeof(gi_line) * count, cudaMemcpyDeviceToHost));
+  if (!c->lines_on_device && count) {
+    if (c->h_lines_cap < count) {
+      if (c->h_lines) cudaFreeHost(c->h_lines);
+      c->h_lines = nullptr;
+      c->h_lines_cap = 0;
+      GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_lines), sizeof(gi_line) * count));
+      c->h_lines_cap = count;
+    }
+    GI_CUDA(c, cudaMemcpyAsync(c->h_lines, c->d_lines.p, sizeof(gi_line) * count,
+                               cudaMemcpyDeviceToHost, c->stream));
+    GI_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   float ms = 0.f;
   GI_CUDA(c, cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+  for (const auto& r : c->phase_recs) {
+    float pm = 0.f;
+    GI_CUDA(c, cudaEventElapsedTime(&pm, r.a, r.b));
+    c->stats.seconds_phase[r.phase] += pm * 1e-3;
+  }
+  c->stats.nlines_filtered = (int64_t)counts[1];
   c->stats.nlines = c->nlines;
   c->stats.npairs_checked = npairs_checked;
   c->stats.nblock_pairs = (int32_t)pairs.size();
@@ -608,7 +651,7 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   c->stats.seconds_gpu = ms * 1e-3;
   c->stats.flops_halfls = fl_half;
   c->stats.flops_final = fl_final;
-  c->stats.kernel_launches = launches;
+  c->stats.bytes_correlate = by_corr;
   c->stats.seconds_total =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   *nlines_out = c->nlines;
@@ -662,6 +705,7 @@ gi_status gi_destroy(gi_ctx* h) {
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   split_release(c);
+  if (c->h_lines) cudaFreeHost(c->h_lines);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -768,7 +812,12 @@ gi_status gi_set_block(gi_ctx* h, int J, int gamma, int nsize, int nvec, const d
       (nvec > 0 && (!vecs || !energies || !quanta)))
     return fail(c, GI_ERR_ARG, "gi_set_block: bad arguments for (J=%d, gamma=%d)", J, gamma);
   cudaSetDevice(c->device);
-  auto b = std::make_unique<Block>();
+  std::unique_ptr<Block> b;
+  auto it = c->blocks.find({J, gamma});
+  if (it != c->blocks.end() && it->second->nsize == nsize && it->second->nvec == nvec)
+    b = std::move(it->second);  // same shape: reuse the device arrays
+  else
+    b = std::make_unique<Block>();
   b->J = J;
   b->gamma = gamma;
   b->nsize = nsize;
@@ -777,12 +826,18 @@ gi_status gi_set_block(gi_ctx* h, int J, int gamma, int nsize, int nvec, const d
   b->energies.assign(energies, energies + nvec);
   const int nq = c->params.nmodes + 1;
   b->quanta.assign(quanta, quanta + (size_t)nvec * nq);
-  GI_CUDA(c, b->d_vecs.alloc((size_t)std::max(nvec, 1) * b->ld));
-  GI_CUDA(c, cudaMemset(b->d_vecs.p, 0, sizeof(double) * b->d_vecs.n));
+  const size_t need = (size_t)std::max(nvec, 1) * b->ld;
+  if (b->d_vecs.n != std::max<size_t>(need, 1)) {
+    GI_CUDA(c, b->d_vecs.alloc(need));
+    GI_CUDA(c, cudaMemset(b->d_vecs.p, 0, sizeof(double) * b->d_vecs.n));
+  }
   if (nvec)
     GI_CUDA(c, cudaMemcpy2D(b->d_vecs.p, sizeof(double) * b->ld, vecs, sizeof(double) * nsize,
                             sizeof(double) * nsize, nvec, cudaMemcpyHostToDevice));
-  GI_CUDA(c, b->d_energies.upload(b->energies));
+  if (b->d_energies.n != (size_t)std::max(nvec, 1)) GI_CUDA(c, b->d_energies.alloc(nvec));
+  if (nvec)
+    GI_CUDA(c, cudaMemcpy(b->d_energies.p, b->energies.data(), sizeof(double) * nvec,
+                          cudaMemcpyHostToDevice));
   c->blocks[{J, gamma}] = std::move(b);
   return GI_OK;
 }
@@ -803,7 +858,7 @@ gi_status gi_get_lines(gi_ctx* h, int64_t offset, int64_t count, gi_line* out) {
   if (c->lines_on_device) {
     GI_CUDA(c, cudaMemcpy(out, c->d_lines.p + offset, sizeof(gi_line) * count, cudaMemcpyDeviceToHost));
   } else {
-    std::memcpy(out, c->lines.data() + offset, sizeof(gi_line) * count);
+    std::memcpy(out, c->h_lines + offset, sizeof(gi_line) * count);
   }
   return GI_OK;
 }

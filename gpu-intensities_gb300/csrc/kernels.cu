@@ -158,12 +158,13 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
                            long long cap) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y;
-  bool keep = false;
+  bool keep = false, pass = false;
   gi_line L;
   if (f < nF && upper_ok[f]) {
     const double ei = EI[i], ef = EF[f];
     const double nu = ef - ei;
     if (nu >= p.fw0 && nu <= p.fw1) {
+      pass = true;
       double t[4] = {0.0, 0.0, 0.0, 0.0};
       for (int dF = 0; dF < p.ndegF; ++dF)
         for (int dI = 0; dI < p.ndegI; ++dI)
@@ -193,9 +194,11 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
       for (int q = 0; q < 4; ++q) L.t[q] = t[q];
     }
   }
+  const int lane = threadIdx.x & 31;
+  const unsigned pmask = __ballot_sync(0xffffffffu, pass);
+  if (pmask && lane == 0) atomicAdd(counter + 1, (unsigned long long)__popc(pmask));
   const unsigned mask = __ballot_sync(0xffffffffu, keep);
   if (mask == 0) return;
-  const int lane = threadIdx.x & 31;
   const int leader = __ffs(mask) - 1;
   unsigned long long base = 0;
   if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));

@@ -2,15 +2,15 @@
 #include "split.h"
 
 namespace gi {
-gi_status split_gemm_dipole(Ctx* c, const double*, int, double*, int, size_t, int, int*) {
+gi_status split_gemm_dipole(Ctx* c, const double*, int, double*, int, size_t, int) {
   c->err = "split precision not available in this build";
   return GI_ERR_ARG;
 }
-gi_status split_gemm_final(Ctx* c, const double*, int, int, const double*, int, int, double*, int,
-                           int*) {
+gi_status split_gemm_final(Ctx* c, const double*, int, int, const double*, int, int, double*, int) {
   c->err = "split precision not available in this build";
   return GI_ERR_ARG;
 }
+gi_status split_prepare(Ctx*) { return GI_OK; }
 void split_invalidate(Ctx*) {}
 void split_release(Ctx*) {}
 }  // namespace gi

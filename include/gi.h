@@ -108,8 +108,20 @@ typedef struct {
   double energy;      /* absolute, cm^-1 */
 } gi_level;
 
+/* Phases of a run, for per-phase device timing (GI_RUN_PHASE_TIMING). */
+enum {
+  GI_PHASE_CORRELATE = 0, /* symmetrised -> primitive + scatter (initial vectors) */
+  GI_PHASE_HALFLS_GEMM,   /* Z = mu^T Y, the dense part of the half line strength */
+  GI_PHASE_STENCIL,       /* 3j/K-tau combination + projection onto the final basis */
+  GI_PHASE_FINAL_GEMM,    /* T = V_F^T H, the final-state contraction */
+  GI_PHASE_EPILOGUE,      /* S, A, I, filters, line output */
+  GI_PHASE_SLICE,         /* FP64 -> bf16 slice conversion (split precision) */
+  GI_NPHASE
+};
+
 typedef struct {
-  int64_t nlines;          /* lines returned */
+  int64_t nlines;          /* lines returned (after the thresholds) */
+  int64_t nlines_filtered; /* lines passing every filter, before the thresholds */
   int64_t npairs_checked;  /* (i, f) pairs that passed the block-level rules */
   int32_t nblock_pairs;
   int32_t nlevels;
@@ -118,6 +130,10 @@ typedef struct {
   double seconds_gpu;      /* device time of the last gi_run (CUDA events) */
   double flops_halfls;     /* algorithmic FP64 flops of the half line strength */
   double flops_final;      /* algorithmic FP64 flops of the final contraction */
+  double flops_tensor;     /* bf16 tensor flops executed by the split-precision GEMMs */
+  double bytes_correlate;  /* algorithmic HBM bytes of the correlate phase */
+  double seconds_phase[GI_NPHASE]; /* device time per phase (GI_RUN_PHASE_TIMING) */
+  int32_t launches_phase[GI_NPHASE];
   int32_t kernel_launches; /* kernels launched by the last gi_run */
   int32_t reserved;
 } gi_stats;
@@ -156,6 +172,7 @@ gi_status gi_set_block(gi_ctx* ctx, int J, int gamma, int nsize, int nvec, const
 
 /* Run ---------------------------------------------------------------------- */
 #define GI_RUN_LINES_ON_DEVICE 1 /* keep lines in device memory (no D2H) */
+#define GI_RUN_PHASE_TIMING 2    /* time every kernel with CUDA events (gi_stats) */
 /* Computes every line of the job (all loaded J; |dJ| <= 1; the reference's
    filters).  *nlines receives the count. */
 gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);
