@@ -120,6 +120,8 @@ def lib():
         L.gi_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_stats)]
         L.gi_half_ls.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p]
         L.gi_measure_fp64_peak.argtypes = [C.c_int, f64p]
+        L.gi_half_ls_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
         for name in header_functions():
             if name not in ("gi_last_error", "gi_status_string"):
                 getattr(L, name).restype = C.c_int

@@ -197,5 +197,9 @@ cudaError_t gemm_fp64_nt(const double* A, int lda, size_t strideA, const double*
 // ------------------------------------------------------------------ host math
 double three_j(int j1, int j2, int j3, int k1, int k2, int k3);
 void precompute_threej(int jmax, std::vector<double>& out);
+// Half-line-strength terms for every final key (2*jF+2 keys, 6 slots each);
+// threej may be null, in which case three_j() supplies the values.
+void stencil_fill(const Basis& bI, const Basis& bF, const double* threej, int tj_jmax,
+                  StencilTerm* st, int32_t* st_n);
 
 }  // namespace gi

@@ -219,14 +219,17 @@ static gi_status ensure_ycsr(Ctx* c, Basis& b) {
 // Terms of the half line strength for a final key (kF, tauF) towards the
 // initial basis of J=jI (dipole_kernals.cu:191-223): coefficient
 // (-1)^sigmaF (-1)^(sigmaI+kI) L f3j s and dipole component c.
-static void build_stencil(const Basis& bI, const Basis& bF, const std::vector<double>& threej,
-                          int tj_jmax, std::vector<StencilTerm>& st, std::vector<int32_t>& st_n) {
+// Fixed-array core: st holds (2*jF+2)*6 terms, st_n (2*jF+2) counts.  With a
+// null table the 3j values come from three_j() itself (the same numbers the
+// table holds).
+void stencil_fill(const Basis& bI, const Basis& bF, const double* threej, int tj_jmax,
+                  StencilTerm* st, int32_t* st_n) {
   const int J1 = tj_jmax + 1;
   const int jI = bI.J, jF = bF.J;
   const double sq2 = 1.0 / std::sqrt(2.0);
   const int nkey = 2 * jF + 2;
-  st.assign((size_t)nkey * 6, StencilTerm{0, 0, 0.0});
-  st_n.assign(nkey, 0);
+  for (int i = 0; i < nkey * 6; i++) st[i] = StencilTerm{0, 0, 0.0};
+  for (int i = 0; i < nkey; i++) st_n[i] = 0;
   for (int keyF = 0; keyF < nkey; keyF++) {
     const int kF = keyF >> 1, tauF = keyF & 1;
     const int sigF = (kF % 3) * tauF;
@@ -237,7 +240,9 @@ static void build_stencil(const Basis& bI, const Basis& bF, const std::vector<do
         if (slot < 0) continue;
         const int sigI = (kI % 3) * tauI;
         const double sgnI = ((sigI + kI) & 1) ? -1.0 : 1.0;
-        const double f3j = threej[jI + kI * J1 + (jF - jI + 1) * J1 * J1 + (kF - kI + 1) * J1 * J1 * 3];
+        const double f3j =
+            threej ? threej[jI + kI * J1 + (jF - jI + 1) * J1 * J1 + (kF - kI + 1) * J1 * J1 * 3]
+                   : three_j(jI, 1, jF, kI, kF - kI, -kF);
         int comp;
         double L;
         if (kF == kI) {
@@ -256,6 +261,14 @@ static void build_stencil(const Basis& bI, const Basis& bF, const std::vector<do
         st[(size_t)keyF * 6 + st_n[keyF]++] = StencilTerm{slot, comp, coef};
       }
   }
+}
+
+static void build_stencil(const Basis& bI, const Basis& bF, const std::vector<double>& threej,
+                          int tj_jmax, std::vector<StencilTerm>& st, std::vector<int32_t>& st_n) {
+  const int nkey = 2 * bF.J + 2;
+  st.resize((size_t)nkey * 6);
+  st_n.resize(nkey);
+  stencil_fill(bI, bF, threej.data(), tj_jmax, st.data(), st_n.data());
 }
 
 // ------------------------------------------------------------------ job plan

@@ -187,6 +187,28 @@ gi_status gi_get_stats(gi_ctx* ctx, gi_stats* out);
 gi_status gi_half_ls(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF, const double* vsym,
                      double* half_ls);
 
+/* Allocation-free variant of gi_half_ls.  No counterpart in the reference.
+   For callers that cannot allocate device memory when they compute a half
+   line strength: a serving loop whose HBM is fully reserved by its admission
+   budget, a host framework or eigensolver that owns device memory through its
+   own pool, or a latency-sensitive caller that cannot afford the implicit
+   device-wide synchronisation of cudaMalloc/cudaFree.  The call allocates
+   nothing: vsym_dev (nsize doubles of block (jI, gammaI)) and half_ls_dev
+   (D_F doubles) are device buffers the caller owns, and the scratch is one
+   fixed device array of GI_NOALLOC_SCRATCH_BYTES inside the library, held by
+   every GPU that loads it until the process exits.  Limits: degen(gammaI) *
+   (number of (k, tau) slots of J=jI) * round_up(N, 64) <= 2^19 and
+   jI, jF <= 255; larger sizes return GI_ERR_ARG (use gi_half_ls).  The work is
+   enqueued on `stream` (a cudaStream_t; NULL = the context's stream) and the
+   call returns without waiting.  All calls share the scratch array, which
+   keeps the last call's contents: calls whose work overlaps on the GPU race,
+   so order them (one stream, or events).  The first call on a device looks up
+   the array's device address once (cudaGetSymbolAddress) with that device
+   current; make that first call before any stream capture. */
+#define GI_NOALLOC_SCRATCH_BYTES ((16u << 20) + (52u << 10))
+gi_status gi_half_ls_noalloc(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF,
+                             const double* vsym_dev, double* half_ls_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
