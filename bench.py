@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--jmax", type=int, default=None, help="restrict J to 0..jmax")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--slices", type=int, default=0, help="bf16 digits per operand (split)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
@@ -232,7 +233,7 @@ def main_ours(args):
             torch.distributed.barrier()
 
     eng = pkg.Engine(local)
-    eng.load(prob, precision=prec)
+    eng.load(prob, precision=prec, split_slices=args.slices)
     for _ in range(args.warmup):
         eng.run(lines_on_device=True)
     torch.cuda.synchronize()

@@ -93,7 +93,10 @@ struct Level {
   double energy;
 };
 
+struct SplitState;  // split-precision state (split.cu)
+
 struct Ctx {
+  SplitState* split = nullptr;
   int device = 0;
   size_t budget = 0;
   int nsm = 0;

@@ -633,6 +633,10 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   unsigned long long counts[2] = {0, 0};
   GI_CUDA(c, cudaMemcpyAsync(counts, c->w_counter.p, sizeof(counts), cudaMemcpyDeviceToHost, c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (P.precision == GI_PREC_SPLIT) {
+    gi_status s = split_check(c);
+    if (s != GI_OK) return s;
+  }
   const unsigned long long count = counts[0];
   if (count > c->d_lines.n) return fail(c, GI_ERR_DEVICE, "line buffer overflow (%llu lines)", count);
   c->nlines = (int64_t)count;

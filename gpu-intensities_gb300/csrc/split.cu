@@ -1,16 +1,582 @@
-// Split-precision GEMMs: placeholder until the tcgen05 kernels land.
+// Split-precision GEMMs on the tcgen05 tensor pipe (sm_103a).
+//
+// C[z][n*ldc + m] = sum_k A[z][m][k] * B[n][k] in FP64 accuracy from bf16
+// tensor-core products (an Ozaki-style error-free splitting):
+//
+//   * every row r of A (and of B) is scaled by 2^-e_r so that |x| < 1 and
+//     split into s integer digits of w bits,
+//       x = sum_p a_p 2^(-w(p+1)) + tail,  a_0 in [-2^w, 2^w],
+//       a_p in [-2^(w-1), 2^(w-1)] (p >= 1), |tail| <= 2^-(ws+1),
+//     each digit an exact bf16 integer;
+//   * the products a_p * b_q with p + q = d <= s-1 share the weight 2^(-wd);
+//     each diagonal d is accumulated in its own fp32 TMEM accumulator, where
+//     sums of integer products stay exact while they stay below 2^24 (for
+//     w = 6 and K <= 2048 that holds in the worst case for d <= 5; diagonals
+//     beyond carry weights <= 2^-36 so fp32 rounding there is negligible);
+//   * the epilogue combines the diagonals in FP64 (Horner in 2^-w) and
+//     rescales by 2^(e_m + e_n - 2w).
+//
+// Kernel: one 128 x BN output tile per CTA; warp 0 issues TMA loads (one 3-D
+// box brings all s digit planes of a 32-wide K block), warp 1 (one thread)
+// issues tcgen05.mma for every digit pair of the block, warps 2-5 read the s
+// accumulators from TMEM and write FP64.  Every mbarrier wait is bounded by
+// %globaltimer; a timeout sets a device error word and the CTA unwinds.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+
 #include "split.h"
 
 namespace gi {
-gi_status split_gemm_dipole(Ctx* c, const double*, int, double*, int, size_t, int) {
-  c->err = "split precision not available in this build";
-  return GI_ERR_ARG;
+namespace {
+
+constexpr int kBM = 128;       // tile rows (MMA M)
+constexpr int kBK = 32;        // K elements per stage (64 bytes: SWIZZLE_64B rows)
+constexpr int kStages = 2;
+constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
+constexpr int kMaxSlices = 10;
+constexpr int kDefaultSlices = 9;
+constexpr int kDefaultW = 6;
+
+struct SplitShape {
+  int s, w, bn;
+};
+
+__host__ __device__ constexpr int bn_for(int s) { return s <= 8 ? 64 : 48; }
+// At least 120 KB so that one CTA holds an SM (it allocates all 512 TMEM columns).
+size_t smem_bytes(int s, int bn) {
+  const size_t need = (size_t)kStages * s * (kBM + bn) * kBK * 2 + 1024 /*align*/ + 256;
+  return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;
 }
-gi_status split_gemm_final(Ctx* c, const double*, int, int, const double*, int, int, double*, int) {
-  c->err = "split precision not available in this build";
-  return GI_ERR_ARG;
+
+// ------------------------------------------------------------------ PTX
+__device__ __forceinline__ uint32_t sptr(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
 }
-gi_status split_prepare(Ctx*) { return GI_OK; }
-void split_invalidate(Ctx*) {}
-void split_release(Ctx*) {}
+__device__ __forceinline__ void mbar_init(uint64_t* b, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(sptr(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(sptr(b)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ uint32_t mbar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(sptr(b)), "r"(parity)
+      : "memory");
+  return ok;
+}
+__device__ __forceinline__ uint64_t gtimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;\n" : "=l"(t));
+  return t;
+}
+// Bounded wait on an mbarrier phase.  Returns false when the CTA is aborting
+// (another warp timed out) or this wait exceeded its time limit (then it
+// raises the abort itself and records the error).
+__device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err,
+                          int code) {
+  uint64_t t0 = 0;
+  for (uint32_t it = 1;; ++it) {
+    if (mbar_try(b, parity)) return true;
+    if ((it & 63) == 0) {
+      if (*abort_flag) return false;
+      const uint64_t t = gtimer();
+      if (t0 == 0) {
+        t0 = t;
+      } else if (t - t0 > 4000000000ull) {  // 4 s: far beyond any tile's work
+        *abort_flag = 1;
+        atomicExch(err, code);
+        return false;
+      }
+    }
+  }
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];\n" ::"r"(sptr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(sptr(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+// Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 64
+// bytes (32 elements) with the 64-byte swizzle: 8-row groups 512 bytes apart.
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
+  d |= (uint64_t)1 << 16;                          // leading byte offset (unused here)
+  d |= (uint64_t)((512 >> 4) & 0x3FFF) << 32;      // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)1 << 46;                          // descriptor version (tcgen05)
+  d |= (uint64_t)4 << 61;                          // SWIZZLE_64B
+  return d;
+}
+// Instruction descriptor: kind::f16, bf16 x bf16 -> f32, K-major A and B.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4)                    // D format f32
+         | (1u << 7)                  // A format bf16
+         | (1u << 10)                 // B format bf16
+         | ((uint32_t)(N >> 3) << 17)  // N
+         | ((uint32_t)(M >> 4) << 24); // M
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          sptr(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// ------------------------------------------------------------------ GEMM
+template <int S, int BN>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                 const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
+                 int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int* err) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t kAbytes = S * kBM * kBK * 2;
+  constexpr uint32_t kBbytes = S * BN * kBK * 2;
+  constexpr uint32_t kStage = kAbytes + kBbytes;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStage);
+  uint64_t* empty = full + kStages;
+  uint64_t* accf = empty + kStages;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(accf + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * kBM, z = blockIdx.z;
+  const int nk = K / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kStages; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(accf, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {  // the whole warp allocates all 512 TMEM columns
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     sptr(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      int issued = 0;
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % kStages;
+        if (kb >= kStages && !mbar_wait(&empty[st], ((kb / kStages) - 1) & 1, abort_flag, err, 1))
+          break;
+        unsigned char* sa = smem + st * kStage;
+        mbar_expect_tx(&full[st], kStage);
+        tma_load_3d(sa, &tmA, &full[st], kb * kBK, z * Mpad + m0, 0);
+        tma_load_3d(sa + kAbytes, &tmB, &full[st], kb * kBK, n0, 0);
+        issued = kb + 1;
+      }
+      if (*abort_flag) {
+        // let the copies still in flight land before the CTA's smem goes away
+        for (int kb = (issued > kStages ? issued - kStages : 0); kb < issued; ++kb) {
+          uint64_t t0 = gtimer();
+          while (!mbar_try(&full[kb % kStages], (kb / kStages) & 1) && gtimer() - t0 < 1000000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = idesc_bf16(kBM, BN);
+      for (int kb = 0; kb < nk; ++kb) {
+        const int st = kb % kStages;
+        if (!mbar_wait(&full[st], (kb / kStages) & 1, abort_flag, err, 2)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t a0 = sptr(smem + st * kStage);
+        const uint32_t b0 = a0 + kAbytes;
+#pragma unroll
+        for (int ks = 0; ks < kBK / 16; ++ks) {
+#pragma unroll
+          for (int d = 0; d < S; ++d) {
+#pragma unroll
+            for (int p = 0; p <= d; ++p) {
+              const int q = d - p;
+              const uint64_t ad = sdesc_sw64(a0 + p * (kBM * kBK * 2) + ks * 32);
+              const uint64_t bd = sdesc_sw64(b0 + q * (BN * kBK * 2) + ks * 32);
+              const uint32_t acc = (kb > 0 || ks > 0 || p > 0) ? 1u : 0u;
+              mma_bf16(tmem + d * BN, ad, bd, idesc, acc);
+            }
+          }
+        }
+        mma_commit(&empty[st]);  // the stage is free once these MMAs have read it
+      }
+      mma_commit(accf);  // all accumulators final
+      if (*abort_flag) {
+        // the MMAs already issued must finish before TMEM is released
+        uint64_t t0 = gtimer();
+        while (!mbar_try(accf, 0) && gtimer() - t0 < 1000000000ull) {
+        }
+      }
+    }
+  } else {
+    // epilogue warps 2..5: TMEM lane quarter = warp % 4
+    const int q4 = warp & 3;
+    const int m = m0 + q4 * 32 + lane;
+    const bool ok = mbar_wait(accf, 0, abort_flag, err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    if (ok) {
+      const double inv = 1.0 / (double)(1 << w);
+      const int emr = (m < M) ? ea[z * Mpad + m] : 0;
+      double* Cz = C + (size_t)z * strideC;
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        double v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0.0;
+        for (int d = S - 1; d >= 0; --d) {
+          float f[16];
+          tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + d * BN + c0, f);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = fma(v[j], inv, (double)f[j]);
+        }
+        if (m < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < Nc) Cz[(size_t)n * ldc + m] = ldexp(v[j], emr + eb[n] - 2 * w);
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
+// ------------------------------------------------------------------ slicing
+// One warp per row: the row's max |x| sets the exponent e (|x| 2^-e < 1), then
+// s digit planes of w bits are written as bf16 integers, plane-major:
+// out[p][r][k].  Rows beyond `rows` and columns k >= K are zero.
+__global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, int K,
+                             int rows_pad, int s, int w, __nv_bfloat16_raw* __restrict__ out,
+                             size_t plane, int32_t* __restrict__ e_out) {
+  const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= rows_pad) return;
+  const double* x = X + (size_t)r * ldx;
+  double mx = 0.0;
+  if (r < rows)
+    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(x[k]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  int e = 0;
+  if (mx > 0.0) e = ilogb(mx) + 1;  // 2^(e-1) <= mx < 2^e
+  if (lane == 0) e_out[r] = e;
+  const double scale_w = (double)(1 << w);
+  for (int k = lane; k < K; k += 32) {
+    double t = (r < rows) ? ldexp(x[k], -e) : 0.0;
+    for (int p = 0; p < s; ++p) {
+      t *= scale_w;
+      const double a = rint(t);
+      t -= a;
+      const __nv_bfloat16 b = __float2bfloat16_rn((float)a);  // |a| <= 2^w: exact
+      out[(size_t)p * plane + (size_t)r * K + k] = *reinterpret_cast<const __nv_bfloat16_raw*>(&b);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ host
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 3-D map over digit planes [s][rows][K] of bf16 with a (32, box_rows, s) box.
+bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)s};
+  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)K * rows * 2};
+  cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, (cuuint32_t)s};
+  cuuint32_t es[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+SplitShape shape_of(const Ctx* c) {
+  int s = c->params.split_slices > 0 ? c->params.split_slices : kDefaultSlices;
+  s = std::min(std::max(s, 2), kMaxSlices);
+  return SplitShape{s, kDefaultW, bn_for(s)};
+}
+
+template <int S>
+cudaError_t launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const int32_t* ea,
+                        const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
+                        int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
+  constexpr int BN = bn_for(S);
+  const size_t sm = smem_bytes(S, BN);
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_split_gemm<S, BN>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  dim3 grid((Nc + BN - 1) / BN, (M + kBM - 1) / kBM, batch);
+  k_split_gemm<S, BN><<<grid, kThreads, sm, st>>>(tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc,
+                                                  K, w, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gemm_s(int s, const CUtensorMap& tA, const CUtensorMap& tB, const int32_t* ea,
+                          const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
+                          int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
+  switch (s) {
+#define GI_S(SS) \
+  case SS: return launch_gemm<SS>(tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, err, st);
+    GI_S(2) GI_S(3) GI_S(4) GI_S(5) GI_S(6) GI_S(7) GI_S(8) GI_S(9) GI_S(10)
+#undef GI_S
+  }
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s, int w,
+                  __nv_bfloat16_raw* out, int32_t* e, cudaStream_t st) {
+  if (rows_pad <= 0) return cudaSuccess;
+  const int wpb = 8;
+  k_slice_rows<<<(rows_pad + wpb - 1) / wpb, wpb * 32, 0, st>>>(
+      X, ldx, rows, K, rows_pad, s, w, out, (size_t)rows_pad * K, e);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+// Per-context state of the split path.
+struct SplitState {
+  int s = 0, w = 0;
+  int N = -1;                                 // dipole the slices belong to
+  DevArray<__nv_bfloat16_raw> mu_slices;      // [s][3*Mpad][Kp]
+  DevArray<int32_t> mu_exp;                   // [3*Mpad]
+  int Mpad = 0;
+  DevArray<__nv_bfloat16_raw> b_slices;       // workspace: [s][rows][K]
+  DevArray<int32_t> b_exp;
+  DevArray<__nv_bfloat16_raw> v_slices;       // workspace for the final-state vectors
+  DevArray<int32_t> v_exp;
+  DevArray<int> err;
+};
+
+static SplitState* state(Ctx* c) {
+  if (!c->split) c->split = new SplitState();
+  return c->split;
+}
+
+static gi_status check(Ctx* c, cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return GI_OK;
+  c->err = std::string("split precision: ") + what + ": " + cudaGetErrorString(e);
+  return e == cudaErrorMemoryAllocation ? GI_ERR_NOMEM : GI_ERR_CUDA;
+}
+
+gi_status split_prepare(Ctx* c) {
+  SplitState* S = state(c);
+  const SplitShape sh = shape_of(c);
+  if (!encode_fn()) {
+    c->err = "split precision: cuTensorMapEncodeTiled unavailable";
+    return GI_ERR_CUDA;
+  }
+  gi_status g = check(c, S->err.reserve(1), "error word");
+  if (g != GI_OK) return g;
+  g = check(c, cudaMemsetAsync(S->err.p, 0, sizeof(int), c->stream), "error word");
+  if (g != GI_OK) return g;
+  if (S->N == c->N && S->s == sh.s && S->w == sh.w) return GI_OK;
+  // digit planes of the dipole: rows = 3 components x Mpad, K = Kp
+  S->s = sh.s;
+  S->w = sh.w;
+  S->Mpad = round_up(c->N, kBM);
+  const size_t rows = (size_t)3 * S->Mpad;
+  g = check(c, S->mu_slices.alloc((size_t)sh.s * rows * c->Kp), "dipole slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->mu_exp.alloc(rows), "dipole exponents");
+  if (g != GI_OK) return g;
+  // slice all three components at once: the padded dipole is [3][N][Kp]; the
+  // planes want [3][Mpad] rows, so slice component by component into a
+  // temporary plane set and copy row blocks
+  DevArray<__nv_bfloat16_raw> tmp;
+  DevArray<int32_t> texp;
+  g = check(c, tmp.alloc((size_t)sh.s * S->Mpad * c->Kp), "dipole slice temp");
+  if (g != GI_OK) return g;
+  g = check(c, texp.alloc(S->Mpad), "dipole exp temp");
+  if (g != GI_OK) return g;
+  for (int comp = 0; comp < 3; ++comp) {
+    g = check(c,
+              slice(c->d_mu.p + (size_t)comp * c->N * c->Kp, c->Kp, c->N, c->Kp, S->Mpad, sh.s,
+                    sh.w, tmp.p, texp.p, c->stream),
+              "slice dipole");
+    if (g != GI_OK) return g;
+    for (int p = 0; p < sh.s; ++p) {
+      g = check(c,
+                cudaMemcpyAsync(S->mu_slices.p + ((size_t)p * rows + (size_t)comp * S->Mpad) * c->Kp,
+                                tmp.p + (size_t)p * S->Mpad * c->Kp,
+                                sizeof(__nv_bfloat16_raw) * S->Mpad * c->Kp,
+                                cudaMemcpyDeviceToDevice, c->stream),
+                "copy dipole planes");
+      if (g != GI_OK) return g;
+    }
+    g = check(c,
+              cudaMemcpyAsync(S->mu_exp.p + (size_t)comp * S->Mpad, texp.p,
+                              sizeof(int32_t) * S->Mpad, cudaMemcpyDeviceToDevice, c->stream),
+              "copy dipole exponents");
+    if (g != GI_OK) return g;
+  }
+  g = check(c, cudaStreamSynchronize(c->stream), "slice dipole sync");
+  if (g != GI_OK) return g;
+  S->N = c->N;
+  return GI_OK;
+}
+
+static gi_status gemm(Ctx* c, const __nv_bfloat16_raw* Aslices, int Arows_total, const int32_t* ea,
+                      int Mpad, const __nv_bfloat16_raw* Bslices, int Brows, const int32_t* eb,
+                      double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch) {
+  SplitState* S = state(c);
+  CUtensorMap tA, tB;
+  const int bn = bn_for(S->s);
+  if (!make_map(&tA, Aslices, K, Arows_total, S->s, kBM) ||
+      !make_map(&tB, Bslices, K, Brows, S->s, bn)) {
+    c->err = "split precision: cuTensorMapEncodeTiled failed";
+    return GI_ERR_CUDA;
+  }
+  return check(c, launch_gemm_s(S->s, tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch,
+                                S->w, S->err.p, c->stream),
+               "split GEMM launch");
+}
+
+gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zstride,
+                            int ncol) {
+  SplitState* S = state(c);
+  const int K = c->Kp;
+  gi_status g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "Y slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->b_exp.reserve(ncol), "Y exponents");
+  if (g != GI_OK) return g;
+  g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+              return slice(Y, ldy, ncol, K, ncol, S->s, S->w, S->b_slices.p, S->b_exp.p,
+                           c->stream);
+            }),
+            "slice Y");
+  if (g != GI_OK) return g;
+  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * K * 3;
+  gi_status r = GI_OK;
+  cudaError_t e = timed(c, GI_PHASE_HALFLS_GEMM, [&] {
+    r = gemm(c, S->mu_slices.p, 3 * S->Mpad, S->mu_exp.p, S->Mpad, S->b_slices.p, ncol,
+             S->b_exp.p, Z, ldz, zstride, c->N, ncol, K, 3);
+    return cudaSuccess;
+  });
+  (void)e;
+  return r;
+}
+
+gi_status split_gemm_final(Ctx* c, const double* V, int ldv, int nvec, const double* H, int ldh,
+                           int ncol, double* T, int ldt) {
+  SplitState* S = state(c);
+  const int K = ldh;
+  const int vpad = round_up(nvec, kBM);
+  gi_status g = check(c, S->v_slices.reserve((size_t)S->s * vpad * K), "V slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->v_exp.reserve(vpad), "V exponents");
+  if (g != GI_OK) return g;
+  g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "H slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->b_exp.reserve(ncol), "H exponents");
+  if (g != GI_OK) return g;
+  g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+              cudaError_t e = slice(V, ldv, nvec, K, vpad, S->s, S->w, S->v_slices.p, S->v_exp.p,
+                                    c->stream);
+              if (e != cudaSuccess) return e;
+              return slice(H, ldh, ncol, K, ncol, S->s, S->w, S->b_slices.p, S->b_exp.p,
+                           c->stream);
+            }),
+            "slice V/H");
+  if (g != GI_OK) return g;
+  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * nvec * (double)ncol * K;
+  gi_status r = GI_OK;
+  timed(c, GI_PHASE_FINAL_GEMM, [&] {
+    r = gemm(c, S->v_slices.p, vpad, S->v_exp.p, vpad, S->b_slices.p, ncol, S->b_exp.p, T, ldt,
+             0, nvec, ncol, K, 1);
+    return cudaSuccess;
+  });
+  return r;
+}
+
+gi_status split_check(Ctx* c) {
+  if (!c->split || !c->split->err.p) return GI_OK;
+  int e = 0;
+  if (cudaMemcpy(&e, c->split->err.p, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return GI_ERR_CUDA;
+  if (e) {
+    char buf[128];
+    snprintf(buf, sizeof(buf), "split GEMM: a pipeline wait timed out (code %d)", e);
+    c->err = buf;
+    return GI_ERR_DEVICE;
+  }
+  return GI_OK;
+}
+
+void split_invalidate(Ctx* c) {
+  if (c->split) c->split->N = -1;
+}
+
+void split_release(Ctx* c) {
+  delete c->split;
+  c->split = nullptr;
+}
+
 }  // namespace gi

@@ -12,5 +12,7 @@ gi_status split_gemm_final(Ctx* c, const double* V, int ldv, int nvec, const dou
 // Called once per run before the launch loop (sizes workspaces, slices the dipole).
 gi_status split_prepare(Ctx* c);
 void split_invalidate(Ctx* c);  // the dipole changed: drop its cached slices
+// After a run: reads the device error word the split kernels set on a timeout.
+gi_status split_check(Ctx* c);
 void split_release(Ctx* c);
 }  // namespace gi

@@ -1,0 +1,44 @@
+"""Split-precision path (bf16 digit GEMMs on tcgen05) against the CPU oracle:
+identical line selection and <= 1e-10 relative error on S."""
+import numpy as np
+import pytest
+
+from paritylib import compare
+
+pytestmark = pytest.mark.gpu
+
+
+def run(pkg, prob, slices=0):
+    with pkg.Engine(0) as eng:
+        eng.load(prob, precision=pkg.GI_PREC_SPLIT, split_slices=slices)
+        eng.run()
+        return pkg.keyed(eng.lines(), eng.levels()), eng.stats()
+
+
+@pytest.mark.parametrize("case", ["c2v", "c3v", "c3v_reduced"])
+def test_split_matches_oracle(pkg, synth, oracle, case):
+    if case == "c2v":
+        prob = synth.make_c2v(11, 30, [0, 1, 2, 3], nvec_max=8)
+    else:
+        prob = synth.make_c3v(12, 24, [0, 1, 2, 3], nvec_max=8, reduced=case.endswith("reduced"))
+    got, st = run(pkg, prob)
+    res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
+    assert st["flops_tensor"] > 0
+    print(case, res)
+
+
+def test_split_small_workload(pkg, synth, oracle):
+    prob = synth.workload("c2v_small", seed=1)
+    got, st = run(pkg, prob)
+    res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
+    print(res, st["seconds_gpu"])
+
+
+@pytest.mark.parametrize("slices", [6, 9, 10])
+def test_split_slice_counts(pkg, synth, oracle, slices):
+    prob = synth.make_c2v(4, 40, [0, 1, 2], nvec_max=10)
+    got, _ = run(pkg, prob, slices)
+    ref = oracle.run_all(prob)
+    tol = {6: 1e-6, 9: 1e-10, 10: 1e-10}[slices]
+    res = compare(got, ref, rtol_S=tol, norm_tol=tol / 100)
+    print(slices, res)
