@@ -86,6 +86,11 @@ struct Block {
   std::vector<double> energies;
   std::vector<int32_t> quanta;                          // [nvec][nmodes+1]
   DevArray<double> d_energies;
+  // bf16 digit planes of the vectors for the split-precision path (cut on
+  // first use, dropped when the block is replaced)
+  DevArray<uint16_t> d_digits;
+  DevArray<int32_t> d_digit_exp;
+  int digits_s = 0, digits_w = 0;
 };
 
 struct Level {

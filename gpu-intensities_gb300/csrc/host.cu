@@ -591,8 +591,7 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
                                       c->w_stencil_n.p + pp->st_off, 6, c->w_h.p, c->stream);
               }));
       if (P.precision == GI_PREC_SPLIT) {
-        gi_status s = split_gemm_final(c, fb.d_vecs.p, fb.ld, fb.nvec, c->w_h.p, ldh, ncolH,
-                                       c->w_t.p, ldt);
+        gi_status s = split_gemm_final(c, *Fp.blk, c->w_h.p, ldh, ncolH, c->w_t.p, ldt);
         if (s != GI_OK) return s;
       } else {
         GI_CUDA(c, timed(c, GI_PHASE_FINAL_GEMM, [&] {
@@ -840,6 +839,7 @@ gi_status gi_set_block(gi_ctx* h, int J, int gamma, int nsize, int nvec, const d
   b->nsize = nsize;
   b->nvec = nvec;
   b->ld = round_up(nsize, 64);
+  b->digits_s = 0;  // new vectors: their split-precision digits are stale
   b->energies.assign(energies, energies + nvec);
   const int nq = c->params.nmodes + 1;
   b->quanta.assign(quanta, quanta + (size_t)nvec * nq);

@@ -258,24 +258,40 @@ __global__ void __launch_bounds__(kThreads, 1)
     const bool ok = mbar_wait(accf, 0, abort_flag, err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (ok) {
-      const double inv = 1.0 / (double)(1 << w);
+      // The accumulators hold integers (|acc| < 2^31), so the diagonals are
+      // combined exactly in two int64 words, hi = sum_{d<kHi} acc_d 2^(w(kHi-1-d))
+      // (< 2^53) and lo = sum_{d>=kHi} acc_d 2^(w(S-1-d)); FP64 is used only
+      // for the final value hi 2^(E-w(kHi-1)) + lo 2^(E-w(S-1)).
+      constexpr int kHi = S < 4 ? S : 4;
       const int emr = (m < M) ? ea[z * Mpad + m] : 0;
       double* Cz = C + (size_t)z * strideC;
       for (int c0 = 0; c0 < BN; c0 += 16) {
-        double v[16];
+        long long hi[16], lo[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = 0.0;
-        for (int d = S - 1; d >= 0; --d) {
+        for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0;
+#pragma unroll
+        for (int d = 0; d < S; ++d) {
           float f[16];
           tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + d * BN + c0, f);
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = fma(v[j], inv, (double)f[j]);
+          for (int j = 0; j < 16; ++j) {
+            const long long a = (long long)__float2int_rn(f[j]);
+            if (d < kHi)
+              hi[j] = (hi[j] << w) + a;
+            else
+              lo[j] = (lo[j] << w) + a;
+          }
         }
         if (m < M) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             const int n = n0 + c0 + j;
-            if (n < Nc) Cz[(size_t)n * ldc + m] = ldexp(v[j], emr + eb[n] - 2 * w);
+            if (n < Nc) {
+              const int E = emr + eb[n] - 2 * w;
+              const double v = ldexp((double)hi[j], E - w * (kHi - 1)) +
+                               ldexp((double)lo[j], E - w * (S - 1));
+              Cz[(size_t)n * ldc + m] = v;
+            }
           }
         }
       }
@@ -290,34 +306,81 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 // ------------------------------------------------------------------ slicing
-// One warp per row: the row's max |x| sets the exponent e (|x| 2^-e < 1), then
-// s digit planes of w bits are written as bf16 integers, plane-major:
-// out[p][r][k].  Rows beyond `rows` and columns k >= K are zero.
+// FP64 arithmetic is scarce on this GPU, so the digits are cut with integer
+// operations on the bit pattern.  For a row with exponent e (max|x| < 2^e),
+// each element becomes the fixed-point integer X = round(x 2^(ws - e)),
+// |X| < 2^(ws), and X is split from the bottom into balanced base-2^w digits:
+// a_p in [-2^(w-1), 2^(w-1)) for p >= 1 and the remaining top digit
+// |a_0| <= 2^w, so X = sum_p a_p 2^(w(s-1-p)) exactly.
+
+// Row exponent from the largest magnitude's bit pattern: 2^(e-1) <= max < 2^e.
+__device__ __forceinline__ int row_exponent(unsigned long long maxbits) {
+  if (maxbits == 0) return 0;
+  const int eb = (int)(maxbits >> 52);
+  return eb ? eb - 1022 : -1021 - (__clzll((long long)maxbits) - 12);
+}
+
+__device__ __forceinline__ long long fixed_point(double x, int e, int ws) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const int eb = (int)((b >> 52) & 0x7FF);
+  const long long mant = (long long)(b & 0xFFFFFFFFFFFFFull) | (eb ? (1ll << 52) : 0ll);
+  const int sh = (eb ? eb : 1) - 1075 - e + ws;  // x 2^(ws-e) = mant 2^sh
+  long long X;
+  if (sh >= 0) {
+    X = mant << sh;
+  } else if (sh > -54) {
+    X = (mant + (1ll << (-sh - 1))) >> (-sh);  // round half up
+  } else {
+    X = 0;
+  }
+  return (b >> 63) ? -X : X;
+}
+
+__device__ __forceinline__ uint16_t bf16_of_int(int a) {
+  const __nv_bfloat16 h = __float2bfloat16_rn((float)a);  // |a| <= 256: exact
+  return *reinterpret_cast<const uint16_t*>(&h);
+}
+
+// One warp per row, two elements per lane: out[p][r][k] (plane-major) and the
+// row exponent.  Rows beyond `rows` are zero; K is even.
 __global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, int K,
-                             int rows_pad, int s, int w, __nv_bfloat16_raw* __restrict__ out,
+                             int rows_pad, int s, int w, uint32_t* __restrict__ out,
                              size_t plane, int32_t* __restrict__ e_out) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= rows_pad) return;
-  const double* x = X + (size_t)r * ldx;
-  double mx = 0.0;
+  const double2* x2 = reinterpret_cast<const double2*>(X + (size_t)r * ldx);
+  const int K2 = K >> 1;
+  unsigned long long mx = 0;
   if (r < rows)
-    for (int k = lane; k < K; k += 32) mx = fmax(mx, fabs(x[k]));
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  int e = 0;
-  if (mx > 0.0) e = ilogb(mx) + 1;  // 2^(e-1) <= mx < 2^e
-  if (lane == 0) e_out[r] = e;
-  const double scale_w = (double)(1 << w);
-  for (int k = lane; k < K; k += 32) {
-    double t = (r < rows) ? ldexp(x[k], -e) : 0.0;
-    for (int p = 0; p < s; ++p) {
-      t *= scale_w;
-      const double a = rint(t);
-      t -= a;
-      const __nv_bfloat16 b = __float2bfloat16_rn((float)a);  // |a| <= 2^w: exact
-      out[(size_t)p * plane + (size_t)r * K + k] = *reinterpret_cast<const __nv_bfloat16_raw*>(&b);
+    for (int k = lane; k < K2; k += 32) {
+      const double2 v = x2[k];
+      mx = max(mx, (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull);
+      mx = max(mx, (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull);
     }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int e = row_exponent(mx);
+  if (lane == 0) e_out[r] = e;
+  const int ws = w * s;
+  const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
+  uint32_t* o = out + ((size_t)r * K >> 1);
+  for (int k = lane; k < K2; k += 32) {
+    long long X0 = 0, X1 = 0;
+    if (r < rows) {
+      const double2 v = x2[k];
+      X0 = fixed_point(v.x, e, ws);
+      X1 = fixed_point(v.y, e, ws);
+    }
+    for (int p = s - 1; p >= 1; --p) {
+      const long long a0 = ((X0 + half) & mask) - half;
+      const long long a1 = ((X1 + half) & mask) - half;
+      X0 = (X0 - a0) >> w;
+      X1 = (X1 - a1) >> w;
+      o[(size_t)p * (plane >> 1) + k] =
+          (uint32_t)bf16_of_int((int)a0) | ((uint32_t)bf16_of_int((int)a1) << 16);
+    }
+    o[k] = (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
   }
 }
 
@@ -391,11 +454,12 @@ cudaError_t launch_gemm_s(int s, const CUtensorMap& tA, const CUtensorMap& tB, c
 }
 
 cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s, int w,
-                  __nv_bfloat16_raw* out, int32_t* e, cudaStream_t st) {
+                  uint16_t* out, int32_t* e, cudaStream_t st) {
   if (rows_pad <= 0) return cudaSuccess;
   const int wpb = 8;
+  if (K & 1) return cudaErrorInvalidValue;
   k_slice_rows<<<(rows_pad + wpb - 1) / wpb, wpb * 32, 0, st>>>(
-      X, ldx, rows, K, rows_pad, s, w, out, (size_t)rows_pad * K, e);
+      X, ldx, rows, K, rows_pad, s, w, reinterpret_cast<uint32_t*>(out), (size_t)rows_pad * K, e);
   return cudaGetLastError();
 }
 
@@ -405,12 +469,12 @@ cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s
 struct SplitState {
   int s = 0, w = 0;
   int N = -1;                                 // dipole the slices belong to
-  DevArray<__nv_bfloat16_raw> mu_slices;      // [s][3*Mpad][Kp]
+  DevArray<uint16_t> mu_slices;      // [s][3*Mpad][Kp]
   DevArray<int32_t> mu_exp;                   // [3*Mpad]
   int Mpad = 0;
-  DevArray<__nv_bfloat16_raw> b_slices;       // workspace: [s][rows][K]
+  DevArray<uint16_t> b_slices;       // workspace: [s][rows][K]
   DevArray<int32_t> b_exp;
-  DevArray<__nv_bfloat16_raw> v_slices;       // workspace for the final-state vectors
+  DevArray<uint16_t> v_slices;       // workspace for the final-state vectors
   DevArray<int32_t> v_exp;
   DevArray<int> err;
 };
@@ -450,7 +514,7 @@ gi_status split_prepare(Ctx* c) {
   // slice all three components at once: the padded dipole is [3][N][Kp]; the
   // planes want [3][Mpad] rows, so slice component by component into a
   // temporary plane set and copy row blocks
-  DevArray<__nv_bfloat16_raw> tmp;
+  DevArray<uint16_t> tmp;
   DevArray<int32_t> texp;
   g = check(c, tmp.alloc((size_t)sh.s * S->Mpad * c->Kp), "dipole slice temp");
   if (g != GI_OK) return g;
@@ -466,7 +530,7 @@ gi_status split_prepare(Ctx* c) {
       g = check(c,
                 cudaMemcpyAsync(S->mu_slices.p + ((size_t)p * rows + (size_t)comp * S->Mpad) * c->Kp,
                                 tmp.p + (size_t)p * S->Mpad * c->Kp,
-                                sizeof(__nv_bfloat16_raw) * S->Mpad * c->Kp,
+                                sizeof(uint16_t) * S->Mpad * c->Kp,
                                 cudaMemcpyDeviceToDevice, c->stream),
                 "copy dipole planes");
       if (g != GI_OK) return g;
@@ -483,8 +547,8 @@ gi_status split_prepare(Ctx* c) {
   return GI_OK;
 }
 
-static gi_status gemm(Ctx* c, const __nv_bfloat16_raw* Aslices, int Arows_total, const int32_t* ea,
-                      int Mpad, const __nv_bfloat16_raw* Bslices, int Brows, const int32_t* eb,
+static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const int32_t* ea,
+                      int Mpad, const uint16_t* Bslices, int Brows, const int32_t* eb,
                       double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch) {
   SplitState* S = state(c);
   CUtensorMap tA, tB;
@@ -524,33 +588,44 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
   return r;
 }
 
-gi_status split_gemm_final(Ctx* c, const double* V, int ldv, int nvec, const double* H, int ldh,
-                           int ncol, double* T, int ldt) {
+gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol, double* T,
+                           int ldt) {
   SplitState* S = state(c);
   const int K = ldh;
+  const int nvec = fb.nvec;
   const int vpad = round_up(nvec, kBM);
-  gi_status g = check(c, S->v_slices.reserve((size_t)S->s * vpad * K), "V slices");
-  if (g != GI_OK) return g;
-  g = check(c, S->v_exp.reserve(vpad), "V exponents");
-  if (g != GI_OK) return g;
+  gi_status g;
+  // the final-state vectors are fixed inputs: their digits are cut once and
+  // kept with the block until it is replaced
+  if (fb.digits_s != S->s || fb.digits_w != S->w) {
+    g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
+    if (g != GI_OK) return g;
+    g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
+    if (g != GI_OK) return g;
+    g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, fb.d_digits.p,
+                             fb.d_digit_exp.p, c->stream);
+              }),
+              "slice V");
+    if (g != GI_OK) return g;
+    fb.digits_s = S->s;
+    fb.digits_w = S->w;
+  }
   g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "H slices");
   if (g != GI_OK) return g;
   g = check(c, S->b_exp.reserve(ncol), "H exponents");
   if (g != GI_OK) return g;
   g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-              cudaError_t e = slice(V, ldv, nvec, K, vpad, S->s, S->w, S->v_slices.p, S->v_exp.p,
-                                    c->stream);
-              if (e != cudaSuccess) return e;
               return slice(H, ldh, ncol, K, ncol, S->s, S->w, S->b_slices.p, S->b_exp.p,
                            c->stream);
             }),
-            "slice V/H");
+            "slice H");
   if (g != GI_OK) return g;
   c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * nvec * (double)ncol * K;
   gi_status r = GI_OK;
   timed(c, GI_PHASE_FINAL_GEMM, [&] {
-    r = gemm(c, S->v_slices.p, vpad, S->v_exp.p, vpad, S->b_slices.p, ncol, S->b_exp.p, T, ldt,
-             0, nvec, ncol, K, 1);
+    r = gemm(c, fb.d_digits.p, vpad, fb.d_digit_exp.p, vpad, S->b_slices.p, ncol, S->b_exp.p, T,
+             ldt, 0, nvec, ncol, K, 1);
     return cudaSuccess;
   });
   return r;

@@ -6,9 +6,10 @@ namespace gi {
 // Z[c][n*ldz + f] = sum_v mu_c(v, f) * Y[n*ldy + v] for c = 0..2, n < ncol.
 gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zstride,
                             int ncol);
-// T[n*ldt + f] = sum_s V[f*ldv + s] * H[n*ldh + s], f < nvec, n < ncol.
-gi_status split_gemm_final(Ctx* c, const double* V, int ldv, int nvec, const double* H, int ldh,
-                           int ncol, double* T, int ldt);
+// T[n*ldt + f] = sum_s V_F[f][s] * H[n*ldh + s] for the vectors of block fb
+// (f < nvec, n < ncol); the block's digit planes are cut on first use.
+gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol, double* T,
+                           int ldt);
 // Called once per run before the launch loop (sizes workspaces, slices the dipole).
 gi_status split_prepare(Ctx* c);
 void split_invalidate(Ctx* c);  // the dipole changed: drop its cached slices
