@@ -27,6 +27,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "split.h"
@@ -35,8 +36,8 @@ namespace gi {
 namespace {
 
 constexpr int kBM = 128;       // tile rows (MMA M)
-constexpr int kBK = 32;        // K elements per stage (64 bytes: SWIZZLE_64B rows)
-constexpr int kStages = 2;
+constexpr int kBK = 16;        // K elements per stage (32 bytes: SWIZZLE_32B rows)
+constexpr int kStages = 4;
 constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int kMaxSlices = 10;
 constexpr int kDefaultSlices = 9;
@@ -46,6 +47,7 @@ struct SplitShape {
   int s, w, bn;
 };
 
+// One-pass tile width: S accumulators of BN columns fit the 512 TMEM columns.
 __host__ __device__ constexpr int bn_for(int s) { return s <= 8 ? 64 : 48; }
 // At least 120 KB so that one CTA holds an SM (it allocates all 512 TMEM columns).
 size_t smem_bytes(int s, int bn) {
@@ -83,11 +85,14 @@ __device__ __forceinline__ uint64_t gtimer() {
 // Bounded wait on an mbarrier phase.  Returns false when the CTA is aborting
 // (another warp timed out) or this wait exceeded its time limit (then it
 // raises the abort itself and records the error).
+// `sleep_ns` backs the poll off so that a waiting warp leaves the issue slots of
+// its SM sub-partition to the MMA-issuing warp.
 __device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err,
-                          int code) {
+                          int code, unsigned sleep_ns = 0) {
   uint64_t t0 = 0;
   for (uint32_t it = 1;; ++it) {
     if (mbar_try(b, parity)) return true;
+    if (sleep_ns) __nanosleep(sleep_ns);
     if ((it & 63) == 0) {
       if (*abort_flag) return false;
       const uint64_t t = gtimer();
@@ -109,15 +114,15 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       "l"(reinterpret_cast<uint64_t>(map)), "r"(sptr(bar)), "r"(c0), "r"(c1), "r"(c2)
       : "memory");
 }
-// Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 64
-// bytes (32 elements) with the 64-byte swizzle: 8-row groups 512 bytes apart.
-__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t addr) {
+// Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 32
+// bytes (16 elements) with the 32-byte swizzle: 8-row groups 256 bytes apart.
+__device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr) {
   uint64_t d = 0;
   d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
   d |= (uint64_t)1 << 16;                          // leading byte offset (unused here)
-  d |= (uint64_t)((512 >> 4) & 0x3FFF) << 32;      // stride byte offset: 8 rows x 64 B
+  d |= (uint64_t)((256 >> 4) & 0x3FFF) << 32;      // stride byte offset: 8 rows x 32 B
   d |= (uint64_t)1 << 46;                          // descriptor version (tcgen05)
-  d |= (uint64_t)4 << 61;                          // SWIZZLE_64B
+  d |= (uint64_t)6 << 61;                          // SWIZZLE_32B
   return d;
 }
 // Instruction descriptor: kind::f16, bf16 x bf16 -> f32, K-major A and B.
@@ -160,13 +165,15 @@ template <int S, int BN>
 __global__ void __launch_bounds__(kThreads, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
-                 int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int* err) {
+                 int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM,
+                 int nA, int nN, int GA, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   constexpr uint32_t kAbytes = S * kBM * kBK * 2;
   constexpr uint32_t kBbytes = S * BN * kBK * 2;
   constexpr uint32_t kStage = kAbytes + kBbytes;
+  static_assert(S * BN <= 512, "tensor memory columns");
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + kStages * kStage);
   uint64_t* empty = full + kStages;
   uint64_t* accf = empty + kStages;
@@ -174,7 +181,14 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n0 = blockIdx.x * BN, m0 = blockIdx.y * kBM, z = blockIdx.z;
+  // Raster: tiles come in groups of GA row tiles (A, across m and z) that stay
+  // in L2 while every column tile (B) streams past them once per group.
+  const int t = blockIdx.x;  // one tile per CTA, nA * nN tiles (nA = nM * batch)
+  const int grp = t / (GA * nN);
+  const int r = t - grp * GA * nN;
+  const int gsz = min(GA, nA - grp * GA);
+  const int ai = grp * GA + r % gsz;
+  const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
   const int nk = K / kBK;
 
   if (threadIdx.x == 0) {
@@ -201,7 +215,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       int issued = 0;
       for (int kb = 0; kb < nk; ++kb) {
         const int st = kb % kStages;
-        if (kb >= kStages && !mbar_wait(&empty[st], ((kb / kStages) - 1) & 1, abort_flag, err, 1))
+        if (kb >= kStages &&
+            !mbar_wait(&empty[st], ((kb / kStages) - 1) & 1, abort_flag, err, 1, 64))
           break;
         unsigned char* sa = smem + st * kStage;
         mbar_expect_tx(&full[st], kStage);
@@ -227,17 +242,15 @@ __global__ void __launch_bounds__(kThreads, 1)
         asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
         const uint32_t a0 = sptr(smem + st * kStage);
         const uint32_t b0 = a0 + kAbytes;
-#pragma unroll
-        for (int ks = 0; ks < kBK / 16; ++ks) {
+        {
 #pragma unroll
           for (int d = 0; d < S; ++d) {
 #pragma unroll
             for (int p = 0; p <= d; ++p) {
               const int q = d - p;
-              const uint64_t ad = sdesc_sw64(a0 + p * (kBM * kBK * 2) + ks * 32);
-              const uint64_t bd = sdesc_sw64(b0 + q * (BN * kBK * 2) + ks * 32);
-              const uint32_t acc = (kb > 0 || ks > 0 || p > 0) ? 1u : 0u;
-              mma_bf16(tmem + d * BN, ad, bd, idesc, acc);
+              const uint64_t ad = sdesc_sw32(a0 + p * (kBM * kBK * 2));
+              const uint64_t bd = sdesc_sw32(b0 + q * (BN * kBK * 2));
+              mma_bf16(tmem + d * BN, ad, bd, idesc, (kb > 0 || p > 0) ? 1u : 0u);
             }
           }
         }
@@ -255,7 +268,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     // epilogue warps 2..5: TMEM lane quarter = warp % 4
     const int q4 = warp & 3;
     const int m = m0 + q4 * 32 + lane;
-    const bool ok = mbar_wait(accf, 0, abort_flag, err, 3);
+    const bool ok = mbar_wait(accf, 0, abort_flag, err, 3, 1000);
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     if (ok) {
       // The accumulators hold integers (|acc| < 2^31), so the diagonals are
@@ -294,6 +307,183 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
         }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
+// Two-pass variant.  A 128 x N x 16 bf16 MMA costs max(44, 32 + N/4) cycles on
+// this GPU, so it reaches the full tensor rate only from N = 128; one pass with
+// all S accumulators in tensor memory limits N to 512/S.  Here pass 0 sweeps K
+// for the diagonals [0, D1) and pass 1 sweeps it again for [D1, S), each with
+// BN-wide accumulators.  Pass 0's epilogue turns its diagonals (exactly, in
+// int64) into FP64 in C; pass 1's epilogue adds its part.  Pass 0 loads only
+// the digit planes it uses (p, q < D1).
+constexpr int kStages2 = 3;
+
+template <int S, int BN, int D1>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_split_gemm2(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
+                  int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
+                  int nN, int GA, int* err) {
+  static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t kAplane = kBM * kBK * 2, kBplane = BN * kBK * 2;
+  constexpr uint32_t kStage = S * (kAplane + kBplane);
+  constexpr int ST = kStages2;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
+  uint64_t* empty = full + ST;
+  uint64_t* accf = empty + ST;  // [2]: a pass's accumulators are final
+  uint64_t* tfree = accf + 2;   // pass 0's accumulators have been read
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tfree + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x;
+  const int grp = t / (GA * nN);
+  const int r = t - grp * GA * nN;
+  const int gsz = min(GA, nA - grp * GA);
+  const int ai = grp * GA + r % gsz;
+  const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
+  const int nk = K / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ST; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&accf[0], 1);
+    mbar_init(&accf[1], 1);
+    mbar_init(tfree, 128);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     sptr(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer: both passes, one continuous stage ring
+      int issued = 0;
+      for (int it = 0; it < 2 * nk; ++it) {
+        const int pass = it >= nk, kb = it - pass * nk, st = it % ST;
+        const int np = pass ? S : D1;
+        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 1, 64))
+          break;
+        unsigned char* sa = smem + st * kStage;
+        mbar_expect_tx(&full[st], np * (kAplane + kBplane));
+        for (int p = 0; p < np; ++p) {
+          tma_load_3d(sa + p * kAplane, &tmA, &full[st], kb * kBK, z * Mpad + m0, p);
+          tma_load_3d(sa + S * kAplane + p * kBplane, &tmB, &full[st], kb * kBK, n0, p);
+        }
+        issued = it + 1;
+      }
+      if (*abort_flag) {
+        for (int it = (issued > ST ? issued - ST : 0); it < issued; ++it) {
+          uint64_t t0 = gtimer();
+          while (!mbar_try(&full[it % ST], (it / ST) & 1) && gtimer() - t0 < 1000000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = idesc_bf16(kBM, BN);
+      bool ok = true;
+      int last = 0;  // the last pass whose MMAs were committed
+      for (int pass = 0; pass < 2 && ok; ++pass) {
+        last = pass;
+        if (pass == 1) {
+          ok = mbar_wait(tfree, 0, abort_flag, err, 4);
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          if (!ok) break;
+        }
+        for (int kb = 0; kb < nk; ++kb) {
+          const int it = pass * nk + kb, st = it % ST;
+          if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 2)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t a0 = sptr(smem + st * kStage);
+          const uint32_t b0 = a0 + S * kAplane;
+          if (pass == 0) {
+#pragma unroll
+            for (int d = 0; d < D1; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + d * BN, sdesc_sw32(a0 + p * kAplane),
+                         sdesc_sw32(b0 + (d - p) * kBplane), idesc, (kb > 0 || p > 0) ? 1u : 0u);
+          } else {
+#pragma unroll
+            for (int d = D1; d < S; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + (d - D1) * BN, sdesc_sw32(a0 + p * kAplane),
+                         sdesc_sw32(b0 + (d - p) * kBplane), idesc, (kb > 0 || p > 0) ? 1u : 0u);
+          }
+          mma_commit(&empty[st]);
+        }
+        mma_commit(&accf[pass]);
+      }
+      if (*abort_flag) {
+        // the MMAs already issued must finish before TMEM is released
+        uint64_t t0 = gtimer();
+        while (!mbar_try(&accf[last], 0) && gtimer() - t0 < 1000000000ull) {
+        }
+      }
+    }
+  } else {
+    const int q4 = warp & 3;
+    const int m = m0 + q4 * 32 + lane;
+    const int emr = (m < M) ? ea[z * Mpad + m] : 0;
+    double* Cz = C + (size_t)z * strideC;
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool ok = mbar_wait(&accf[pass], 0, abort_flag, err, 3, 1000);
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (!ok) break;
+      const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        long long v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0;
+        for (int d = d0; d < d1; ++d) {
+          float f[16];
+          tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (d - d0) * BN + c0, f);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = (v[j] << w) + (long long)__float2int_rn(f[j]);
+        }
+        if (m < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < Nc) {
+              const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
+              double* dst = Cz + (size_t)n * ldc + m;
+              const double part = ldexp((double)v[j], E);
+              *dst = pass ? *dst + part : part;
+            }
+          }
+        }
+      }
+      if (pass == 0) {
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
       }
     }
   }
@@ -403,41 +593,80 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-// 3-D map over digit planes [s][rows][K] of bf16 with a (32, box_rows, s) box.
-bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int box_rows) {
+// 3-D map over digit planes [s][rows][K] of bf16 with a (16, box_rows, box_planes) box.
+bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int box_rows,
+              int box_planes) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)s};
   cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)K * rows * 2};
-  cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, (cuuint32_t)s};
+  cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, (cuuint32_t)box_planes};
   cuuint32_t es[3] = {1, 1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
-            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_32B,
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
+
+// GI_SPLIT_KERNEL=1 selects the one-pass kernel (for comparison runs).
+bool one_pass() {
+  static int v = -1;
+  if (v < 0) {
+    const char* e = getenv("GI_SPLIT_KERNEL");
+    v = (e && e[0] == '1') ? 1 : 0;
+  }
+  return v == 1;
+}
+
+// Two-pass geometry: diagonals [0, S/2) then [S/2, S), each pass's accumulators
+// within the 512 tensor-memory columns, at most 128 wide.
+__host__ __device__ constexpr int d1_of(int s) { return s / 2; }
+__host__ __device__ constexpr int bn2_of(int s) {
+  return ((512 / (s - s / 2)) / 16 * 16) > 128 ? 128 : ((512 / (s - s / 2)) / 16 * 16);
+}
+size_t smem2_bytes(int s, int bn) {
+  const size_t need = (size_t)kStages2 * s * (kBM + bn) * kBK * 2 + 1024 + 256;
+  return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;  // one CTA per SM
+}
+
+int tile_n(int s) { return one_pass() ? bn_for(s) : bn2_of(s); }
 
 SplitShape shape_of(const Ctx* c) {
   int s = c->params.split_slices > 0 ? c->params.split_slices : kDefaultSlices;
   s = std::min(std::max(s, 2), kMaxSlices);
-  return SplitShape{s, kDefaultW, bn_for(s)};
+  return SplitShape{s, kDefaultW, tile_n(s)};
 }
 
 template <int S>
 cudaError_t launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const int32_t* ea,
                         const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
                         int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
-  constexpr int BN = bn_for(S);
-  const size_t sm = smem_bytes(S, BN);
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(k_split_gemm<S, BN>,
+  const bool one = one_pass();
+  constexpr int BN1 = bn_for(S), BN2 = bn2_of(S), D1 = d1_of(S);
+  const int BN = one ? BN1 : BN2;
+  const size_t sm = one ? smem_bytes(S, BN1) : smem2_bytes(S, BN2);
+  static bool attr1 = false, attr2 = false;
+  if (one && !attr1) {
+    cudaError_t e = cudaFuncSetAttribute(k_split_gemm<S, BN1>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr1 = true;
   }
-  dim3 grid((Nc + BN - 1) / BN, (M + kBM - 1) / kBM, batch);
-  k_split_gemm<S, BN><<<grid, kThreads, sm, st>>>(tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc,
-                                                  K, w, err);
+  if (!one && !attr2) {
+    cudaError_t e = cudaFuncSetAttribute(k_split_gemm2<S, BN2, D1>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+    if (e != cudaSuccess) return e;
+    attr2 = true;
+  }
+  const int nM = (M + kBM - 1) / kBM, nN = (Nc + BN - 1) / BN, nA = nM * batch;
+  // row tiles per L2 group: their digit planes (128 x K x S bf16 each) within ~64 MB
+  const size_t a_tile = (size_t)kBM * K * S * 2;
+  const int GA = std::max(1, std::min(nA, (int)(((size_t)64 << 20) / a_tile)));
+  if (one)
+    k_split_gemm<S, BN1><<<nA * nN, kThreads, sm, st>>>(
+        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
+  else
+    k_split_gemm2<S, BN2, D1><<<nA * nN, kThreads, sm, st>>>(
+        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
   return cudaGetLastError();
 }
 
@@ -552,9 +781,10 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
                       double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch) {
   SplitState* S = state(c);
   CUtensorMap tA, tB;
-  const int bn = bn_for(S->s);
-  if (!make_map(&tA, Aslices, K, Arows_total, S->s, kBM) ||
-      !make_map(&tB, Bslices, K, Brows, S->s, bn)) {
+  const int bn = tile_n(S->s);
+  const int planes = one_pass() ? S->s : 1;  // the two-pass kernel loads plane by plane
+  if (!make_map(&tA, Aslices, K, Arows_total, S->s, kBM, planes) ||
+      !make_map(&tB, Bslices, K, Brows, S->s, bn, planes)) {
     c->err = "split precision: cuTensorMapEncodeTiled failed";
     return GI_ERR_CUDA;
   }
