@@ -485,20 +485,31 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   // line buffer: the whole job on the device
   GI_CUDA(c, c->d_lines.reserve(std::max<size_t>(cap_total, 1)));
 
-  // workspace: per initial block, chunked to the budget; every per-chunk
-  // table is planned here and uploaded once, so the launch loop never waits
+  // Work is organised in rounds that fit the workspace budget.  A round is a
+  // set of units (a range of initial vectors of one block); all its Y columns
+  // go through ONE half-line-strength GEMM, and for every final block all the
+  // units that target it go through ONE final-state GEMM.  Every per-unit table
+  // is planned and uploaded here, so the launch sequence never waits.
   const int N = c->N, Kp = c->Kp;
-  const size_t ws_limit = c->budget ? c->budget / 2 : ((size_t)24 << 30);
-  struct Chunk {
+  const size_t ws_limit = c->budget ? c->budget / 2 : ((size_t)64 << 30);
+  const int s_digits = (P.precision == GI_PREC_SPLIT) ? split_digits(c) : 0;
+  struct Unit {
     BlockPlan* I;
     std::vector<PairPlan*> pairs;
-    int nI;
-    size_t off;  // into the ivec/level and energy tables
+    int nI, ncolY;
+    size_t off;   // into the record/level and energy tables
+    size_t ycol;  // first Y/Z column of the unit within its round
   };
-  std::vector<Chunk> chunks;
-  std::vector<int32_t> h_ivec;  // per chunk: nI record ids then nI level ids
+  struct Round {
+    std::vector<Unit> units;
+    size_t ncolY = 0;
+  };
+  std::vector<Round> rounds(1);
+  std::vector<int32_t> h_ivec;  // per unit: nI record ids then nI level ids
   std::vector<double> h_EI;
-  size_t max_y = 1, max_z = 1, max_h = 1, max_t = 1;
+  // bytes per Y column: Y, 3 Z, digit planes; plus the widest H/T per column
+  const size_t per_col = (size_t)Kp * (8 * 4 + 2 * (size_t)s_digits);
+  size_t round_bytes = 0;
   for (auto& kv : plans) {
     BlockPlan& I = kv.second;
     std::vector<PairPlan*> mine;
@@ -507,34 +518,65 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     if (mine.empty()) continue;
     const int ndegI = c->degen[I.blk->gamma];
     const int nslot = c->bases[I.blk->J]->nslot;
-    size_t per_vec = (size_t)ndegI * nslot * Kp * 8 * 4;
+    size_t per_vec = (size_t)ndegI * nslot * per_col;
     for (auto* pp : mine) {
-      const int ndegF = c->degen[pp->F->blk->gamma];
-      per_vec += (size_t)ndegI * ndegF * (pp->F->blk->ld + round_up(pp->F->blk->nvec, 2)) * 8;
+      const Block& fb = *pp->F->blk;
+      per_vec += (size_t)ndegI * c->degen[fb.gamma] *
+                 (fb.ld * (8 + 2 * (size_t)s_digits) + round_up(fb.nvec, 2) * 8);
     }
-    int chunk = (int)std::min<size_t>(std::max<size_t>(1, ws_limit / per_vec), I.ivec.size());
+    const int chunk =
+        (int)std::min<size_t>(std::max<size_t>(1, ws_limit / per_vec), I.ivec.size());
     for (int i0 = 0; i0 < (int)I.ivec.size(); i0 += chunk) {
-      Chunk ch{&I, mine, std::min(chunk, (int)I.ivec.size() - i0), h_EI.size()};
-      for (int i = 0; i < ch.nI; i++) h_EI.push_back(I.blk->energies[I.ivec[i0 + i]]);
-      for (int i = 0; i < ch.nI; i++) h_ivec.push_back(I.ivec[i0 + i]);
-      for (int i = 0; i < ch.nI; i++) h_ivec.push_back(I.level_of_rec[I.ivec[i0 + i]]);
-      const size_t ncolY = (size_t)ch.nI * ndegI * nslot;
-      max_y = std::max(max_y, ncolY * Kp);
-      max_z = std::max(max_z, 3 * ncolY * Kp);
-      for (auto* pp : mine) {
-        const size_t ncolH = (size_t)ch.nI * ndegI * c->degen[pp->F->blk->gamma];
-        max_h = std::max(max_h, ncolH * pp->F->blk->ld);
-        max_t = std::max(max_t, ncolH * round_up(pp->F->blk->nvec, 2));
+      const int nI = std::min(chunk, (int)I.ivec.size() - i0);
+      if (round_bytes + per_vec * nI > ws_limit && !rounds.back().units.empty()) {
+        rounds.emplace_back();
+        round_bytes = 0;
       }
-      chunks.push_back(std::move(ch));
+      Round& R = rounds.back();
+      Unit u{&I, mine, nI, nI * ndegI * nslot, h_EI.size(), R.ncolY};
+      for (int i = 0; i < nI; i++) h_EI.push_back(I.blk->energies[I.ivec[i0 + i]]);
+      for (int i = 0; i < nI; i++) h_ivec.push_back(I.ivec[i0 + i]);
+      for (int i = 0; i < nI; i++) h_ivec.push_back(I.level_of_rec[I.ivec[i0 + i]]);
+      R.ncolY += u.ncolY;
+      round_bytes += per_vec * nI;
+      R.units.push_back(std::move(u));
     }
   }
-  // ivec/level tables are laid out [chunk: nI recs, nI levels]; energies [chunk: nI]
+  // final blocks of a round and the H/T column ranges of their units
+  struct Target {
+    BlockPlan* F;
+    std::vector<std::pair<const Unit*, PairPlan*>> parts;
+    std::vector<size_t> hcol;
+    size_t ncolH = 0;
+  };
+  std::vector<std::vector<Target>> targets(rounds.size());
+  size_t max_y = 1, max_h = 1, max_t = 1;
+  for (size_t r = 0; r < rounds.size(); r++) {
+    max_y = std::max(max_y, rounds[r].ncolY * Kp);
+    std::map<BlockPlan*, size_t> idx;
+    for (const Unit& u : rounds[r].units)
+      for (PairPlan* pp : u.pairs) {
+        auto it = idx.find(pp->F);
+        if (it == idx.end()) {
+          idx[pp->F] = targets[r].size();
+          targets[r].push_back(Target{pp->F, {}, {}, 0});
+          it = idx.find(pp->F);
+        }
+        Target& T = targets[r][it->second];
+        T.hcol.push_back(T.ncolH);
+        T.parts.push_back({&u, pp});
+        T.ncolH += (size_t)u.nI * c->degen[u.I->blk->gamma] * c->degen[pp->F->blk->gamma];
+      }
+    for (const Target& T : targets[r]) {
+      max_h = std::max(max_h, T.ncolH * T.F->blk->ld);
+      max_t = std::max(max_t, T.ncolH * round_up(T.F->blk->nvec, 2));
+    }
+  }
   GI_CUDA(c, c->w_ivec.upload(h_ivec));
   DevArray<double> d_EI;
   GI_CUDA(c, d_EI.upload(h_EI));
   GI_CUDA(c, c->w_y.reserve(max_y));
-  GI_CUDA(c, c->w_z.reserve(max_z));
+  GI_CUDA(c, c->w_z.reserve(3 * max_y));
   GI_CUDA(c, c->w_h.reserve(max_h));
   GI_CUDA(c, c->w_t.reserve(max_t));
   if (P.precision == GI_PREC_SPLIT) {
@@ -550,82 +592,92 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   int64_t npairs_checked = 0;
 
   GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
-  for (const Chunk& ch : chunks) {
-    BlockPlan& I = *ch.I;
-    const Basis& bI = *c->bases[I.blk->J];
-    const int ndegI = c->degen[I.blk->gamma];
-    const int nslot = bI.nslot;
-    const int nI = ch.nI;
-    const int32_t* d_ivec = c->w_ivec.p + 2 * ch.off;
-    const int32_t* d_lvI = d_ivec + nI;
-    const double* d_ei = d_EI.p + ch.off;
-    const int ncolY = nI * ndegI * nslot;
-    GI_CUDA(c, timed(c, GI_PHASE_CORRELATE, [&] {
-              return launch_build_y(I.blk->d_vecs.p, I.blk->ld, d_ivec, nI, ndegI, bI,
-                                    I.blk->gamma, ndegI, N, Kp, c->w_y.p, c->stream);
-            }));
-    by_corr += 8.0 * ((double)nI * I.blk->nsize + (double)ncolY * Kp);
-    const size_t zc = (size_t)ncolY * Kp;
+  for (size_t r = 0; r < rounds.size(); r++) {
+    const Round& R = rounds[r];
+    if (R.units.empty()) continue;
+    const size_t zc = R.ncolY * Kp;  // stride between dipole components in Z
+    for (const Unit& u : R.units) {
+      const Basis& bI = *c->bases[u.I->blk->J];
+      const int ndegI = c->degen[u.I->blk->gamma];
+      GI_CUDA(c, timed(c, GI_PHASE_CORRELATE, [&] {
+                return launch_build_y(u.I->blk->d_vecs.p, u.I->blk->ld, c->w_ivec.p + 2 * u.off,
+                                      u.nI, ndegI, bI, u.I->blk->gamma, ndegI, N, Kp,
+                                      c->w_y.p + u.ycol * Kp, c->stream);
+              }));
+      by_corr += 8.0 * ((double)u.nI * u.I->blk->nsize + (double)u.ncolY * Kp);
+    }
     if (P.precision == GI_PREC_SPLIT) {
-      gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, ncolY);
+      gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY);
       if (s != GI_OK) return s;
     } else {
       GI_CUDA(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
                 return gemm_fp64_nt(c->d_mu.p, Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp,
-                                    zc, N, ncolY, Kp, 3, c->stream);
+                                    zc, N, (int)R.ncolY, Kp, 3, c->stream);
               }));
     }
-    fl_half += 2.0 * 3.0 * N * (double)N * ncolY;
+    fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
 
-    for (auto* pp : ch.pairs) {
-      BlockPlan& Fp = *pp->F;
+    for (const Target& T : targets[r]) {
+      BlockPlan& Fp = *T.F;
       const Block& fb = *Fp.blk;
       const Basis& bF = *c->bases[fb.J];
       const int ndegF = c->degen[fb.gamma];
       const int ldh = fb.ld;
-      const int ncolH = nI * ndegI * ndegF;
       const int ldt = round_up(fb.nvec, 2);
-      GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
-                return launch_build_h(c->w_z.p, zc, Kp, nslot, ndegI, nI, bF, fb.gamma, ndegF,
-                                      fb.nsize, ldh, c->w_stencil.p + pp->st_off * 6,
-                                      c->w_stencil_n.p + pp->st_off, 6, c->w_h.p, c->stream);
-              }));
+      for (size_t k = 0; k < T.parts.size(); k++) {
+        const Unit& u = *T.parts[k].first;
+        const PairPlan* pp = T.parts[k].second;
+        const int ndegI = c->degen[u.I->blk->gamma];
+        const int nslot = c->bases[u.I->blk->J]->nslot;
+        GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
+                  return launch_build_h(c->w_z.p + u.ycol * Kp, zc, Kp, nslot, ndegI, u.nI, bF,
+                                        fb.gamma, ndegF, fb.nsize, ldh,
+                                        c->w_stencil.p + pp->st_off * 6,
+                                        c->w_stencil_n.p + pp->st_off, 6,
+                                        c->w_h.p + T.hcol[k] * ldh, c->stream);
+                }));
+      }
       if (P.precision == GI_PREC_SPLIT) {
-        gi_status s = split_gemm_final(c, *Fp.blk, c->w_h.p, ldh, ncolH, c->w_t.p, ldt);
+        gi_status s = split_gemm_final(c, *Fp.blk, c->w_h.p, ldh, (int)T.ncolH, c->w_t.p, ldt);
         if (s != GI_OK) return s;
       } else {
         GI_CUDA(c, timed(c, GI_PHASE_FINAL_GEMM, [&] {
                   return gemm_fp64_nt(fb.d_vecs.p, fb.ld, 0, c->w_h.p, ldh, c->w_t.p, ldt, 0,
-                                      fb.nvec, ncolH, ldh, 1, c->stream);
+                                      fb.nvec, (int)T.ncolH, ldh, 1, c->stream);
                 }));
       }
-      fl_final += 2.0 * fb.nsize * (double)fb.nvec * ncolH;
-      EpiParams ep{};
-      ep.jI = I.blk->J;
-      ep.jF = fb.J;
-      ep.ndegI = ndegI;
-      ep.ndegF = ndegF;
-      ep.reduced = P.reduced;
-      ep.combo_mask = pp->combo_mask;
-      ep.gns = P.gns[I.blk->gamma];
-      ep.zpe = zpe;
-      ep.beta = beta;
-      ep.q_stat = P.q_stat;
-      ep.fw0 = P.freq_window[0];
-      ep.fw1 = P.freq_window[1];
-      ep.thresh_S = P.thresh_linestrength;
-      ep.thresh_I = P.thresh_intensity;
-      ep.A_coef = ph.A_coef;
-      ep.intens_cm_mol = ph.intens_cm_mol;
-      ep.avogno = ph.avogno;
+      fl_final += 2.0 * fb.nsize * (double)fb.nvec * T.ncolH;
       const auto off = farr[&Fp];
-      GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
-                return launch_epilogue(c->w_t.p, ldt, nI, fb.nvec, d_lvI, d_ei,
-                                       c->w_int.p + off.first, fb.d_energies.p,
-                                       c->w_upper.p + off.second, ep, c->d_lines.p,
-                                       c->w_counter.p, (long long)c->d_lines.n, c->stream);
-              }));
-      npairs_checked += (int64_t)nI * Fp.nupper;
+      for (size_t k = 0; k < T.parts.size(); k++) {
+        const Unit& u = *T.parts[k].first;
+        const PairPlan* pp = T.parts[k].second;
+        EpiParams ep{};
+        ep.jI = u.I->blk->J;
+        ep.jF = fb.J;
+        ep.ndegI = c->degen[u.I->blk->gamma];
+        ep.ndegF = ndegF;
+        ep.reduced = P.reduced;
+        ep.combo_mask = pp->combo_mask;
+        ep.gns = P.gns[u.I->blk->gamma];
+        ep.zpe = zpe;
+        ep.beta = beta;
+        ep.q_stat = P.q_stat;
+        ep.fw0 = P.freq_window[0];
+        ep.fw1 = P.freq_window[1];
+        ep.thresh_S = P.thresh_linestrength;
+        ep.thresh_I = P.thresh_intensity;
+        ep.A_coef = ph.A_coef;
+        ep.intens_cm_mol = ph.intens_cm_mol;
+        ep.avogno = ph.avogno;
+        const int32_t* d_lvI = c->w_ivec.p + 2 * u.off + u.nI;
+        GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+                  return launch_epilogue(c->w_t.p + T.hcol[k] * ldt, ldt, u.nI, fb.nvec, d_lvI,
+                                         d_EI.p + u.off, c->w_int.p + off.first, fb.d_energies.p,
+                                         c->w_upper.p + off.second, ep, c->d_lines.p,
+                                         c->w_counter.p, (long long)c->d_lines.n, c->stream);
+                }));
+        npairs_checked += (int64_t)u.nI * Fp.nupper;
+      }
     }
   }
   GI_CUDA(c, cudaEventRecord(c->ev1, c->stream));

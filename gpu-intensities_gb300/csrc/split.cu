@@ -861,6 +861,8 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
   return r;
 }
 
+int split_digits(const Ctx* c) { return shape_of(c).s; }
+
 gi_status split_check(Ctx* c) {
   if (!c->split || !c->split->err.p) return GI_OK;
   int e = 0;

@@ -12,6 +12,8 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
                            int ldt);
 // Called once per run before the launch loop (sizes workspaces, slices the dipole).
 gi_status split_prepare(Ctx* c);
+// Digit planes per operand the next split-precision run will use.
+int split_digits(const Ctx* c);
 void split_invalidate(Ctx* c);  // the dipole changed: drop its cached slices
 // After a run: reads the device error word the split kernels set on a timeout.
 gi_status split_check(Ctx* c);
