@@ -52,12 +52,13 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="c2v_plain")
     ap.add_argument("--jmax", type=int, default=None, help="restrict J to 0..jmax")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="split", choices=["fp64", "split"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--slices", type=int, default=0, help="bf16 digits per operand (split)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-path comparison")
     return ap.parse_args()
 
 
@@ -185,6 +186,40 @@ def cpu_baseline(prob, nlow=8):
                       f"initial levels ({n} lines in {dt:.1f} s)"}
 
 
+# ---------------------------------------------------------------- accuracy
+def split_accuracy(pkg, prob, slices, device):
+    """Split path against the FP64 GPU path (itself parity-tested against the
+    CPU oracle) on the J <= 3 part of the workload: identical line selection
+    and the per-line relative error of S."""
+    from gpu_intensities_gb300 import synth
+    sub = synth.Problem(prob.sym_type, prob.N, prob.mu,
+                        {J: b for J, b in prob.bases.items() if J <= 3},
+                        {k: b for k, b in prob.blocks.items() if k[0] <= 3}, prob.params,
+                        name=prob.name + "_J0-3")
+    out = {}
+    for name, prec in (("fp64", pkg.GI_PREC_FP64), ("split", pkg.GI_PREC_SPLIT)):
+        with pkg.Engine(device) as e:
+            e.load(sub, precision=prec, split_slices=slices)
+            e.run()
+            out[name] = pkg.keyed(e.lines(), e.levels())
+    a, b = out["fp64"], out["split"]
+    keys = ("jI", "gammaI", "recI", "jF", "gammaF", "recF")
+    a = a[np.lexsort(tuple(a[k] for k in reversed(keys)))]
+    b = b[np.lexsort(tuple(b[k] for k in reversed(keys)))]
+    same = len(a) == len(b) and all(np.array_equal(a[k], b[k]) for k in keys)
+    res = {"sample": "J<=3 part of the workload, split vs FP64 GPU path",
+           "lines": int(len(a)), "identical_selection": bool(same)}
+    if same and len(a):
+        rel = np.abs(b["S"] - a["S"]) / np.where(a["S"] > 0, a["S"], 1.0)
+        tmax = np.abs(a["t"]).max()
+        well = np.abs(a["t"]).max(axis=1) >= 1e-4 * tmax
+        res.update({"rel_err_S_max": float(rel.max()), "rel_err_S_p99": float(np.quantile(rel, 0.99)),
+                    "rel_err_S_max_well_conditioned": float(rel[well].max()),
+                    "well_conditioned_fraction": float(well.mean()),
+                    "note": "well conditioned: |t| >= 1e-4 max|t| (no cancellation beyond 1e4)"})
+    return res
+
+
 # ---------------------------------------------------------------- reference arm
 def main_reference(args):
     rank, world, _ = dist_env()
@@ -234,21 +269,38 @@ def main_ours(args):
 
     eng = pkg.Engine(local)
     eng.load(prob, precision=prec, split_slices=args.slices)
+    # the engine's launches go to this stream, so its CUDA events bracket them
+    stream = torch.cuda.Stream(device=local)
+    eng.set_stream(stream.cuda_stream)
+
+    def timed_steps(k, fn):
+        """Device seconds per step of k calls of fn, CUDA events on the stream."""
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        barrier()
+        a.record(stream)
+        out = None
+        for _ in range(k):
+            out = fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        return a.elapsed_time(b) * 1e-3 / k, out
+
     for _ in range(args.warmup):
         eng.run(lines_on_device=True)
-    torch.cuda.synchronize()
-    barrier()
     stats = []
+
+    def one():
+        eng.run(lines_on_device=True)
+        stats.append(eng.stats())
+
     with ClockSampler(local) as clk:
-        torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for _ in range(args.steps):
-            eng.run(lines_on_device=True)
-            stats.append(eng.stats())
-        torch.cuda.synchronize()
+        dt, _ = timed_steps(args.steps, one)
         t1 = time.perf_counter()
-    barrier()
-    dt = (t1 - t0) / args.steps
+    wall = (t1 - t0) / args.steps
     lines_pre = stats[-1]["nlines_filtered"]
     lines_post = stats[-1]["nlines"]
     launches = int(sum(s["kernel_launches"] for s in stats))
@@ -304,18 +356,25 @@ def main_ours(args):
             return eng.run(lines_on_device=False)
 
         step()
-        torch.cuda.synchronize()
-        barrier()
-        te0 = time.perf_counter()
-        for _ in range(ne):
-            n = step()
-        torch.cuda.synchronize()
-        te1 = time.perf_counter()
-        barrier()
+        te, n = timed_steps(ne, step)
         st = eng.stats()
-        e2e = {"value": world * st["nlines_filtered"] / ((te1 - te0) / ne), "unit": METRIC,
+        e2e = {"value": world * st["nlines_filtered"] / te, "unit": METRIC,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(n * 80 + 16),
-               "ms_per_step": 1e3 * (te1 - te0) / ne}
+               "ms_per_step": 1e3 * te, "steps": ne}
+
+    # the plain FP64 GPU path on the same job, and per-line accuracy of the
+    # split path against it on the J <= 3 part of the workload
+    fp64 = accuracy = None
+    if args.precision == "split" and not args.no_fp64:
+        eng.set_params(prob.params, precision=pkg.GI_PREC_FP64)
+        eng.run(lines_on_device=True)
+        tf, _ = timed_steps(1, lambda: eng.run(lines_on_device=True))
+        fs = eng.stats()
+        fp64 = {"value": world * fs["nlines_filtered"] / tf, "unit": METRIC,
+                "ms_per_step": 1e3 * tf, "steps": 1, "warmup": 1,
+                "speedup_split_over_fp64": (lines_pre / dt) / (fs["nlines_filtered"] / tf)}
+        eng.set_params(prob.params, precision=prec, split_slices=args.slices)
+        accuracy = split_accuracy(pkg, prob, args.slices, local)
 
     if world > 1:
         t = torch.tensor([dt], device="cuda")
@@ -325,13 +384,14 @@ def main_ours(args):
     if rank == 0:
         out = {"metric": METRIC, "value": world * lines_pre / dt, "unit": METRIC,
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-               "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak",
+               "ms_per_step": 1e3 * dt, "wall_ms_per_step": 1e3 * wall,
+               "higher_is_better": True, "scaling": "weak",
                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
                "config": config_of(args, prob),
                "lines_per_step": lines_pre, "lines_above_threshold_per_step": lines_post,
                "value_above_threshold": world * lines_post / dt,
                "gpu_launches": launches, "roofline": roof, "e2e": e2e,
-               "clocks": clk.summary()}
+               "fp64_path": fp64, "accuracy": accuracy, "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(prob)
         print(json.dumps(out))

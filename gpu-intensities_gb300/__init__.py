@@ -101,6 +101,7 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.gi_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_size_t]
         L.gi_destroy.argtypes = [C.c_void_p]
+        L.gi_set_stream.argtypes = [C.c_void_p, C.c_void_p]
         L.gi_last_error.restype = C.c_char_p
         L.gi_last_error.argtypes = [C.c_void_p]
         L.gi_status_string.restype = C.c_char_p
@@ -120,6 +121,7 @@ def lib():
         L.gi_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_stats)]
         L.gi_half_ls.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p]
         L.gi_measure_fp64_peak.argtypes = [C.c_int, f64p]
+        L.gi_measure_mma_cycles.argtypes = [C.c_int, C.c_int, f64p]
         L.gi_half_ls_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_void_p, C.c_void_p, C.c_void_p]
         for name in header_functions():
@@ -135,6 +137,15 @@ def measure_fp64_peak(device: int = 0) -> float:
     st = lib().gi_measure_fp64_peak(device, C.byref(v))
     if st != GI_OK:
         raise GiError(st, "gi_measure_fp64_peak failed")
+    return v.value
+
+
+def measure_mma_cycles(device: int = 0, n: int = 128) -> float:
+    """Cycles of one bf16 tcgen05 MMA (M=128, K=16) of width n (gi_measure_mma_cycles)."""
+    v = C.c_double(0.0)
+    st = lib().gi_measure_mma_cycles(device, n, C.byref(v))
+    if st != GI_OK:
+        raise GiError(st, "gi_measure_mma_cycles failed")
     return v.value
 
 
@@ -203,6 +214,11 @@ class Engine:
             raise GiError(st, msg)
 
     # inputs --------------------------------------------------------------
+    def set_stream(self, stream: int | None):
+        """Order the engine's device work on a caller's cudaStream_t (an int
+        handle, e.g. torch.cuda.Stream().cuda_stream); None: its own stream."""
+        self._ck(self._L.gi_set_stream(self._h, C.c_void_p(stream or None)))
+
     def set_symmetry(self, sym_type: int):
         self._ck(self._L.gi_set_symmetry(self._h, sym_type))
 

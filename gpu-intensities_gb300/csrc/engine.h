@@ -40,10 +40,13 @@ struct DevArray {
     if (e == cudaSuccess) n = count; else p = nullptr;
     return e;
   }
+  // A pageable cudaMemcpy may return before its DMA lands; the legacy-stream
+  // sync orders the copy before work on any (also non-blocking) stream.
   cudaError_t upload(const T* h, size_t count) {
     cudaError_t e = alloc(count);
     if (e != cudaSuccess || count == 0) return e;
-    return cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
+    e = cudaMemcpy(p, h, count * sizeof(T), cudaMemcpyHostToDevice);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(cudaStreamLegacy);
   }
   cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
   // grow-only workspace
@@ -105,7 +108,8 @@ struct Ctx {
   int device = 0;
   size_t budget = 0;
   int nsm = 0;
-  cudaStream_t stream = nullptr;
+  cudaStream_t stream = nullptr;      // where all device work is ordered
+  cudaStream_t own_stream = nullptr;  // the context's own stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   std::string err;
 

@@ -758,11 +758,13 @@ gi_status gi_create(gi_ctx** out, int device, size_t hbm_budget_bytes) {
   c->device = device;
   c->budget = hbm_budget_bytes;
   cudaDeviceGetAttribute(&c->nsm, cudaDevAttrMultiProcessorCount, device);
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  if (cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) {
+    if (c->own_stream) cudaStreamDestroy(c->own_stream);
     delete c;
     return GI_ERR_CUDA;
   }
+  c->stream = c->own_stream;
   *out = reinterpret_cast<gi_ctx*>(c);
   return GI_OK;
 }
@@ -776,8 +778,17 @@ gi_status gi_destroy(gi_ctx* h) {
   if (c->h_lines) cudaFreeHost(c->h_lines);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
-  if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
+  return GI_OK;
+}
+
+gi_status gi_set_stream(gi_ctx* h, void* stream) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return GI_ERR_ARG;
+  cudaSetDevice(c->device);
+  GI_CUDA(c, cudaStreamSynchronize(c->stream));
+  c->stream = stream ? static_cast<cudaStream_t>(stream) : c->own_stream;
   return GI_OK;
 }
 

@@ -141,6 +141,13 @@ typedef struct {
 /* Context ---------------------------------------------------------------- */
 gi_status gi_create(gi_ctx** out, int device, size_t hbm_budget_bytes);
 gi_status gi_destroy(gi_ctx* ctx);
+/* Orders all later device work of the context (runs, half line strengths,
+ * uploads' consumers) on the caller's cudaStream_t `stream`; NULL returns to
+ * the context's own stream.  Waits for work already queued on the previous
+ * stream.  The stream must belong to the context's device and outlive its use.
+ * No counterpart in the reference, whose kernels run on its own streams
+ * (cuda_host.cu:980-992). */
+gi_status gi_set_stream(gi_ctx* ctx, void* stream);
 const char* gi_last_error(const gi_ctx* ctx);
 const char* gi_status_string(gi_status s);
 
