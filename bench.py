@@ -42,6 +42,10 @@ import __graft_entry__ as G  # noqa: E402
 
 METRIC = "linestrengths/s"
 THRESH_I = 1e-30  # cm/molecule
+# DRAM bytes (read + write) of one half-line-strength k_split_gemm2 launch per Y
+# column: ncu on the J <= 4 part of c2v_plain measured 71.35 GB + 9.13 GB for a
+# launch of 1000 x 96-column tiles.
+SPLIT_HALFLS_DRAM_BYTES_PER_COL = (71.346804e9 + 9.126300e9) / 96000
 
 
 def parse():
@@ -316,14 +320,25 @@ def main_ours(args):
     except OSError:
         pass
     if args.precision == "split":
+        # the dominant launch: the half-line-strength split GEMM (k_split_gemm2),
+        # one launch per step; digit-pair products x 2 x 3 x N x N x Y columns
         dom = "halfls_gemm"
-        flops = ps["flops_tensor"]
+        pairs = ps["flops_tensor"] / max(ps["flops_halfls"] + ps["flops_final"], 1.0)
+        flops = pairs * ps["flops_halfls"]
+        ncol = ps["flops_halfls"] / (6.0 * prob.N * prob.N)
         peak = peaks.get("bf16_tflops", 1900.0)
-        tens_time = sp["halfls_gemm"] + sp["final_gemm"]
-        achieved = flops / tens_time / 1e12 if tens_time else 0.0
-        roof = {"bound": "tensor", "kernel": "split bf16 slice GEMMs (tcgen05)",
+        achieved = flops / sp[dom] / 1e12 if sp[dom] else 0.0
+        roof = {"bound": "tensor", "kernel": "k_split_gemm2 (tcgen05 bf16 digit GEMM, "
+                                             "half line strength)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak,
+                "traffic": SPLIT_HALFLS_DRAM_BYTES_PER_COL * ncol / lp[dom],
+                "traffic_source": "ncu dram__bytes_read+write of this kernel on the J<=4 part "
+                                  "of the workload, scaled by Y columns",
+                "algorithmic_tflop_per_launch": flops / lp[dom] / 1e12,
+                "digit_pair_products": pairs,
+                "both_gemms_tflops": ps["flops_tensor"] /
+                (sp["halfls_gemm"] + sp["final_gemm"]) / 1e12,
                 "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"
                 if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s"}
     else:

@@ -807,7 +807,8 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
             }),
             "slice Y");
   if (g != GI_OK) return g;
-  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * K * 3;
+  // algorithmic count: the true contraction length N, not the padded K
+  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * c->N * 3;
   gi_status r = GI_OK;
   cudaError_t e = timed(c, GI_PHASE_HALFLS_GEMM, [&] {
     r = gemm(c, S->mu_slices.p, 3 * S->Mpad, S->mu_exp.p, S->Mpad, S->b_slices.p, ncol,
@@ -851,7 +852,7 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
             }),
             "slice H");
   if (g != GI_OK) return g;
-  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * nvec * (double)ncol * K;
+  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * nvec * (double)ncol * fb.nsize;
   gi_status r = GI_OK;
   timed(c, GI_PHASE_FINAL_GEMM, [&] {
     r = gemm(c, fb.d_digits.p, vpad, fb.d_digit_exp.p, vpad, S->b_slices.p, ncol, S->b_exp.p, T,

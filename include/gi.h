@@ -130,7 +130,8 @@ typedef struct {
   double seconds_gpu;      /* device time of the last gi_run (CUDA events) */
   double flops_halfls;     /* algorithmic FP64 flops of the half line strength */
   double flops_final;      /* algorithmic FP64 flops of the final contraction */
-  double flops_tensor;     /* bf16 tensor flops executed by the split-precision GEMMs */
+  double flops_tensor;     /* bf16 tensor flops of the split-precision GEMMs: digit-pair
+                              products x 2 x the true (unpadded) M, N and K */
   double bytes_correlate;  /* algorithmic HBM bytes of the correlate phase */
   double seconds_phase[GI_NPHASE]; /* device time per phase (GI_RUN_PHASE_TIMING) */
   int32_t launches_phase[GI_NPHASE];
