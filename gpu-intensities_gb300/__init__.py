@@ -67,6 +67,33 @@ class gi_stats(C.Structure):
                 ("kernel_launches", C.c_int32), ("reserved", C.c_int32)]
 
 
+class gi_serve_config(C.Structure):
+    _fields_ = [("slots", C.c_int32), ("reserved", C.c_int32),
+                ("hbm_budget_bytes", C.c_size_t), ("slot_workspace_bytes", C.c_size_t)]
+
+
+class gi_job_info(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("nlines", C.c_int64),
+                ("nlines_filtered", C.c_int64), ("seconds_queued", C.c_double),
+                ("seconds_latency", C.c_double), ("seconds_gpu", C.c_double)]
+
+
+class gi_serve_stats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64),
+                ("lines", C.c_int64), ("lines_filtered", C.c_int64),
+                ("evictions", C.c_int64), ("restores", C.c_int64),
+                ("queued", C.c_int32), ("running", C.c_int32),
+                ("latency_p50", C.c_double), ("latency_p99", C.c_double),
+                ("latency_mean", C.c_double), ("latency_max", C.c_double),
+                ("queue_p50", C.c_double), ("queue_p99", C.c_double),
+                ("resident_bytes", C.c_size_t), ("peak_resident_bytes", C.c_size_t),
+                ("budget_bytes", C.c_size_t), ("slot_workspace_bytes", C.c_size_t),
+                ("slots", C.c_int32), ("reserved", C.c_int32)]
+
+
+GI_JOB_QUEUED, GI_JOB_RUNNING, GI_JOB_DONE, GI_JOB_FAILED = range(4)
+
+
 class GiError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"gi status {status}: {msg}")
@@ -114,7 +141,18 @@ def lib():
         L.gi_set_threej.argtypes = [C.c_void_p, C.c_int, f64p]
         L.gi_set_block.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p,
                                    i32p]
+        L.gi_set_block_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.c_void_p, f64p, i32p]
         L.gi_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]
+        L.gi_serve_start.argtypes = [C.c_void_p, C.POINTER(gi_serve_config)]
+        L.gi_serve_stop.argtypes = [C.c_void_p]
+        L.gi_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                C.POINTER(C.c_uint64)]
+        L.gi_job_wait.argtypes = [C.c_void_p, C.c_uint64, C.c_double, C.POINTER(gi_job_info)]
+        L.gi_job_lines.argtypes = [C.c_void_p, C.c_uint64, C.c_int64, C.c_int64, C.c_void_p]
+        L.gi_job_release.argtypes = [C.c_void_p, C.c_uint64]
+        L.gi_serve_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_serve_stats)]
+        L.gi_serve_reset_stats.argtypes = [C.c_void_p]
         L.gi_get_lines.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
         L.gi_num_levels.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.gi_get_levels.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
@@ -254,6 +292,14 @@ class Engine:
         self._ck(self._L.gi_set_block(self._h, J, gamma, nsize, nvec, _p(v, f64p), _p(e, f64p),
                                       _p(q, i32p)))
 
+    def set_block_device(self, J: int, gamma: int, vecs_dev_ptr: int, nvec: int, nsize: int,
+                         energies: np.ndarray, quanta: np.ndarray):
+        """Block whose vectors are already in device memory ([nvec][nsize] doubles)."""
+        e = np.ascontiguousarray(energies, np.float64)
+        q = np.ascontiguousarray(quanta, np.int32)
+        self._ck(self._L.gi_set_block_device(self._h, J, gamma, nsize, nvec,
+                                             C.c_void_p(vecs_dev_ptr), _p(e, f64p), _p(q, i32p)))
+
     def load(self, prob, precision: int = GI_PREC_FP64, split_slices: int = 0):
         """Hand a synth.Problem (or any object with the same fields) to the engine."""
         self.set_symmetry(prob.sym_type)
@@ -297,6 +343,43 @@ class Engine:
         out["seconds_phase"] = dict(zip(PHASES, list(s.seconds_phase)))
         out["launches_phase"] = dict(zip(PHASES, list(s.launches_phase)))
         return out
+
+    # serving ---------------------------------------------------------------
+    def serve_start(self, slots: int = 3, budget: int = 0, slot_workspace: int = 0):
+        cfg = gi_serve_config(slots, 0, budget, slot_workspace)
+        self._ck(self._L.gi_serve_start(self._h, C.byref(cfg)))
+
+    def serve_stop(self):
+        self._ck(self._L.gi_serve_stop(self._h))
+
+    def submit(self, jI: int, gammaI: int, jF: int, gammaF: int) -> int:
+        i = C.c_uint64(0)
+        self._ck(self._L.gi_submit(self._h, jI, gammaI, jF, gammaF, C.byref(i)))
+        return int(i.value)
+
+    def wait(self, job: int, timeout: float = -1.0, check: bool = True) -> Dict[str, float]:
+        info = gi_job_info()
+        st = self._L.gi_job_wait(self._h, job, timeout, C.byref(info))
+        if check:
+            self._ck(st)
+        return {f: getattr(info, f) for f, _ in gi_job_info._fields_}
+
+    def job_lines(self, job: int, release: bool = True) -> np.ndarray:
+        n = self.wait(job)["nlines"]
+        out = np.empty(n, LINE_DTYPE)
+        if n:
+            self._ck(self._L.gi_job_lines(self._h, job, 0, n, out.ctypes.data))
+        if release:
+            self._ck(self._L.gi_job_release(self._h, job))
+        return out
+
+    def serve_stats(self) -> Dict[str, float]:
+        s = gi_serve_stats()
+        self._ck(self._L.gi_serve_get_stats(self._h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in gi_serve_stats._fields_ if f != "reserved"}
+
+    def serve_reset_stats(self):
+        self._ck(self._L.gi_serve_reset_stats(self._h))
 
     def half_ls(self, jI: int, gammaI: int, ideg: int, jF: int, vsym: np.ndarray,
                 D_F: int) -> np.ndarray:

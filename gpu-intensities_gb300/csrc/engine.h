@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <utility>
 #include <vector>
@@ -90,10 +91,26 @@ struct Block {
   std::vector<int32_t> quanta;                          // [nvec][nmodes+1]
   DevArray<double> d_energies;
   // bf16 digit planes of the vectors for the split-precision path (cut on
-  // first use, dropped when the block is replaced)
+  // first use, dropped when the block is replaced); digits_ev marks their
+  // completion on the stream that cut them
   DevArray<uint16_t> d_digits;
   DevArray<int32_t> d_digit_exp;
   int digits_s = 0, digits_w = 0;
+  cudaEvent_t digits_ev = nullptr;
+  // residency under a serving budget: an evicted block keeps its vectors in
+  // pinned host memory and has no device arrays
+  bool resident = true;
+  double* h_vecs = nullptr;  // pinned [nvec][nsize] while evicted
+  int pins = 0;              // running jobs that use the block
+  uint64_t last_use = 0;     // serving clock of the last admission
+  size_t device_bytes() const {
+    return d_vecs.n * sizeof(double) + d_energies.n * sizeof(double) +
+           d_digits.n * sizeof(uint16_t) + d_digit_exp.n * sizeof(int32_t);
+  }
+  ~Block() {
+    if (digits_ev) cudaEventDestroy(digits_ev);
+    if (h_vecs) cudaFreeHost(h_vecs);
+  }
 };
 
 struct Level {
@@ -102,9 +119,24 @@ struct Level {
 };
 
 struct SplitState;  // split-precision state (split.cu)
+struct Server;      // serving loop (serve.cu)
+
+// One pair job of the serving loop: the lines of block (jI, gI) -> (jF, gF)
+// under the filters of the whole loaded job (its ZPE and J range).
+struct JobSel {
+  bool on = false;
+  int jI = 0, gI = 0, jF = 0, gF = 0;
+  double zpe = 0.0;
+  int jmin = 0, jmax = 0;
+};
 
 struct Ctx {
   SplitState* split = nullptr;
+  Ctx* parent = nullptr;      // a serving worker shares its parent's model state
+  Server* server = nullptr;
+  std::mutex model_mu;        // guards lazily derived shared state (digits)
+  std::mutex& mmu() { return parent ? parent->model_mu : model_mu; }
+  JobSel job;
   int device = 0;
   size_t budget = 0;
   int nsm = 0;
@@ -120,9 +152,10 @@ struct Ctx {
 
   int N = 0, Kp = 0;          // dipole size and padded row stride
   DevArray<double> d_mu;      // [3][N rows f][Kp]: row f holds mu_c(:, f)
+  const double* mu() const { return parent ? parent->d_mu.p : d_mu.p; }
 
-  std::map<int, std::unique_ptr<Basis>> bases;
-  std::map<std::pair<int, int>, std::unique_ptr<Block>> blocks;
+  std::map<int, std::shared_ptr<Basis>> bases;
+  std::map<std::pair<int, int>, std::shared_ptr<Block>> blocks;
 
   int threej_jmax = -1;
   bool threej_user = false;
@@ -179,6 +212,26 @@ cudaError_t timed(Ctx* c, int phase, F&& launch) {
   c->phase_recs.push_back({phase, a, b});
   return e;
 }
+
+// ------------------------------------------------------------------ host
+gi_status fail(Ctx* c, gi_status s, const char* fmt, ...);
+#define GI_CUDA(c, call)                                                                   \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return ::gi::fail((c), e_ == cudaErrorMemoryAllocation ? GI_ERR_NOMEM : GI_ERR_CUDA, \
+                        "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+// Runs every block pair of the loaded job (or the one pair of c->job).
+gi_status run_job(Ctx* c, int flags, int64_t* nlines_out);
+// Builds the (slot, v) -> roots table of a basis for the context's dipole size.
+gi_status ensure_ycsr(Ctx* c, Basis& b);
+// Serving: frees device memory for `bytes` more by evicting unpinned blocks
+// other than `keep` (least recently used first).  Caller holds model_mu.
+gi_status server_make_room(Ctx* c, size_t bytes, Block* keep);
+// Stops the serving loop of c (if any): fails queued jobs, joins the workers.
+gi_status server_stop(Ctx* c);
 
 // ------------------------------------------------------------------ kernels
 struct EpiParams {

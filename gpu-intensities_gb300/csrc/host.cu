@@ -16,7 +16,7 @@
 namespace gi {
 
 // ------------------------------------------------------------------ errors
-static gi_status fail(Ctx* c, gi_status s, const char* fmt, ...) {
+gi_status fail(Ctx* c, gi_status s, const char* fmt, ...) {
   char buf[512];
   va_list ap;
   va_start(ap, fmt);
@@ -25,14 +25,6 @@ static gi_status fail(Ctx* c, gi_status s, const char* fmt, ...) {
   if (c) c->err = buf;
   return s;
 }
-
-#define GI_CUDA(c, call)                                                                   \
-  do {                                                                                     \
-    cudaError_t e_ = (call);                                                               \
-    if (e_ != cudaSuccess)                                                                 \
-      return fail((c), e_ == cudaErrorMemoryAllocation ? GI_ERR_NOMEM : GI_ERR_CUDA,       \
-                  "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__);    \
-  } while (0)
 
 // ------------------------------------------------------------------ 3j
 // Scaled factorial a!/10^a and Wigner 3j symbol computed the way TROVE's
@@ -197,7 +189,7 @@ static gi_status derive_basis(Ctx* c, Basis& b) {
 }
 
 // (slot, v) -> roots, once the dipole size N is known.
-static gi_status ensure_ycsr(Ctx* c, Basis& b) {
+gi_status ensure_ycsr(Ctx* c, Basis& b) {
   if (b.y_N == c->N) return GI_OK;
   const int N = c->N;
   std::vector<int32_t> ptr((size_t)b.nslot * N + 1, 0), roots(b.D);
@@ -317,7 +309,7 @@ static bool degeneracy_ok(const Ctx* c, int gI, int gF, int dI, int dF) {
   return true;
 }
 
-static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
+gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   auto t_start = std::chrono::steady_clock::now();
   if (c->nrep == 0) return fail(c, GI_ERR_STATE, "gi_set_symmetry not called");
   if (!c->have_params) return fail(c, GI_ERR_STATE, "gi_set_params not called");
@@ -331,7 +323,9 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
 
   std::vector<int> jlist;
   for (auto& kv : c->bases) jlist.push_back(kv.first);
-  const int jmin = jlist.front(), jmax = jlist.back();
+  // a pair job keeps the J range of the whole loaded job
+  const int jmin = c->job.on ? c->job.jmin : jlist.front();
+  const int jmax = c->job.on ? c->job.jmax : jlist.back();
   for (auto& kv : c->blocks) {
     auto it = c->bases.find(kv.first.first);
     if (it == c->bases.end()) return fail(c, GI_ERR_STATE, "block J=%d has no basis", kv.first.first);
@@ -339,9 +333,12 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       return fail(c, GI_ERR_ARG, "block (J=%d, gamma=%d): nsize %d != Ntotal %d", kv.first.first,
                   kv.first.second, kv.second->nsize, it->second->Ntotal[kv.first.second]);
   }
-  for (auto& kv : c->bases) {
-    gi_status s = ensure_ycsr(c, *kv.second);
-    if (s != GI_OK) return s;
+  {
+    std::lock_guard<std::mutex> lk(c->mmu());  // bases may be shared with other workers
+    for (auto& kv : c->bases) {
+      gi_status s = ensure_ycsr(c, *kv.second);
+      if (s != GI_OK) return s;
+    }
   }
 
   // igamma pairs (trove_functions.cpp:1041-1072)
@@ -359,8 +356,8 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   }
 
   // ZPE: while negative, every J=0 Gamma=0 record replaces it (trove_functions.cpp:1200-1201)
-  double zpe = P.ZPE;
-  {
+  double zpe = c->job.on ? c->job.zpe : P.ZPE;
+  if (!c->job.on) {
     auto it = c->blocks.find({0, 0});
     if (zpe < 0 && c->bases.count(0) && isym_do(c, 0) && it != c->blocks.end())
       for (double e : it->second->energies)
@@ -405,6 +402,7 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     BlockPlan& bp = kv.second;
     for (int r = 0; r < bp.blk->nvec; r++) {
       if (bp.level_of_rec[r] < 0) continue;
+      if (c->job.on) bp.level_of_rec[r] = r;  // pair jobs report record indices
       const int32_t* q = bp.blk->quanta.data() + (size_t)r * nq;
       const double E = bp.blk->energies[r];
       bp.lower_ok[r] = F.lower(bp.blk->J, E, q);
@@ -431,12 +429,15 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     BlockPlan& I = kv.second;
     const int JI = I.blk->J, gI = I.blk->gamma;
     if (I.ivec.empty() || !(P.gns[gI] > 0.0)) continue;
+    if (c->job.on && (JI != c->job.jI || gI != c->job.gI)) continue;
     for (int JF = JI - 1; JF <= JI + 1; JF++) {
       if (!c->bases.count(JF)) continue;
+      if (c->job.on && JF != c->job.jF) continue;
       if (JI + JF < 1) continue;
       if (JI == jmin && JF == jmin) continue;
       const int gF = igamma_pair[gI];
       if (P.isym_pairs[gI] != P.isym_pairs[gF]) continue;
+      if (c->job.on && gF != c->job.gF) continue;
       auto fit = plans.find({JF, gF});
       if (fit == plans.end() || fit->second.nupper == 0) continue;
       int mask = 0;
@@ -611,7 +612,7 @@ static gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       if (s != GI_OK) return s;
     } else {
       GI_CUDA(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
-                return gemm_fp64_nt(c->d_mu.p, Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp,
+                return gemm_fp64_nt(c->mu(), Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp,
                                     zc, N, (int)R.ncolY, Kp, 3, c->stream);
               }));
     }
@@ -773,6 +774,7 @@ gi_status gi_destroy(gi_ctx* h) {
   if (!h) return GI_OK;
   Ctx* c = reinterpret_cast<Ctx*>(h);
   cudaSetDevice(c->device);
+  server_stop(c);
   cudaStreamSynchronize(c->stream);
   split_release(c);
   if (c->h_lines) cudaFreeHost(c->h_lines);
@@ -799,6 +801,7 @@ const char* gi_last_error(const gi_ctx* h) {
 gi_status gi_set_symmetry(gi_ctx* h, int sym_type) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_set_symmetry while serving");
   switch (sym_type) {
     case 1: c->degen = {1, 1, 1, 1}; break;
     case 2: c->degen = {1, 1, 2}; break;
@@ -825,6 +828,7 @@ gi_status gi_set_params(gi_ctx* h, const gi_params* p) {
 gi_status gi_set_dipole(gi_ctx* h, int N, const double* mu) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c || N <= 0 || !mu) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_set_dipole while serving (gi_serve_stop first)");
   cudaSetDevice(c->device);
   const int Kp = round_up(N, 64);
   std::vector<double> hbuf((size_t)3 * N * Kp, 0.0);
@@ -846,11 +850,12 @@ gi_status gi_set_basis(gi_ctx* h, int J, int D, int ncase, int max_deg_size, int
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c) return GI_ERR_ARG;
   if (c->nrep == 0) return fail(c, GI_ERR_STATE, "gi_set_symmetry must precede gi_set_basis");
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_set_basis while serving (gi_serve_stop first)");
   if (J < 0 || D <= 0 || ncase <= 0 || mat_size <= 0 || !icontr2icase || !iroot_correlat_j0 ||
       !k || !ktau || !Nsym || !Ntotal || !repres)
     return fail(c, GI_ERR_ARG, "gi_set_basis: bad arguments for J=%d", J);
   cudaSetDevice(c->device);
-  auto b = std::make_unique<Basis>();
+  auto b = std::make_shared<Basis>();
   b->J = J;
   b->D = D;
   b->ncase = ncase;
@@ -876,55 +881,100 @@ gi_status gi_set_basis(gi_ctx* h, int J, int D, int ncase, int max_deg_size, int
 gi_status gi_set_threej(gi_ctx* h, int jmax, const double* threej) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c || jmax < 0 || !threej) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_set_threej while serving");
   c->threej.assign(threej, threej + (size_t)(jmax + 1) * (jmax + 1) * 9);
   c->threej_jmax = jmax;
   c->threej_user = true;
   return GI_OK;
 }
 
-gi_status gi_set_block(gi_ctx* h, int J, int gamma, int nsize, int nvec, const double* vecs,
-                       const double* energies, const int32_t* quanta) {
-  Ctx* c = reinterpret_cast<Ctx*>(h);
+static gi_status set_block(Ctx* c, int J, int gamma, int nsize, int nvec, const double* vecs,
+                           bool vecs_on_device, const double* energies, const int32_t* quanta) {
   if (!c) return GI_ERR_ARG;
   if (!c->have_params) return fail(c, GI_ERR_STATE, "gi_set_params must precede gi_set_block");
   if (gamma < 0 || gamma >= c->nrep || nsize < 0 || nvec < 0 || (nsize == 0 && nvec > 0) ||
       (nvec > 0 && (!vecs || !energies || !quanta)))
     return fail(c, GI_ERR_ARG, "gi_set_block: bad arguments for (J=%d, gamma=%d)", J, gamma);
   cudaSetDevice(c->device);
-  std::unique_ptr<Block> b;
+  std::unique_lock<std::mutex> lk(c->model_mu);
+  std::shared_ptr<Block> b;
   auto it = c->blocks.find({J, gamma});
-  if (it != c->blocks.end() && it->second->nsize == nsize && it->second->nvec == nvec)
-    b = std::move(it->second);  // same shape: reuse the device arrays
+  // same shape and used by no running job: reuse the device arrays
+  if (it != c->blocks.end() && it->second->nsize == nsize && it->second->nvec == nvec &&
+      it->second.use_count() == 1 && it->second->resident)
+    b = it->second;
   else
-    b = std::make_unique<Block>();
+    b = std::make_shared<Block>();
   b->J = J;
   b->gamma = gamma;
   b->nsize = nsize;
   b->nvec = nvec;
   b->ld = round_up(nsize, 64);
   b->digits_s = 0;  // new vectors: their split-precision digits are stale
+  b->d_digits.reset();
+  b->d_digit_exp.reset();
   b->energies.assign(energies, energies + nvec);
   const int nq = c->params.nmodes + 1;
   b->quanta.assign(quanta, quanta + (size_t)nvec * nq);
   const size_t need = (size_t)std::max(nvec, 1) * b->ld;
+  if (c->server && b->d_vecs.n != need) {
+    // serving: make room under the budget; if even that fails the block
+    // waits in pinned host memory until a job needs it
+    const size_t bytes = need * sizeof(double) + sizeof(double) * std::max(nvec, 1);
+    if (server_make_room(c, bytes, b.get()) != GI_OK) {
+      const size_t n = (size_t)nvec * nsize;
+      b->d_vecs.reset();
+      if (n) {
+        GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&b->h_vecs), sizeof(double) * n));
+        GI_CUDA(c, cudaMemcpy(b->h_vecs, vecs, sizeof(double) * n,
+                              vecs_on_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+      }
+      if (b->d_energies.n != (size_t)std::max(nvec, 1)) GI_CUDA(c, b->d_energies.alloc(nvec));
+      if (nvec)
+        GI_CUDA(c, cudaMemcpy(b->d_energies.p, b->energies.data(), sizeof(double) * nvec,
+                              cudaMemcpyHostToDevice));
+      GI_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));
+      b->resident = false;
+      c->err.clear();
+      c->blocks[{J, gamma}] = b;
+      return GI_OK;
+    }
+  }
   if (b->d_vecs.n != std::max<size_t>(need, 1)) {
     GI_CUDA(c, b->d_vecs.alloc(need));
     GI_CUDA(c, cudaMemset(b->d_vecs.p, 0, sizeof(double) * b->d_vecs.n));
   }
   if (nvec)
     GI_CUDA(c, cudaMemcpy2D(b->d_vecs.p, sizeof(double) * b->ld, vecs, sizeof(double) * nsize,
-                            sizeof(double) * nsize, nvec, cudaMemcpyHostToDevice));
+                            sizeof(double) * nsize, nvec,
+                            vecs_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
   if (b->d_energies.n != (size_t)std::max(nvec, 1)) GI_CUDA(c, b->d_energies.alloc(nvec));
   if (nvec)
     GI_CUDA(c, cudaMemcpy(b->d_energies.p, b->energies.data(), sizeof(double) * nvec,
                           cudaMemcpyHostToDevice));
-  c->blocks[{J, gamma}] = std::move(b);
+  // the copies above ran on the legacy stream; order them before any stream
+  GI_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));
+  b->resident = true;
+  c->blocks[{J, gamma}] = b;
   return GI_OK;
+}
+
+gi_status gi_set_block(gi_ctx* h, int J, int gamma, int nsize, int nvec, const double* vecs,
+                       const double* energies, const int32_t* quanta) {
+  return set_block(reinterpret_cast<Ctx*>(h), J, gamma, nsize, nvec, vecs, false, energies, quanta);
+}
+
+gi_status gi_set_block_device(gi_ctx* h, int J, int gamma, int nsize, int nvec,
+                              const double* vecs_dev, const double* energies,
+                              const int32_t* quanta) {
+  return set_block(reinterpret_cast<Ctx*>(h), J, gamma, nsize, nvec, vecs_dev, true, energies,
+                   quanta);
 }
 
 gi_status gi_run(gi_ctx* h, int flags, int64_t* nlines) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c || !nlines) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_run while serving (gi_serve_stop first)");
   cudaSetDevice(c->device);
   c->err.clear();
   return run_job(c, flags, nlines);

@@ -730,6 +730,19 @@ gi_status split_prepare(Ctx* c) {
   if (g != GI_OK) return g;
   g = check(c, cudaMemsetAsync(S->err.p, 0, sizeof(int), c->stream), "error word");
   if (g != GI_OK) return g;
+  if (c->parent) {
+    // a serving worker uses its parent's dipole digits (cut before admission)
+    const SplitState* P = c->parent->split;
+    if (!P || P->N != c->N || P->s != sh.s || P->w != sh.w) {
+      c->err = "split precision: the dipole digits of the serving context are not prepared";
+      return GI_ERR_STATE;
+    }
+    S->s = P->s;
+    S->w = P->w;
+    S->N = P->N;
+    S->Mpad = P->Mpad;
+    return GI_OK;
+  }
   if (S->N == c->N && S->s == sh.s && S->w == sh.w) return GI_OK;
   // digit planes of the dipole: rows = 3 components x Mpad, K = Kp
   S->s = sh.s;
@@ -811,7 +824,8 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
   c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * c->N * 3;
   gi_status r = GI_OK;
   cudaError_t e = timed(c, GI_PHASE_HALFLS_GEMM, [&] {
-    r = gemm(c, S->mu_slices.p, 3 * S->Mpad, S->mu_exp.p, S->Mpad, S->b_slices.p, ncol,
+    const SplitState* D = c->parent ? c->parent->split : S;  // owner of the dipole digits
+    r = gemm(c, D->mu_slices.p, 3 * S->Mpad, D->mu_exp.p, S->Mpad, S->b_slices.p, ncol,
              S->b_exp.p, Z, ldz, zstride, c->N, ncol, K, 3);
     return cudaSuccess;
   });
@@ -827,20 +841,34 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
   const int vpad = round_up(nvec, kBM);
   gi_status g;
   // the final-state vectors are fixed inputs: their digits are cut once and
-  // kept with the block until it is replaced
-  if (fb.digits_s != S->s || fb.digits_w != S->w) {
-    g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
-    if (g != GI_OK) return g;
-    g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
-    if (g != GI_OK) return g;
-    g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-                return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, fb.d_digits.p,
-                             fb.d_digit_exp.p, c->stream);
-              }),
-              "slice V");
-    if (g != GI_OK) return g;
-    fb.digits_s = S->s;
-    fb.digits_w = S->w;
+  // kept with the block until it is replaced.  Serving workers share blocks,
+  // so the cut happens under the model lock and the others wait on its event.
+  {
+    std::lock_guard<std::mutex> lk(c->mmu());
+    if (fb.digits_s != S->s || fb.digits_w != S->w) {
+      g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
+      if (g != GI_OK) return g;
+      g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
+      if (g != GI_OK) return g;
+      g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                  return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, fb.d_digits.p,
+                               fb.d_digit_exp.p, c->stream);
+                }),
+                "slice V");
+      if (g != GI_OK) return g;
+      if (!fb.digits_ev) {
+        g = check(c, cudaEventCreateWithFlags(&fb.digits_ev, cudaEventDisableTiming), "event");
+        if (g != GI_OK) return g;
+      }
+      g = check(c, cudaEventRecord(fb.digits_ev, c->stream), "event");
+      if (g != GI_OK) return g;
+      fb.digits_s = S->s;
+      fb.digits_w = S->w;
+    }
+    if (fb.digits_ev) {
+      g = check(c, cudaStreamWaitEvent(c->stream, fb.digits_ev, 0), "event wait");
+      if (g != GI_OK) return g;
+    }
   }
   g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "H slices");
   if (g != GI_OK) return g;

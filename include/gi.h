@@ -178,6 +178,14 @@ gi_status gi_set_threej(gi_ctx* ctx, int jmax, const double* threej);
 gi_status gi_set_block(gi_ctx* ctx, int J, int gamma, int nsize, int nvec, const double* vecs,
                        const double* energies, const int32_t* quanta);
 
+/* The same, with vecs_dev a device pointer of the context's GPU
+   (vecs_dev[nvec][nsize], e.g. an eigensolver's output already in HBM); the
+   engine copies it device to device.  No counterpart in the reference, which
+   reads every vector from disk (cuda_host.cu:1196-1199). */
+gi_status gi_set_block_device(gi_ctx* ctx, int J, int gamma, int nsize, int nvec,
+                              const double* vecs_dev, const double* energies,
+                              const int32_t* quanta);
+
 /* Run ---------------------------------------------------------------------- */
 #define GI_RUN_LINES_ON_DEVICE 1 /* keep lines in device memory (no D2H) */
 #define GI_RUN_PHASE_TIMING 2    /* time every kernel with CUDA events (gi_stats) */
@@ -216,6 +224,71 @@ gi_status gi_half_ls(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF, const do
 #define GI_NOALLOC_SCRATCH_BYTES ((16u << 20) + (52u << 10))
 gi_status gi_half_ls_noalloc(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF,
                              const double* vsym_dev, double* half_ls_dev, void* stream);
+
+/* Serving ----------------------------------------------------------------- */
+/* No counterpart in the reference, which processes one (J, J+1) job per
+ * process (main.cu:34-95).  A serving context takes intensity jobs of single
+ * block pairs (J, Gamma) -> (J', Gamma') as an upstream eigensolver finishes
+ * blocks, and runs up to `slots` of them at once, each on its own stream, so
+ * their work overlaps on the GPU.  Jobs are admitted in arrival order when a
+ * slot is free and their blocks fit the budget; blocks stay resident in HBM
+ * and the least recently used blocks that no running job holds move to pinned
+ * host memory when room is needed.  A job's lines are the lines of that block
+ * pair that gi_run over all loaded blocks produces (same filters, ZPE and J
+ * range), with level_i / level_f holding record indices within the two blocks.
+ * While serving, gi_set_block / gi_set_block_device / gi_set_params (except
+ * precision and split_slices) / gi_submit and the job calls may be used from
+ * the context's thread; the other setters and gi_run return GI_ERR_STATE. */
+typedef struct {
+  int32_t slots;                /* jobs in flight, one stream each (0: 3) */
+  int32_t reserved;
+  size_t hbm_budget_bytes;      /* device bytes for resident blocks and slot
+                                   workspaces (0: the context's budget, else
+                                   80 % of the free memory) */
+  size_t slot_workspace_bytes;  /* workspace cap per slot (0: budget / (4 slots)) */
+} gi_serve_config;
+
+#define GI_JOB_QUEUED 0
+#define GI_JOB_RUNNING 1
+#define GI_JOB_DONE 2
+#define GI_JOB_FAILED 3
+
+typedef struct {
+  int32_t state;              /* GI_JOB_* */
+  int32_t status;             /* gi_status of a finished job */
+  int64_t nlines;             /* lines kept (after the intensity threshold) */
+  int64_t nlines_filtered;    /* lines that passed the selection filters */
+  double seconds_queued;      /* submit -> admission */
+  double seconds_latency;     /* submit -> done (or -> now while in flight) */
+  double seconds_gpu;         /* device time of the job's launch sequence */
+} gi_job_info;
+
+typedef struct {
+  int64_t submitted, completed, failed;
+  int64_t lines, lines_filtered;
+  int64_t evictions, restores;  /* blocks moved to / back from pinned host */
+  int32_t queued, running;
+  double latency_p50, latency_p99, latency_mean, latency_max;  /* seconds */
+  double queue_p50, queue_p99;
+  size_t resident_bytes, peak_resident_bytes, budget_bytes, slot_workspace_bytes;
+  int32_t slots;
+  int32_t reserved;
+} gi_serve_stats;
+
+gi_status gi_serve_start(gi_ctx* ctx, const gi_serve_config* cfg);
+/* Waits for the running jobs; queued jobs fail with GI_ERR_STATE. */
+gi_status gi_serve_stop(gi_ctx* ctx);
+gi_status gi_submit(gi_ctx* ctx, int jI, int gammaI, int jF, int gammaF, uint64_t* job_id);
+/* Waits up to timeout_s seconds (< 0: without limit) for the job to finish;
+   info (optional) receives its state.  Returns the job's status once done. */
+gi_status gi_job_wait(gi_ctx* ctx, uint64_t job_id, double timeout_s, gi_job_info* info);
+gi_status gi_job_lines(gi_ctx* ctx, uint64_t job_id, int64_t offset, int64_t count,
+                       gi_line* out);
+/* Forgets a finished job and its lines. */
+gi_status gi_job_release(gi_ctx* ctx, uint64_t job_id);
+/* Latency percentiles over the jobs finished since start / the last reset. */
+gi_status gi_serve_get_stats(gi_ctx* ctx, gi_serve_stats* out);
+gi_status gi_serve_reset_stats(gi_ctx* ctx);
 
 #ifdef __cplusplus
 }
