@@ -63,6 +63,11 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-path comparison")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--serve-jmax", type=int, default=4,
+                    help="serving: pair jobs of the J <= jmax part of the workload")
+    ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: Poisson jobs/s")
+    ap.add_argument("--serve-slots", type=int, default=3)
     return ap.parse_args()
 
 
@@ -255,6 +260,50 @@ def main_reference(args):
     return 0
 
 
+# ---------------------------------------------------------------- serving
+def serve_bench(pkg, args, device, precision):
+    """Pair jobs (J, Gamma) -> (J', Gamma') of the J <= serve_jmax part of the
+    workload, submitted in random order with Poisson arrivals at serve_rate
+    jobs/s to a serving context; latency is submit -> lines on the host."""
+    import argparse as _a
+    sub = _a.Namespace(**vars(args))
+    sub.jmax = args.serve_jmax
+    prob = make_problem(sub)
+    jobs = prob.pair_jobs()
+    rng = np.random.default_rng(args.seed + 17)
+    order = [jobs[i] for i in rng.permutation(len(jobs))]
+    gaps = rng.exponential(1.0 / args.serve_rate, size=len(order))
+    with pkg.Engine(device) as eng:
+        eng.load(prob, precision=precision, split_slices=args.slices)
+        eng.serve_start(slots=args.serve_slots)
+        eng.job_lines(eng.submit(*order[0]))  # first launch of every kernel
+        eng.serve_reset_stats()
+        ids = []
+        t0 = time.perf_counter()
+        due = t0
+        for job, gap in zip(order, gaps):
+            due += gap
+            delay = due - time.perf_counter()
+            if delay > 0:
+                time.sleep(delay)
+            ids.append(eng.submit(*job))
+        for i in ids:
+            eng.job_lines(i)
+        makespan = time.perf_counter() - t0
+        st = eng.serve_stats()
+        eng.serve_stop()
+    return {"workload": f"{args.workload} J<={args.serve_jmax} pair jobs", "jobs": len(order),
+            "arrival": f"Poisson {args.serve_rate:g} jobs/s, random order",
+            "slots": st["slots"], "precision": "split" if precision else "fp64",
+            "latency_p50_s": st["latency_p50"], "latency_p99_s": st["latency_p99"],
+            "latency_max_s": st["latency_max"], "latency_mean_s": st["latency_mean"],
+            "queue_p50_s": st["queue_p50"], "queue_p99_s": st["queue_p99"],
+            "makespan_s": makespan, "value": st["lines_filtered"] / makespan, "unit": METRIC,
+            "lines_filtered": st["lines_filtered"], "lines_above_threshold": st["lines"],
+            "failed": st["failed"], "evictions": st["evictions"],
+            "budget_bytes": st["budget_bytes"], "peak_resident_bytes": st["peak_resident_bytes"]}
+
+
 # ---------------------------------------------------------------- our arm
 def main_ours(args):
     import torch
@@ -391,6 +440,12 @@ def main_ours(args):
         eng.set_params(prob.params, precision=prec, split_slices=args.slices)
         accuracy = split_accuracy(pkg, prob, args.slices, local)
 
+    serving = None
+    if not args.no_serve and world == 1:
+        serving = {"split": serve_bench(pkg, args, local, pkg.GI_PREC_SPLIT)}
+        if not args.no_fp64:
+            serving["fp64"] = serve_bench(pkg, args, local, pkg.GI_PREC_FP64)
+
     if world > 1:
         t = torch.tensor([dt], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -406,7 +461,8 @@ def main_ours(args):
                "lines_per_step": lines_pre, "lines_above_threshold_per_step": lines_post,
                "value_above_threshold": world * lines_post / dt,
                "gpu_launches": launches, "roofline": roof, "e2e": e2e,
-               "fp64_path": fp64, "accuracy": accuracy, "clocks": clk.summary()}
+               "fp64_path": fp64, "accuracy": accuracy, "serving": serving,
+               "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(prob)
         print(json.dumps(out))

@@ -136,6 +136,7 @@ def lib():
         L.gi_set_symmetry.argtypes = [C.c_void_p, C.c_int]
         L.gi_set_params.argtypes = [C.c_void_p, C.POINTER(gi_params)]
         L.gi_set_dipole.argtypes = [C.c_void_p, C.c_int, f64p]
+        L.gi_set_dipole_flipped.argtypes = [C.c_void_p, C.c_int, f64p]
         L.gi_set_basis.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    i32p, i32p, i32p, i32p, i32p, i32p, C.POINTER(f64p)]
         L.gi_set_threej.argtypes = [C.c_void_p, C.c_int, f64p]
@@ -269,6 +270,13 @@ class Engine:
         if m.size != 3 * N * N:
             raise ValueError("mu must hold 3*N*N doubles")
         self._ck(self._L.gi_set_dipole(self._h, N, _p(m, f64p)))
+
+    def set_dipole_flipped(self, N: int, dip: np.ndarray):
+        """Dipole in the reference's flipped layout: dip[c][i][f] = mu_c(i, f)."""
+        m = np.ascontiguousarray(dip, np.float64).reshape(-1)
+        if m.size != 3 * N * N:
+            raise ValueError("dip must hold 3*N*N doubles")
+        self._ck(self._L.gi_set_dipole_flipped(self._h, N, _p(m, f64p)))
 
     def set_basis(self, b):
         arrs = [np.ascontiguousarray(getattr(b, n), np.int32) for n in

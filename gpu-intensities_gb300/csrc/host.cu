@@ -843,6 +843,26 @@ gi_status gi_set_dipole(gi_ctx* h, int N, const double* mu) {
   return GI_OK;
 }
 
+gi_status gi_set_dipole_flipped(gi_ctx* h, int N, const double* dip) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || N <= 0 || !dip) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_set_dipole_flipped while serving");
+  cudaSetDevice(c->device);
+  const int Kp = round_up(N, 64);
+  std::vector<double> hbuf((size_t)3 * N * Kp, 0.0);
+  // dip[f + i*N + c*N*N] = mu_c(i, f); device row f holds mu_c(:, f)
+  for (int comp = 0; comp < 3; comp++)
+    for (int i = 0; i < N; i++) {
+      const double* src = dip + (size_t)comp * N * N + (size_t)i * N;
+      for (int f = 0; f < N; f++) hbuf[((size_t)comp * N + f) * Kp + i] = src[f];
+    }
+  GI_CUDA(c, c->d_mu.upload(hbuf));
+  c->N = N;
+  c->Kp = Kp;
+  split_invalidate(c);
+  return GI_OK;
+}
+
 gi_status gi_set_basis(gi_ctx* h, int J, int D, int ncase, int max_deg_size, int mat_size,
                        const int32_t* icontr2icase, const int32_t* iroot_correlat_j0,
                        const int32_t* k, const int32_t* ktau, const int32_t* Nsym,

@@ -123,6 +123,27 @@ class Problem:
     def jlist(self) -> List[int]:
         return sorted(self.bases)
 
+    def partner(self, g: int) -> int:
+        """The symmetry a level of symmetry g can reach (find_igamma_pair,
+        trove_functions.cpp:1041-1072): the other irrep of its isym_pairs
+        class, or g itself when it is alone in its class."""
+        for h in range(len(self.params.isym_pairs)):
+            if h != g and self.params.isym_pairs[h] == self.params.isym_pairs[g]:
+                return h
+        return g
+
+    def pair_jobs(self) -> List[Tuple[int, int, int, int]]:
+        """Block pairs (jI, gI, jF, gF) that can carry lines: |dJ| <= 1 and
+        gF the partner of gI, both blocks present with vectors."""
+        out = []
+        for (jI, gI), bI in sorted(self.blocks.items()):
+            gF = self.partner(gI)
+            for jF in (jI - 1, jI, jI + 1):
+                bF = self.blocks.get((jF, gF))
+                if bI.nvec and bF is not None and bF.nvec:
+                    out.append((jI, gI, jF, gF))
+        return out
+
     def nlines_upper_bound(self) -> int:
         n = 0
         for (jI, gI), bI in self.blocks.items():

@@ -21,7 +21,7 @@
  *                          (cuda_host.cu:900-993, 1501-1503)
  *   gi_set_symmetry        read_symmetry (fields.cpp:11-115)
  *   gi_set_params          read_intensities / read_fields (fields.cpp:145-282)
- *   gi_set_dipole          read_dipole_flipped + its upload
+ *   gi_set_dipole(_flipped) read_dipole_flipped + its upload
  *                          (trove_functions.cpp:113-205, cuda_host.cu:983)
  *   gi_set_basis           bset_contr_factory + correlate_index +
  *                          compute_ijterms + copy_bset_contr_to_gpu
@@ -159,6 +159,10 @@ gi_status gi_set_params(gi_ctx* ctx, const gi_params* p);
 /* mu: [3][N*N] doubles in the checkpoint's record order, mu_c(i,f) at
    c*N*N + i + f*N (c = x, y, z). */
 gi_status gi_set_dipole(gi_ctx* ctx, int N, const double* mu);
+/* The same dipole in the reference's in-memory layout after
+   read_dipole_flipped (trove_functions.cpp:113-205): dip[f + i*N + c*N*N] =
+   mu_c(i, f), i.e. FintensityJob::dipole_me. */
+gi_status gi_set_dipole_flipped(gi_ctx* ctx, int N, const double* dip);
 /* The per-J contracted basis (TO_bset_contrT):
      icontr2icase[2*D]:   [r] = case, [r+D] = lambda (degenerate component)
      iroot_correlat_j0[D], k[D], ktau[D] (= 2k+tau)

@@ -106,3 +106,19 @@ def test_errors_are_reported(pkg, synth):
         assert e.value.status == pkg.GI_ERR_ARG
         with pytest.raises(pkg.GiError):
             eng.set_symmetry(9)
+
+
+def test_flipped_dipole_layout(pkg, synth):
+    """gi_set_dipole_flipped (the reference's in-memory layout) = gi_set_dipole."""
+    prob = synth.make_c2v(31, 30, [0, 1, 2], nvec_max=6)
+    got = []
+    for flipped in (False, True):
+        with pkg.Engine(0) as eng:
+            eng.load(prob)
+            if flipped:
+                N = prob.N
+                eng.set_dipole_flipped(N, prob.mu.reshape(3, N, N).transpose(0, 2, 1))
+            eng.run()
+            got.append(np.sort(eng.lines(), order=["level_i", "level_f"]))
+    assert len(got[0]) > 50
+    assert np.array_equal(got[0]["S"], got[1]["S"])
