@@ -342,11 +342,11 @@ def main_ours(args):
         return a.elapsed_time(b) * 1e-3 / k, out
 
     for _ in range(args.warmup):
-        eng.run(lines_on_device=True)
+        eng.run(lines_on_device=True, graph=True)
     stats = []
 
     def one():
-        eng.run(lines_on_device=True)
+        eng.run(lines_on_device=True, graph=True)
         stats.append(eng.stats())
 
     with ClockSampler(local) as clk:
@@ -417,7 +417,7 @@ def main_ours(args):
             eng.set_dipole(prob.N, mu.numpy())
             for (J, g), b in sorted(prob.blocks.items()):
                 eng.set_block(J, g, pin[(J, g)].numpy(), b.energies, b.quanta)
-            return eng.run(lines_on_device=False)
+            return eng.run(lines_on_device=False, graph=True)
 
         step()
         te, n = timed_steps(ne, step)
@@ -431,8 +431,8 @@ def main_ours(args):
     fp64 = accuracy = None
     if args.precision == "split" and not args.no_fp64:
         eng.set_params(prob.params, precision=pkg.GI_PREC_FP64)
-        eng.run(lines_on_device=True)
-        tf, _ = timed_steps(1, lambda: eng.run(lines_on_device=True))
+        eng.run(lines_on_device=True, graph=True)
+        tf, _ = timed_steps(1, lambda: eng.run(lines_on_device=True, graph=True))
         fs = eng.stats()
         fp64 = {"value": world * fs["nlines_filtered"] / tf, "unit": METRIC,
                 "ms_per_step": 1e3 * tf, "steps": 1, "warmup": 1,
@@ -460,7 +460,8 @@ def main_ours(args):
                "config": config_of(args, prob),
                "lines_per_step": lines_pre, "lines_above_threshold_per_step": lines_post,
                "value_above_threshold": world * lines_post / dt,
-               "gpu_launches": launches, "roofline": roof, "e2e": e2e,
+               "gpu_launches": launches, "graph": "each step is one CUDA graph launch (captured "
+               "in warm-up, replayed)", "roofline": roof, "e2e": e2e,
                "fp64_path": fp64, "accuracy": accuracy, "serving": serving,
                "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:

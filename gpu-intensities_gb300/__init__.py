@@ -29,6 +29,7 @@ GI_OK, GI_ERR_ARG, GI_ERR_CUDA, GI_ERR_NOMEM, GI_ERR_STATE, GI_ERR_BUDGET, GI_ER
 GI_PREC_FP64, GI_PREC_SPLIT = 0, 1
 GI_RUN_LINES_ON_DEVICE = 1
 GI_RUN_PHASE_TIMING = 2
+GI_RUN_GRAPH = 4
 PHASES = ("correlate", "halfls_gemm", "stencil", "final_gemm", "epilogue", "slice")
 GI_MAX_REP, GI_MAX_MODES = 8, 16
 
@@ -319,10 +320,11 @@ class Engine:
             self.set_block(J, g, b.vecs, b.energies, b.quanta)
 
     # run -----------------------------------------------------------------
-    def run(self, lines_on_device: bool = False, phase_timing: bool = False) -> int:
+    def run(self, lines_on_device: bool = False, phase_timing: bool = False,
+            graph: bool = False) -> int:
         n = C.c_int64(0)
         flags = (GI_RUN_LINES_ON_DEVICE if lines_on_device else 0) | \
-            (GI_RUN_PHASE_TIMING if phase_timing else 0)
+            (GI_RUN_PHASE_TIMING if phase_timing else 0) | (GI_RUN_GRAPH if graph else 0)
         self._ck(self._L.gi_run(self._h, flags, C.byref(n)))
         return int(n.value)
 

@@ -50,6 +50,14 @@ struct DevArray {
     return e != cudaSuccess ? e : cudaStreamSynchronize(cudaStreamLegacy);
   }
   cudaError_t upload(const std::vector<T>& v) { return upload(v.data(), v.size()); }
+  // Like upload, but keeps the allocation (and so the address) when it is
+  // large enough: tables a captured CUDA graph reads stay where they were.
+  cudaError_t assign(const std::vector<T>& v) {
+    cudaError_t e = reserve(std::max<size_t>(v.size(), 1));
+    if (e != cudaSuccess || v.empty()) return e;
+    e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+    return e != cudaSuccess ? e : cudaStreamSynchronize(cudaStreamLegacy);
+  }
   // grow-only workspace
   cudaError_t reserve(size_t count) { return count <= n ? cudaSuccess : alloc(count); }
 };
@@ -65,7 +73,12 @@ struct StencilTerm {
   double coef;
 };
 
+// Process-wide serial numbers: a captured launch sequence is tied to the
+// exact basis objects it read.
+uint64_t next_uid();
+
 struct Basis {
+  uint64_t uid = next_uid();
   int J = 0, D = 0, ncase = 0, max_deg = 0, mat_size = 0;
   std::vector<int32_t> icontr2icase, iroot, k, ktau, Nsym, Ntotal, ijterms;
   std::vector<std::vector<double>> repres;  // per gamma
@@ -188,8 +201,15 @@ struct Ctx {
     return ev_pool[ev_used++];
   }
 
+  // CUDA graph of the last captured launch sequence (GI_RUN_GRAPH) and the
+  // plan it was captured for
+  cudaGraphExec_t gexec = nullptr;
+  uint64_t gsig = 0;
+  gi_stats gstats{};
+  int64_t graph_replays = 0;
+
   // workspaces
-  DevArray<double> w_y, w_z, w_h, w_t;
+  DevArray<double> w_y, w_z, w_h, w_t, w_EI;
   DevArray<unsigned long long> w_counter;
   DevArray<int32_t> w_ivec, w_int;
   DevArray<uint8_t> w_upper;

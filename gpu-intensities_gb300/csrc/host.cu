@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <cstdarg>
@@ -14,6 +15,11 @@
 #include "split.h"
 
 namespace gi {
+
+uint64_t next_uid() {
+  static std::atomic<uint64_t> n{1};
+  return n++;
+}
 
 // ------------------------------------------------------------------ errors
 gi_status fail(Ctx* c, gi_status s, const char* fmt, ...) {
@@ -457,8 +463,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       pairs.push_back(PairPlan{&I, &fit->second, mask, st_off[{JI, JF}]});
     }
   }
-  GI_CUDA(c, c->w_stencil.upload(st_all));
-  GI_CUDA(c, c->w_stencil_n.upload(stn_all));
+  GI_CUDA(c, c->w_stencil.assign(st_all));
+  GI_CUDA(c, c->w_stencil_n.assign(stn_all));
 
   Phys ph;
   const double beta = ph.planck * ph.vellgt / (ph.boltz * P.temperature);
@@ -478,8 +484,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     h_int.insert(h_int.end(), bp.level_of_rec.begin(), bp.level_of_rec.end());
     h_upper.insert(h_upper.end(), bp.upper_ok.begin(), bp.upper_ok.end());
   }
-  GI_CUDA(c, c->w_int.upload(h_int));
-  GI_CUDA(c, c->w_upper.upload(h_upper));
+  GI_CUDA(c, c->w_int.assign(h_int));
+  GI_CUDA(c, c->w_upper.assign(h_upper));
   GI_CUDA(c, c->w_counter.reserve(2));
   GI_CUDA(c, cudaMemsetAsync(c->w_counter.p, 0, 2 * sizeof(unsigned long long), c->stream));
 
@@ -573,26 +579,82 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       max_t = std::max(max_t, T.ncolH * round_up(T.F->blk->nvec, 2));
     }
   }
-  GI_CUDA(c, c->w_ivec.upload(h_ivec));
-  DevArray<double> d_EI;
-  GI_CUDA(c, d_EI.upload(h_EI));
+  GI_CUDA(c, c->w_ivec.assign(h_ivec));
+  GI_CUDA(c, c->w_EI.assign(h_EI));
+  DevArray<double>& d_EI = c->w_EI;
   GI_CUDA(c, c->w_y.reserve(max_y));
   GI_CUDA(c, c->w_z.reserve(3 * max_y));
   GI_CUDA(c, c->w_h.reserve(max_h));
   GI_CUDA(c, c->w_t.reserve(max_t));
-  if (P.precision == GI_PREC_SPLIT) {
-    gi_status s = split_prepare(c);
-    if (s != GI_OK) return s;
-  }
-
   c->stats = gi_stats{};
   c->timing = (flags & GI_RUN_PHASE_TIMING) != 0;
   c->ev_used = 0;
   c->phase_recs.clear();
+  const bool use_graph = (flags & GI_RUN_GRAPH) && !c->timing && !c->parent;
+  if (P.precision == GI_PREC_SPLIT) {
+    gi_status s = split_prepare(c);
+    if (s != GI_OK) return s;
+    // every allocation of the launch sequence happens here, before it
+    size_t max_b = 1, max_cols = 1;
+    std::vector<Block*> finals;
+    for (size_t r = 0; r < rounds.size(); r++) {
+      max_b = std::max(max_b, rounds[r].ncolY * Kp);
+      max_cols = std::max(max_cols, rounds[r].ncolY);
+      for (const Target& T : targets[r]) {
+        max_b = std::max(max_b, T.ncolH * T.F->blk->ld);
+        max_cols = std::max(max_cols, T.ncolH);
+        finals.push_back(T.F->blk);
+      }
+    }
+    s = split_reserve(c, max_b, max_cols, finals);
+    if (s != GI_OK) return s;
+  }
+
+  // The plan's identity for graph replay: every pointer, size and value the
+  // launch sequence passes to a kernel follows from these.
+  uint64_t sig = 1469598103934665603ull;
+  auto mix = [&sig](const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    for (size_t i = 0; i < n; i++) sig = (sig ^ b[i]) * 1099511628211ull;
+  };
+  auto mixv = [&mix](auto v) { mix(&v, sizeof(v)); };
+  if (use_graph) {
+    mix(&P, sizeof(P));
+    mixv(zpe); mixv(beta); mixv(N); mixv(Kp); mixv(c->mu()); mixv(c->stream);
+    for (void* q : {(void*)c->w_y.p, (void*)c->w_z.p, (void*)c->w_h.p, (void*)c->w_t.p,
+                    (void*)c->w_EI.p, (void*)c->w_ivec.p, (void*)c->w_int.p, (void*)c->w_upper.p,
+                    (void*)c->w_stencil.p, (void*)c->w_stencil_n.p, (void*)c->w_counter.p,
+                    (void*)c->d_lines.p})
+      mixv(q);
+    mixv(c->d_lines.n);
+    if (P.precision == GI_PREC_SPLIT) mixv(split_identity(c));
+    for (size_t r = 0; r < rounds.size(); r++) {
+      mixv(rounds[r].ncolY);
+      for (const Unit& u : rounds[r].units) {
+        const Block& b = *u.I->blk;
+        const Basis& bs = *c->bases[b.J];
+        mixv(b.d_vecs.p); mixv(b.ld); mixv(b.J); mixv(b.gamma); mixv(u.nI); mixv(u.off);
+        mixv(u.ycol); mixv(u.ncolY); mixv(bs.uid); mixv(bs.d_yptr.p); mixv(bs.d_yroot.p);
+      }
+      for (const Target& T : targets[r]) {
+        const Block& fb = *T.F->blk;
+        mixv(fb.d_vecs.p); mixv(fb.d_digits.p); mixv(fb.d_digit_exp.p); mixv(fb.d_energies.p);
+        mixv(fb.nvec); mixv(fb.nsize); mixv(fb.ld); mixv(T.ncolH); mixv(fb.J); mixv(fb.gamma);
+        mixv(c->bases[fb.J]->uid);
+        mixv(farr[T.F].first); mixv(farr[T.F].second);
+        for (size_t k = 0; k < T.parts.size(); k++) {
+          mixv(T.hcol[k]); mixv(T.parts[k].first->off); mixv(T.parts[k].first->ycol);
+          mixv(T.parts[k].second->combo_mask); mixv(T.parts[k].second->st_off);
+        }
+      }
+    }
+  }
+
   double fl_half = 0.0, fl_final = 0.0, by_corr = 0.0;
   int64_t npairs_checked = 0;
 
-  GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  // the launch sequence of the job, issued eagerly or under stream capture
+  auto issue = [&]() -> gi_status {
   for (size_t r = 0; r < rounds.size(); r++) {
     const Round& R = rounds[r];
     if (R.units.empty()) continue;
@@ -680,6 +742,54 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         npairs_checked += (int64_t)u.nI * Fp.nupper;
       }
     }
+  }
+  return GI_OK;
+  };
+
+  GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  if (use_graph && c->gexec && c->gsig == sig) {
+    // replay: the captured sequence with this run's table contents
+    GI_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    const gi_stats& g = c->gstats;  // what the captured sequence adds to a run's counts
+    for (int ph = 0; ph < GI_NPHASE; ph++) c->stats.launches_phase[ph] += g.launches_phase[ph];
+    c->stats.kernel_launches += g.kernel_launches;
+    c->stats.flops_tensor += g.flops_tensor;
+    fl_half = g.flops_halfls;
+    fl_final = g.flops_final;
+    by_corr = g.bytes_correlate;
+    npairs_checked = g.npairs_checked;
+    c->graph_replays++;
+  } else if (use_graph) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    c->gexec = nullptr;
+    c->gsig = 0;
+    const gi_stats pre = c->stats;
+    GI_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    gi_status st = issue();
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (st != GI_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return st;
+    }
+    GI_CUDA(c, ce);
+    const cudaError_t ie = cudaGraphInstantiate(&c->gexec, graph, 0);
+    cudaGraphDestroy(graph);
+    GI_CUDA(c, ie);
+    GI_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
+    c->gsig = sig;
+    c->gstats = gi_stats{};
+    for (int ph = 0; ph < GI_NPHASE; ph++)
+      c->gstats.launches_phase[ph] = c->stats.launches_phase[ph] - pre.launches_phase[ph];
+    c->gstats.kernel_launches = c->stats.kernel_launches - pre.kernel_launches;
+    c->gstats.flops_tensor = c->stats.flops_tensor - pre.flops_tensor;
+    c->gstats.flops_halfls = fl_half;
+    c->gstats.flops_final = fl_final;
+    c->gstats.bytes_correlate = by_corr;
+    c->gstats.npairs_checked = npairs_checked;
+  } else {
+    gi_status st = issue();
+    if (st != GI_OK) return st;
   }
   GI_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   unsigned long long counts[2] = {0, 0};
@@ -775,6 +885,7 @@ gi_status gi_destroy(gi_ctx* h) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   cudaSetDevice(c->device);
   server_stop(c);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   cudaStreamSynchronize(c->stream);
   split_release(c);
   if (c->h_lines) cudaFreeHost(c->h_lines);

@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "split.h"
 
@@ -636,6 +637,35 @@ SplitShape shape_of(const Ctx* c) {
   return SplitShape{s, kDefaultW, tile_n(s)};
 }
 
+// Dynamic shared memory above 48 KB must be enabled per kernel, once, before
+// the first launch (and before any graph capture).
+template <int S>
+cudaError_t set_attributes() {
+  constexpr int BN1 = bn_for(S), BN2 = bn2_of(S), D1 = d1_of(S);
+  static std::once_flag once;
+  static cudaError_t status = cudaSuccess;
+  std::call_once(once, [] {
+    status = cudaFuncSetAttribute(k_split_gemm<S, BN1>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem_bytes(S, BN1));
+    if (status == cudaSuccess)
+      status = cudaFuncSetAttribute(k_split_gemm2<S, BN2, D1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem2_bytes(S, BN2));
+  });
+  return status;
+}
+
+cudaError_t kernel_attributes(int s) {
+  switch (s) {
+#define GI_S(SS) \
+  case SS: return set_attributes<SS>();
+    GI_S(2) GI_S(3) GI_S(4) GI_S(5) GI_S(6) GI_S(7) GI_S(8) GI_S(9) GI_S(10)
+#undef GI_S
+  }
+  return cudaErrorInvalidValue;
+}
+
 template <int S>
 cudaError_t launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const int32_t* ea,
                         const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
@@ -644,19 +674,8 @@ cudaError_t launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const int3
   constexpr int BN1 = bn_for(S), BN2 = bn2_of(S), D1 = d1_of(S);
   const int BN = one ? BN1 : BN2;
   const size_t sm = one ? smem_bytes(S, BN1) : smem2_bytes(S, BN2);
-  static bool attr1 = false, attr2 = false;
-  if (one && !attr1) {
-    cudaError_t e = cudaFuncSetAttribute(k_split_gemm<S, BN1>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    attr1 = true;
-  }
-  if (!one && !attr2) {
-    cudaError_t e = cudaFuncSetAttribute(k_split_gemm2<S, BN2, D1>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-    if (e != cudaSuccess) return e;
-    attr2 = true;
-  }
+  cudaError_t e = set_attributes<S>();
+  if (e != cudaSuccess) return e;
   const int nM = (M + kBM - 1) / kBM, nN = (Nc + BN - 1) / BN, nA = nM * batch;
   // row tiles per L2 group: their digit planes (128 x K x S bf16 each) within ~64 MB
   const size_t a_tile = (size_t)kBM * K * S * 2;
@@ -833,6 +852,62 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
   return r;
 }
 
+// The final-state vectors are fixed inputs: their digits are cut once and
+// kept with the block until it is replaced.  Serving workers share blocks, so
+// the cut happens under the model lock and the others wait on its event.
+static gi_status block_digits(Ctx* c, Block& fb, int K, bool wait) {
+  SplitState* S = state(c);
+  const int nvec = fb.nvec;
+  const int vpad = round_up(nvec, kBM);
+  gi_status g;
+  std::lock_guard<std::mutex> lk(c->mmu());
+  if (fb.digits_s != S->s || fb.digits_w != S->w) {
+    g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
+    if (g != GI_OK) return g;
+    g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
+    if (g != GI_OK) return g;
+    g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, fb.d_digits.p,
+                             fb.d_digit_exp.p, c->stream);
+              }),
+              "slice V");
+    if (g != GI_OK) return g;
+    if (!fb.digits_ev) {
+      g = check(c, cudaEventCreateWithFlags(&fb.digits_ev, cudaEventDisableTiming), "event");
+      if (g != GI_OK) return g;
+    }
+    g = check(c, cudaEventRecord(fb.digits_ev, c->stream), "event");
+    if (g != GI_OK) return g;
+    fb.digits_s = S->s;
+    fb.digits_w = S->w;
+  }
+  if (wait && fb.digits_ev) {
+    // inside a graph capture the cut precedes the capture on this stream
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    g = check(c, cudaStreamIsCapturing(c->stream, &cs), "capture status");
+    if (g != GI_OK) return g;
+    if (cs == cudaStreamCaptureStatusNone) {
+      g = check(c, cudaStreamWaitEvent(c->stream, fb.digits_ev, 0), "event wait");
+      if (g != GI_OK) return g;
+    }
+  }
+  return GI_OK;
+}
+
+gi_status split_reserve(Ctx* c, size_t max_elems, size_t max_cols,
+                        const std::vector<Block*>& finals) {
+  SplitState* S = state(c);
+  gi_status g = check(c, S->b_slices.reserve((size_t)S->s * max_elems), "B slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->b_exp.reserve(std::max<size_t>(max_cols, 1)), "B exponents");
+  if (g != GI_OK) return g;
+  for (Block* b : finals) {
+    g = block_digits(c, *b, b->ld, false);
+    if (g != GI_OK) return g;
+  }
+  return check(c, kernel_attributes(S->s), "kernel attributes");
+}
+
 gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol, double* T,
                            int ldt) {
   SplitState* S = state(c);
@@ -840,36 +915,8 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
   const int nvec = fb.nvec;
   const int vpad = round_up(nvec, kBM);
   gi_status g;
-  // the final-state vectors are fixed inputs: their digits are cut once and
-  // kept with the block until it is replaced.  Serving workers share blocks,
-  // so the cut happens under the model lock and the others wait on its event.
-  {
-    std::lock_guard<std::mutex> lk(c->mmu());
-    if (fb.digits_s != S->s || fb.digits_w != S->w) {
-      g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
-      if (g != GI_OK) return g;
-      g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
-      if (g != GI_OK) return g;
-      g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-                  return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, fb.d_digits.p,
-                               fb.d_digit_exp.p, c->stream);
-                }),
-                "slice V");
-      if (g != GI_OK) return g;
-      if (!fb.digits_ev) {
-        g = check(c, cudaEventCreateWithFlags(&fb.digits_ev, cudaEventDisableTiming), "event");
-        if (g != GI_OK) return g;
-      }
-      g = check(c, cudaEventRecord(fb.digits_ev, c->stream), "event");
-      if (g != GI_OK) return g;
-      fb.digits_s = S->s;
-      fb.digits_w = S->w;
-    }
-    if (fb.digits_ev) {
-      g = check(c, cudaStreamWaitEvent(c->stream, fb.digits_ev, 0), "event wait");
-      if (g != GI_OK) return g;
-    }
-  }
+  g = block_digits(c, fb, K, /*wait=*/true);
+  if (g != GI_OK) return g;
   g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "H slices");
   if (g != GI_OK) return g;
   g = check(c, S->b_exp.reserve(ncol), "H exponents");
@@ -891,6 +938,18 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
 }
 
 int split_digits(const Ctx* c) { return shape_of(c).s; }
+
+uint64_t split_identity(Ctx* c) {
+  const SplitState* S = state(c);
+  const SplitState* D = c->parent ? c->parent->split : S;
+  uint64_t h = 1469598103934665603ull;
+  for (uint64_t v : {(uint64_t)(uintptr_t)S->b_slices.p, (uint64_t)(uintptr_t)S->b_exp.p,
+                     (uint64_t)(uintptr_t)S->err.p, (uint64_t)(uintptr_t)D->mu_slices.p,
+                     (uint64_t)(uintptr_t)D->mu_exp.p, (uint64_t)S->s, (uint64_t)S->w,
+                     (uint64_t)S->Mpad, (uint64_t)one_pass()})
+    h = (h ^ v) * 1099511628211ull;
+  return h;
+}
 
 gi_status split_check(Ctx* c) {
   if (!c->split || !c->split->err.p) return GI_OK;

@@ -12,6 +12,15 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
                            int ldt);
 // Called once per run before the launch loop (sizes workspaces, slices the dipole).
 gi_status split_prepare(Ctx* c);
+// Before a launch sequence that must not allocate (graph capture): the B
+// operand workspace for GEMMs of up to max_elems = ncol x K elements and
+// max_cols columns, the digit planes of every final block in `finals`, and
+// the kernels' shared-memory attributes.
+gi_status split_reserve(Ctx* c, size_t max_elems, size_t max_cols,
+                        const std::vector<Block*>& finals);
+// Identity of the split state a captured launch sequence depends on (its
+// workspaces, the dipole digits and the digit shape).
+uint64_t split_identity(Ctx* c);
 // Digit planes per operand the next split-precision run will use.
 int split_digits(const Ctx* c);
 void split_invalidate(Ctx* c);  // the dipole changed: drop its cached slices

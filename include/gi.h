@@ -193,6 +193,10 @@ gi_status gi_set_block_device(gi_ctx* ctx, int J, int gamma, int nsize, int nvec
 /* Run ---------------------------------------------------------------------- */
 #define GI_RUN_LINES_ON_DEVICE 1 /* keep lines in device memory (no D2H) */
 #define GI_RUN_PHASE_TIMING 2    /* time every kernel with CUDA events (gi_stats) */
+#define GI_RUN_GRAPH 4           /* launch the job's kernels as one CUDA graph: captured on
+                                    the first run of a plan, replayed while the plan (blocks,
+                                    parameters, sizes, buffers) is unchanged; ignored with
+                                    GI_RUN_PHASE_TIMING */
 /* Computes every line of the job (all loaded J; |dJ| <= 1; the reference's
    filters).  *nlines receives the count. */
 gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);

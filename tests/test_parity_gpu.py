@@ -122,3 +122,37 @@ def test_flipped_dipole_layout(pkg, synth):
             got.append(np.sort(eng.lines(), order=["level_i", "level_f"]))
     assert len(got[0]) > 50
     assert np.array_equal(got[0]["S"], got[1]["S"])
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_graph_replay_matches_eager(pkg, synth, precision):
+    """GI_RUN_GRAPH: captured once, replayed while the plan is unchanged,
+    recaptured when it changes; every run equals the eager launch sequence."""
+    prob = synth.make_c3v(41, 30, [0, 1, 2, 3], nvec_max=10)
+
+    def lines(eng, **kw):
+        eng.run(**kw)
+        return np.sort(eng.lines(), order=["level_i", "level_f"]), eng.stats()
+
+    with pkg.Engine(0) as eng:
+        eng.load(prob, precision=precision)
+        lines(eng)  # the first run also cuts the final blocks' digit planes
+        eager, st_e = lines(eng)
+        for _ in range(3):  # capture, then two replays
+            g, st_g = lines(eng, graph=True)
+            assert np.array_equal(g, eager)
+            assert st_g["kernel_launches"] == st_e["kernel_launches"]
+        # a new threshold changes the epilogue's arguments: recapture
+        p = prob.params
+        p.thresh_intensity = 1e-24
+        eng.set_params(p, precision=precision)
+        eager2, _ = lines(eng)
+        g2, _ = lines(eng, graph=True)
+        assert len(eager2) < len(eager)
+        assert np.array_equal(g2, eager2)
+        # new vectors of the same shape (same device arrays): replay reads them
+        blk = prob.blocks[(2, 0)]
+        eng.set_block(2, 0, -blk.vecs, blk.energies, blk.quanta)
+        eager3, _ = lines(eng)
+        g3, _ = lines(eng, graph=True)
+        assert np.array_equal(g3, eager3)
