@@ -322,6 +322,10 @@ def main_ours(args):
 
     eng = pkg.Engine(local)
     eng.load(prob, precision=prec, split_slices=args.slices)
+    # the warm-up steps also tune the split GEMM launch configurations
+    import tempfile
+    tune_path = os.path.join(tempfile.gettempdir(), f"gi_tune_{os.getpid()}.txt")
+    eng.set_tuning(1, tune_path)
     # the engine's launches go to this stream, so its CUDA events bracket them
     stream = torch.cuda.Stream(device=local)
     eng.set_stream(stream.cuda_stream)
@@ -343,6 +347,13 @@ def main_ours(args):
 
     for _ in range(args.warmup):
         eng.run(lines_on_device=True, graph=True)
+    autotune = []
+    if os.path.exists(tune_path):
+        for line in open(tune_path).read().splitlines():
+            s_, nA, nb, K, kind, ga, ms = line.split()
+            autotune.append({"digits": int(s_), "row_tiles": int(nA), "cols_bucket": 2 ** int(nb),
+                             "K": int(K), "kernel": "one-pass" if kind == "0" else "two-pass",
+                             "l2_group_mb": int(ga), "ms": float(ms)})
     stats = []
 
     def one():
@@ -461,7 +472,7 @@ def main_ours(args):
                "lines_per_step": lines_pre, "lines_above_threshold_per_step": lines_post,
                "value_above_threshold": world * lines_post / dt,
                "gpu_launches": launches, "graph": "each step is one CUDA graph launch (captured "
-               "in warm-up, replayed)", "roofline": roof, "e2e": e2e,
+               "in warm-up, replayed)", "autotune": autotune, "roofline": roof, "e2e": e2e,
                "fp64_path": fp64, "accuracy": accuracy, "serving": serving,
                "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:

@@ -130,6 +130,7 @@ def lib():
         L.gi_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_size_t]
         L.gi_destroy.argtypes = [C.c_void_p]
         L.gi_set_stream.argtypes = [C.c_void_p, C.c_void_p]
+        L.gi_set_tuning.argtypes = [C.c_void_p, C.c_int, C.c_char_p]
         L.gi_last_error.restype = C.c_char_p
         L.gi_last_error.argtypes = [C.c_void_p]
         L.gi_status_string.restype = C.c_char_p
@@ -258,6 +259,11 @@ class Engine:
         """Order the engine's device work on a caller's cudaStream_t (an int
         handle, e.g. torch.cuda.Stream().cuda_stream); None: its own stream."""
         self._ck(self._L.gi_set_stream(self._h, C.c_void_p(stream or None)))
+
+    def set_tuning(self, mode: int, path: Optional[str] = None):
+        """Split GEMM autotuner: mode 1 times the candidate launch configurations
+        on the first GEMM of each new shape class; path keeps the table on disk."""
+        self._ck(self._L.gi_set_tuning(self._h, mode, path.encode() if path else None))
 
     def set_symmetry(self, sym_type: int):
         self._ck(self._L.gi_set_symmetry(self._h, sym_type))

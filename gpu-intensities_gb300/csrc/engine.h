@@ -145,6 +145,8 @@ struct JobSel {
 
 struct Ctx {
   SplitState* split = nullptr;
+  int tune_mode = 0;          // split GEMM autotuner (gi_set_tuning)
+  std::string tune_path;
   Ctx* parent = nullptr;      // a serving worker shares its parent's model state
   Server* server = nullptr;
   std::mutex model_mu;        // guards lazily derived shared state (digits)
@@ -204,7 +206,7 @@ struct Ctx {
   // CUDA graph of the last captured launch sequence (GI_RUN_GRAPH) and the
   // plan it was captured for
   cudaGraphExec_t gexec = nullptr;
-  uint64_t gsig = 0;
+  uint64_t gsig = 0, gpending = 0;
   gi_stats gstats{};
   int64_t graph_replays = 0;
 

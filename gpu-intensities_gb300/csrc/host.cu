@@ -747,6 +747,13 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   };
 
   GI_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  // With the autotuner on, a new plan first runs eagerly (tuning needs timed,
+  // synchronised launches); the next run of the same plan is captured.
+  bool capture = use_graph;
+  if (use_graph && c->tune_mode > 0 && !(c->gexec && c->gsig == sig) && c->gpending != sig) {
+    capture = false;
+    c->gpending = sig;
+  }
   if (use_graph && c->gexec && c->gsig == sig) {
     // replay: the captured sequence with this run's table contents
     GI_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
@@ -759,7 +766,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     by_corr = g.bytes_correlate;
     npairs_checked = g.npairs_checked;
     c->graph_replays++;
-  } else if (use_graph) {
+  } else if (capture) {
     if (c->gexec) cudaGraphExecDestroy(c->gexec);
     c->gexec = nullptr;
     c->gsig = 0;
@@ -893,6 +900,15 @@ gi_status gi_destroy(gi_ctx* h) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->own_stream) cudaStreamDestroy(c->own_stream);
   delete c;
+  return GI_OK;
+}
+
+gi_status gi_set_tuning(gi_ctx* h, int mode, const char* path) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || mode < 0 || mode > 1) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_set_tuning while serving");
+  c->tune_mode = mode;
+  c->tune_path = path ? path : "";
   return GI_OK;
 }
 

@@ -268,6 +268,8 @@ static Ctx* make_worker(Ctx* c, size_t slot_ws) {
   w->degen = c->degen;
   w->N = c->N;
   w->Kp = c->Kp;
+  w->tune_mode = c->tune_mode;
+  w->tune_path = c->tune_path;
   return w;
 }
 

@@ -29,7 +29,10 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <string>
+#include <tuple>
 
 #include "split.h"
 
@@ -608,15 +611,13 @@ bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int bo
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-// GI_SPLIT_KERNEL=1 selects the one-pass kernel (for comparison runs).
-bool one_pass() {
-  static int v = -1;
-  if (v < 0) {
-    const char* e = getenv("GI_SPLIT_KERNEL");
-    v = (e && e[0] == '1') ? 1 : 0;
-  }
-  return v == 1;
-}
+// One launch configuration of the split GEMM: the kernel (one pass with all
+// diagonals in tensor memory, or two passes with wider tiles) and the L2
+// raster group (row tiles whose digit planes share about ga_mb MB of L2).
+struct GemmConfig {
+  int kind = 1;  // 0: k_split_gemm (one pass), 1: k_split_gemm2 (two passes)
+  int ga_mb = 64;
+};
 
 // Two-pass geometry: diagonals [0, S/2) then [S/2, S), each pass's accumulators
 // within the 512 tensor-memory columns, at most 128 wide.
@@ -629,12 +630,12 @@ size_t smem2_bytes(int s, int bn) {
   return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;  // one CTA per SM
 }
 
-int tile_n(int s) { return one_pass() ? bn_for(s) : bn2_of(s); }
+int tile_n(int s, int kind) { return kind == 0 ? bn_for(s) : bn2_of(s); }
 
 SplitShape shape_of(const Ctx* c) {
   int s = c->params.split_slices > 0 ? c->params.split_slices : kDefaultSlices;
   s = std::min(std::max(s, 2), kMaxSlices);
-  return SplitShape{s, kDefaultW, tile_n(s)};
+  return SplitShape{s, kDefaultW, tile_n(s, 1)};
 }
 
 // Dynamic shared memory above 48 KB must be enabled per kernel, once, before
@@ -667,19 +668,20 @@ cudaError_t kernel_attributes(int s) {
 }
 
 template <int S>
-cudaError_t launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const int32_t* ea,
-                        const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
-                        int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
-  const bool one = one_pass();
+cudaError_t launch_gemm(const GemmConfig& cfg, const CUtensorMap& tA, const CUtensorMap& tB,
+                        const int32_t* ea, const int32_t* eb, double* C, int ldc, size_t strideC,
+                        int M, int Mpad, int Nc, int K, int batch, int w, int* err,
+                        cudaStream_t st) {
+  const bool one = cfg.kind == 0;
   constexpr int BN1 = bn_for(S), BN2 = bn2_of(S), D1 = d1_of(S);
   const int BN = one ? BN1 : BN2;
   const size_t sm = one ? smem_bytes(S, BN1) : smem2_bytes(S, BN2);
   cudaError_t e = set_attributes<S>();
   if (e != cudaSuccess) return e;
   const int nM = (M + kBM - 1) / kBM, nN = (Nc + BN - 1) / BN, nA = nM * batch;
-  // row tiles per L2 group: their digit planes (128 x K x S bf16 each) within ~64 MB
+  // row tiles per L2 group: their digit planes (128 x K x S bf16 each) within ga_mb MB
   const size_t a_tile = (size_t)kBM * K * S * 2;
-  const int GA = std::max(1, std::min(nA, (int)(((size_t)64 << 20) / a_tile)));
+  const int GA = std::max(1, std::min(nA, (int)(((size_t)cfg.ga_mb << 20) / a_tile)));
   if (one)
     k_split_gemm<S, BN1><<<nA * nN, kThreads, sm, st>>>(
         tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
@@ -689,12 +691,15 @@ cudaError_t launch_gemm(const CUtensorMap& tA, const CUtensorMap& tB, const int3
   return cudaGetLastError();
 }
 
-cudaError_t launch_gemm_s(int s, const CUtensorMap& tA, const CUtensorMap& tB, const int32_t* ea,
-                          const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
-                          int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
+cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const CUtensorMap& tA,
+                          const CUtensorMap& tB, const int32_t* ea, const int32_t* eb, double* C,
+                          int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int batch,
+                          int w, int* err, cudaStream_t st) {
   switch (s) {
-#define GI_S(SS) \
-  case SS: return launch_gemm<SS>(tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, err, st);
+#define GI_S(SS)                                                                          \
+  case SS:                                                                                \
+    return launch_gemm<SS>(cfg, tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, \
+                           err, st);
     GI_S(2) GI_S(3) GI_S(4) GI_S(5) GI_S(6) GI_S(7) GI_S(8) GI_S(9) GI_S(10)
 #undef GI_S
   }
@@ -808,21 +813,122 @@ gi_status split_prepare(Ctx* c) {
   return GI_OK;
 }
 
+// ------------------------------------------------------------------ autotuner
+// The launch configuration is chosen per GEMM shape class (digits, row tiles,
+// power-of-two column bucket, K).  With tuning on, the first GEMM of a class
+// times every candidate on its real operands with CUDA events and keeps the
+// fastest; the table lives for the process and, given a path, in a text file
+// ("s nA nbucket K kind ga_mb ms" per line).
+struct TuneKey {
+  int s, nA, nbucket, K;
+  bool operator<(const TuneKey& o) const {
+    return std::tie(s, nA, nbucket, K) < std::tie(o.s, o.nA, o.nbucket, o.K);
+  }
+};
+struct TuneEntry {
+  GemmConfig cfg;
+  float ms;
+};
+struct Tuner {
+  std::mutex mu;
+  std::map<TuneKey, TuneEntry> table;
+  std::string loaded;
+  uint64_t version = 0;  // bumped on every change (captured graphs depend on it)
+};
+static Tuner& tuner() {
+  static Tuner t;
+  return t;
+}
+static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16}, {0, 64}, {0, 32}};
+
+static void tune_load(Tuner& t, const std::string& path) {
+  t.loaded = path;
+  FILE* f = fopen(path.c_str(), "r");
+  if (!f) return;
+  TuneKey k;
+  TuneEntry e;
+  while (fscanf(f, "%d %d %d %d %d %d %f", &k.s, &k.nA, &k.nbucket, &k.K, &e.cfg.kind,
+                &e.cfg.ga_mb, &e.ms) == 7)
+    if ((e.cfg.kind == 0 || e.cfg.kind == 1) && e.cfg.ga_mb > 0) t.table[k] = e;
+  fclose(f);
+  t.version++;
+}
+
+static void tune_save(const Tuner& t, const std::string& path) {
+  const std::string tmp = path + ".tmp";
+  FILE* f = fopen(tmp.c_str(), "w");
+  if (!f) return;
+  for (const auto& kv : t.table)
+    fprintf(f, "%d %d %d %d %d %d %.4f\n", kv.first.s, kv.first.nA, kv.first.nbucket, kv.first.K,
+            kv.second.cfg.kind, kv.second.cfg.ga_mb, kv.second.ms);
+  fclose(f);
+  rename(tmp.c_str(), path.c_str());
+}
+
+static int col_bucket(int n) {
+  int b = 0;
+  while (b < 30 && (2 << b) <= n) b++;
+  return b;
+}
+
 static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const int32_t* ea,
                       int Mpad, const uint16_t* Bslices, int Brows, const int32_t* eb,
                       double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch) {
   SplitState* S = state(c);
-  CUtensorMap tA, tB;
-  const int bn = tile_n(S->s);
-  const int planes = one_pass() ? S->s : 1;  // the two-pass kernel loads plane by plane
-  if (!make_map(&tA, Aslices, K, Arows_total, S->s, kBM, planes) ||
-      !make_map(&tB, Bslices, K, Brows, S->s, bn, planes)) {
-    c->err = "split precision: cuTensorMapEncodeTiled failed";
-    return GI_ERR_CUDA;
+  auto run = [&](const GemmConfig& g) -> cudaError_t {
+    CUtensorMap tA, tB;
+    const int planes = g.kind == 0 ? S->s : 1;  // the two-pass kernel loads plane by plane
+    if (!make_map(&tA, Aslices, K, Arows_total, S->s, kBM, planes) ||
+        !make_map(&tB, Bslices, K, Brows, S->s, tile_n(S->s, g.kind), planes))
+      return cudaErrorInvalidValue;
+    return launch_gemm_s(S->s, g, tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, S->w,
+                         S->err.p, c->stream);
+  };
+  const TuneKey key{S->s, ((M + kBM - 1) / kBM) * batch, col_bucket(Nc), K};
+  GemmConfig cfg;
+  bool known = false;
+  Tuner& t = tuner();
+  {
+    std::lock_guard<std::mutex> lk(t.mu);
+    if (!c->tune_path.empty() && t.loaded != c->tune_path) tune_load(t, c->tune_path);
+    auto it = t.table.find(key);
+    if (it != t.table.end()) {
+      cfg = it->second.cfg;
+      known = true;
+    }
   }
-  return check(c, launch_gemm_s(S->s, tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch,
-                                S->w, S->err.p, c->stream),
-               "split GEMM launch");
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (!known && c->tune_mode > 0 && cudaStreamIsCapturing(c->stream, &cs) == cudaSuccess &&
+      cs == cudaStreamCaptureStatusNone) {
+    cudaEvent_t a = nullptr, b = nullptr;
+    gi_status g = check(c, cudaEventCreate(&a), "tuning event");
+    if (g == GI_OK) g = check(c, cudaEventCreate(&b), "tuning event");
+    if (g == GI_OK) g = check(c, run(cfg), "tuning warm-up");  // the first launch of a shape
+    float best = 1e30f;
+    GemmConfig best_cfg = cfg;
+    for (const GemmConfig& cand : kCandidates) {
+      if (g != GI_OK) break;
+      g = check(c, cudaEventRecord(a, c->stream), "tuning event");
+      if (g == GI_OK) g = check(c, run(cand), "tuning launch");
+      if (g == GI_OK) g = check(c, cudaEventRecord(b, c->stream), "tuning event");
+      if (g == GI_OK) g = check(c, cudaEventSynchronize(b), "tuning sync");
+      float ms = 0.f;
+      if (g == GI_OK) g = check(c, cudaEventElapsedTime(&ms, a, b), "tuning time");
+      if (g == GI_OK && ms < best) {
+        best = ms;
+        best_cfg = cand;
+      }
+    }
+    if (a) cudaEventDestroy(a);
+    if (b) cudaEventDestroy(b);
+    if (g != GI_OK) return g;
+    std::lock_guard<std::mutex> lk(t.mu);
+    t.table[key] = TuneEntry{best_cfg, best};
+    t.version++;
+    if (!c->tune_path.empty()) tune_save(t, c->tune_path);
+    cfg = best_cfg;
+  }
+  return check(c, run(cfg), "split GEMM launch");
 }
 
 gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zstride,
@@ -946,7 +1052,7 @@ uint64_t split_identity(Ctx* c) {
   for (uint64_t v : {(uint64_t)(uintptr_t)S->b_slices.p, (uint64_t)(uintptr_t)S->b_exp.p,
                      (uint64_t)(uintptr_t)S->err.p, (uint64_t)(uintptr_t)D->mu_slices.p,
                      (uint64_t)(uintptr_t)D->mu_exp.p, (uint64_t)S->s, (uint64_t)S->w,
-                     (uint64_t)S->Mpad, (uint64_t)one_pass()})
+                     (uint64_t)S->Mpad, tuner().version})
     h = (h ^ v) * 1099511628211ull;
   return h;
 }

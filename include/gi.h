@@ -149,6 +149,16 @@ gi_status gi_destroy(gi_ctx* ctx);
  * No counterpart in the reference, whose kernels run on its own streams
  * (cuda_host.cu:980-992). */
 gi_status gi_set_stream(gi_ctx* ctx, void* stream);
+/* Autotuner of the split-precision GEMM launch configuration (one- or
+ * two-pass kernel, L2 raster group) per shape class (digits, row tiles,
+ * power-of-two column bucket, K).  mode 0 (default): configurations from the
+ * table, a fixed default for classes not in it; mode 1: the first GEMM of a
+ * class not in the table times every candidate on its operands (CUDA events)
+ * and keeps the fastest.  path (optional, may be NULL): a text file the table
+ * is read from and written to.  The table is shared by all contexts of the
+ * process.  Tuning is skipped inside a CUDA-graph capture.  No counterpart in
+ * the reference (fixed launch shapes, dipole_kernals.cu:162-227). */
+gi_status gi_set_tuning(gi_ctx* ctx, int mode, const char* path);
 const char* gi_last_error(const gi_ctx* ctx);
 const char* gi_status_string(gi_status s);
 

@@ -42,3 +42,22 @@ def test_split_slice_counts(pkg, synth, oracle, slices):
     tol = {6: 1e-6, 9: 1e-10, 10: 1e-10}[slices]
     res = compare(got, ref, rtol_S=tol, norm_tol=tol / 100)
     print(slices, res)
+
+
+def test_autotuner_table_and_results(pkg, synth, tmp_path):
+    """gi_set_tuning(1, path): every GEMM shape class gets a timed choice in the
+    table file, and the tuned run's lines agree with the default ones."""
+    prob = synth.make_c2v(51, 64, [0, 1, 2, 3], nvec_max=24)
+    path = str(tmp_path / "tune.txt")
+    with pkg.Engine(0) as eng:
+        eng.load(prob, precision=1)
+        eng.run()
+        ref = np.sort(eng.lines(), order=["level_i", "level_f"])
+        eng.set_tuning(1, path)
+        eng.run()
+        got = np.sort(eng.lines(), order=["level_i", "level_f"])
+    rows = [l.split() for l in open(path).read().splitlines()]
+    assert len(rows) >= 2 and all(len(r) == 7 for r in rows)
+    assert all(r[4] in ("0", "1") for r in rows)
+    assert np.array_equal(got[["level_i", "level_f"]], ref[["level_i", "level_f"]])
+    assert np.allclose(got["S"], ref["S"], rtol=1e-12, atol=0)
