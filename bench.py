@@ -352,7 +352,8 @@ def main_ours(args):
         for line in open(tune_path).read().splitlines():
             s_, nA, nb, K, kind, ga, ms = line.split()
             autotune.append({"digits": int(s_), "row_tiles": int(nA), "cols_bucket": 2 ** int(nb),
-                             "K": int(K), "kernel": "one-pass" if kind == "0" else "two-pass",
+                             "K": int(K), "kernel": {"0": "one-pass", "1": "two-pass (diagonals split at s/2)",
+                                        "2": "two-pass (split at s - s/2)"}[kind],
                              "l2_group_mb": int(ga), "ms": float(ms)})
     stats = []
 

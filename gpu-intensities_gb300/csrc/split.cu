@@ -615,13 +615,16 @@ bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int bo
 // diagonals in tensor memory, or two passes with wider tiles) and the L2
 // raster group (row tiles whose digit planes share about ga_mb MB of L2).
 struct GemmConfig {
-  int kind = 1;  // 0: k_split_gemm (one pass), 1: k_split_gemm2 (two passes)
+  int kind = 1;  // 0: k_split_gemm (one pass); 1, 2: k_split_gemm2 (two passes,
+                 // diagonals split at s/2 or s - s/2)
   int ga_mb = 64;
 };
 
 // Two-pass geometry: diagonals [0, S/2) then [S/2, S), each pass's accumulators
 // within the 512 tensor-memory columns, at most 128 wide.
 __host__ __device__ constexpr int d1_of(int s) { return s / 2; }
+// the other split point for odd s: the larger half of the diagonals first
+__host__ __device__ constexpr int d1b_of(int s) { return s - s / 2; }
 __host__ __device__ constexpr int bn2_of(int s) {
   return ((512 / (s - s / 2)) / 16 * 16) > 128 ? 128 : ((512 / (s - s / 2)) / 16 * 16);
 }
@@ -631,6 +634,7 @@ size_t smem2_bytes(int s, int bn) {
 }
 
 int tile_n(int s, int kind) { return kind == 0 ? bn_for(s) : bn2_of(s); }
+bool kind_valid(int s, int kind) { return kind == 0 || kind == 1 || (kind == 2 && (s & 1)); }
 
 SplitShape shape_of(const Ctx* c) {
   int s = c->params.split_slices > 0 ? c->params.split_slices : kDefaultSlices;
@@ -651,6 +655,10 @@ cudaError_t set_attributes() {
                                   (int)smem_bytes(S, BN1));
     if (status == cudaSuccess)
       status = cudaFuncSetAttribute(k_split_gemm2<S, BN2, D1>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem2_bytes(S, BN2));
+    if (status == cudaSuccess && d1b_of(S) != D1)
+      status = cudaFuncSetAttribute(k_split_gemm2<S, BN2, d1b_of(S)>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem2_bytes(S, BN2));
   });
@@ -684,6 +692,9 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const CUtensorMap& tA, const CUte
   const int GA = std::max(1, std::min(nA, (int)(((size_t)cfg.ga_mb << 20) / a_tile)));
   if (one)
     k_split_gemm<S, BN1><<<nA * nN, kThreads, sm, st>>>(
+        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
+  else if (cfg.kind == 2 && d1b_of(S) != D1)
+    k_split_gemm2<S, BN2, d1b_of(S)><<<nA * nN, kThreads, sm, st>>>(
         tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
   else
     k_split_gemm2<S, BN2, D1><<<nA * nN, kThreads, sm, st>>>(
@@ -839,7 +850,8 @@ static Tuner& tuner() {
   static Tuner t;
   return t;
 }
-static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16}, {0, 64}, {0, 32}};
+static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16},
+                                         {2, 64}, {2, 32}, {0, 64}, {0, 32}};
 
 static void tune_load(Tuner& t, const std::string& path) {
   t.loaded = path;
@@ -849,7 +861,7 @@ static void tune_load(Tuner& t, const std::string& path) {
   TuneEntry e;
   while (fscanf(f, "%d %d %d %d %d %d %f", &k.s, &k.nA, &k.nbucket, &k.K, &e.cfg.kind,
                 &e.cfg.ga_mb, &e.ms) == 7)
-    if ((e.cfg.kind == 0 || e.cfg.kind == 1) && e.cfg.ga_mb > 0) t.table[k] = e;
+    if (kind_valid(k.s, e.cfg.kind) && e.cfg.ga_mb > 0) t.table[k] = e;
   fclose(f);
   t.version++;
 }
@@ -887,6 +899,12 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
   const TuneKey key{S->s, ((M + kBM - 1) / kBM) * batch, col_bucket(Nc), K};
   GemmConfig cfg;
   bool known = false;
+  // GI_SPLIT_FORCE="kind:ga_mb" pins one configuration (parity tests of every kernel)
+  if (const char* f = getenv("GI_SPLIT_FORCE")) {
+    GemmConfig g;
+    if (sscanf(f, "%d:%d", &g.kind, &g.ga_mb) == 2 && kind_valid(S->s, g.kind) && g.ga_mb > 0)
+      return check(c, run(g), "split GEMM launch");
+  }
   Tuner& t = tuner();
   {
     std::lock_guard<std::mutex> lk(t.mu);
@@ -908,6 +926,7 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
     GemmConfig best_cfg = cfg;
     for (const GemmConfig& cand : kCandidates) {
       if (g != GI_OK) break;
+      if (!kind_valid(S->s, cand.kind)) continue;
       g = check(c, cudaEventRecord(a, c->stream), "tuning event");
       if (g == GI_OK) g = check(c, run(cand), "tuning launch");
       if (g == GI_OK) g = check(c, cudaEventRecord(b, c->stream), "tuning event");
