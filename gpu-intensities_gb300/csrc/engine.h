@@ -108,7 +108,7 @@ struct Block {
   // completion on the stream that cut them
   DevArray<uint16_t> d_digits;
   DevArray<int32_t> d_digit_exp;
-  int digits_s = 0, digits_w = 0;
+  int digits_s = 0, digits_w = 0, digits_layout = -1;
   cudaEvent_t digits_ev = nullptr;
   // residency under a serving budget: an evicted block keeps its vectors in
   // pinned host memory and has no device arrays

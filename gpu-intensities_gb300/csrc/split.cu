@@ -99,6 +99,10 @@ __device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag
     if (sleep_ns) __nanosleep(sleep_ns);
     if ((it & 63) == 0) {
       if (*abort_flag) return false;
+      if (*reinterpret_cast<volatile int*>(err)) {  // another CTA timed out: stop waiting
+        *abort_flag = 1;
+        return false;
+      }
       const uint64_t t = gtimer();
       if (t0 == 0) {
         t0 = t;
@@ -118,6 +122,24 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       "l"(reinterpret_cast<uint64_t>(map)), "r"(sptr(bar)), "r"(c0), "r"(c1), "r"(c2)
       : "memory");
 }
+// The same load delivered to every CTA of `mask` in the cluster (same smem
+// offset, complete_tx on the mbarrier at the same offset in each of them).
+__device__ __forceinline__ void tma_load_3d_mc(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                               int c0, int c1, int c2, uint16_t mask) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      ".multicast::cluster [%0], [%1, {%3, %4, %5}], [%2], %6;\n" ::"r"(sptr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(sptr(bar)), "r"(c0), "r"(c1), "r"(c2), "h"(mask)
+      : "memory");
+}
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release;\nbarrier.cluster.wait.acquire;\n" ::: "memory");
+}
 // Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 32
 // bytes (16 elements) with the 32-byte swizzle: 8-row groups 256 bytes apart.
 __device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr) {
@@ -127,6 +149,19 @@ __device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr) {
   d |= (uint64_t)((256 >> 4) & 0x3FFF) << 32;      // stride byte offset: 8 rows x 32 B
   d |= (uint64_t)1 << 46;                          // descriptor version (tcgen05)
   d |= (uint64_t)6 << 61;                          // SWIZZLE_32B
+  return d;
+}
+// The same for 128-byte rows with the 128-byte swizzle (8-row groups 1024
+// bytes apart).  In the grouped digit layout one such row holds the 16-element
+// K slice of four digit planes; the descriptor of plane p of a group starts
+// 32 p bytes into the row (the K-step offset inside the swizzle atom).
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr >> 4) & 0x3FFF);          // start address
+  d |= (uint64_t)1 << 16;                          // leading byte offset (unused here)
+  d |= (uint64_t)((1024 >> 4) & 0x3FFF) << 32;     // stride byte offset: 8 rows x 128 B
+  d |= (uint64_t)1 << 46;                          // descriptor version (tcgen05)
+  d |= (uint64_t)2 << 61;                          // SWIZZLE_128B
   return d;
 }
 // Instruction descriptor: kind::f16, bf16 x bf16 -> f32, K-major A and B.
@@ -148,6 +183,15 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
           sptr(bar))
+      : "memory");
+}
+// Arrives on the mbarrier at this offset in every CTA of `mask` once the
+// MMAs issued so far have completed.
+__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
+      " [%0], %1;\n" ::"r"(sptr(bar)),
+      "h"(mask)
       : "memory");
 }
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
@@ -330,6 +374,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 // int64) into FP64 in C; pass 1's epilogue adds its part.  Pass 0 loads only
 // the digit planes it uses (p, q < D1).
 constexpr int kStages2 = 3;
+// Stage of the grouped layout: s/4 four-plane groups of 128-byte rows and s%4
+// planes of 32-byte rows, for 128 A rows and bn B rows; 1024-byte aligned so
+// every 128-byte-swizzle tile starts on a swizzle period.
+__host__ __device__ constexpr uint32_t stage_bytes_g(int s, int bn) {
+  return ((uint32_t)((s / 4) * (kBM + bn) * 128 + (s % 4) * (kBM + bn) * 32) + 1023u) / 1024u *
+         1024u;
+}
 
 template <int S, int BN, int D1>
 __global__ void __launch_bounds__(kThreads, 1)
@@ -499,6 +550,395 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
 }
 
+
+// Cluster variant of the two-pass kernel.  A cluster of CM x CN CTAs computes
+// CM row tiles x CN column tiles; the CN CTAs of one row tile share its A digit
+// planes and the CM CTAs of one column tile share its B planes.  Each plane is
+// fetched from L2 once per cluster by one of its sharers and multicast into
+// every sharer's shared memory, which divides the L2-to-SM traffic per tile by
+// up to CN (A) and CM (B).  A CTA may refill a stage only when every CTA it
+// sends to has released it, so each CTA's MMA commit arrives on the "empty"
+// barrier of all CTAs that share its row or its column tile.  Tiles past the
+// edge still take part in the loads and releases (their TMA boxes read zeros)
+// and skip the stores.
+template <int S, int BN, int D1, int CM, int CN>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_split_gemm3(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
+                  int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
+                  int nN, int GAc, int* err) {
+  static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
+  static_assert(CM * CN >= 2 && CM * CN <= 8, "portable cluster size");
+  constexpr int CS = CM * CN;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t kAplane = kBM * kBK * 2, kBplane = BN * kBK * 2;
+  constexpr uint32_t kStage = S * (kAplane + kBplane);
+  constexpr int ST = kStages2;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
+  uint64_t* empty = full + ST;
+  uint64_t* accf = empty + ST;
+  uint64_t* tfree = accf + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tfree + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int rank = (int)cluster_rank();
+  const int rm = rank % CM, rn = rank / CM;
+  const int q = blockIdx.x / CS;
+  const int nAc = (nA + CM - 1) / CM, nNc = (nN + CN - 1) / CN;
+  const int grp = q / (GAc * nNc);
+  const int r = q - grp * GAc * nNc;
+  const int gsz = min(GAc, nAc - grp * GAc);
+  const int ai = (grp * GAc + r % gsz) * CM + rm;
+  const int nt = (r / gsz) * CN + rn;
+  const bool valid = ai < nA && nt < nN;
+  const int n0 = nt * BN, m0 = (ai % nM) * kBM, z = ai / nM;
+  const int arow = z * Mpad + m0;  // past the last row tile: rows beyond the map read zeros
+  const int nk = K / kBK;
+  uint16_t maskA = 0, maskB = 0;  // CTAs sharing my row tile / my column tile
+  for (int j = 0; j < CN; ++j) maskA |= (uint16_t)(1u << (rm + CM * j));
+  for (int i = 0; i < CM; ++i) maskB |= (uint16_t)(1u << (i + CM * rn));
+  const uint16_t mask_rel = maskA | maskB;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ST; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], CM + CN - 1);
+    }
+    mbar_init(&accf[0], 1);
+    mbar_init(&accf[1], 1);
+    mbar_init(tfree, 128);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     sptr(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  cluster_sync_all();  // every CTA's barriers exist before any peer signals them
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer: this CTA's share of the planes, multicast
+      for (int it = 0; it < 2 * nk; ++it) {
+        const int pass = it >= nk, kb = it - pass * nk, st = it % ST;
+        const int np = pass ? S : D1;
+        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 11, 64))
+          break;
+        unsigned char* sa = smem + st * kStage;
+        mbar_expect_tx(&full[st], np * (kAplane + kBplane));  // everything landing here
+        for (int p = 0; p < np; ++p) {
+          if (p % CN == rn)
+            tma_load_3d_mc(sa + p * kAplane, &tmA, &full[st], kb * kBK, arow, p, maskA);
+          if (p % CM == rm)
+            tma_load_3d_mc(sa + S * kAplane + p * kBplane, &tmB, &full[st], kb * kBK, n0, p,
+                           maskB);
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = idesc_bf16(kBM, BN);
+      bool ok = true;
+      int last = 0;
+      for (int pass = 0; pass < 2 && ok; ++pass) {
+        last = pass;
+        if (pass == 1) {
+          ok = mbar_wait(tfree, 0, abort_flag, err, 14);
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          if (!ok) break;
+        }
+        for (int kb = 0; kb < nk; ++kb) {
+          const int it = pass * nk + kb, st = it % ST;
+          if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 12)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t a0 = sptr(smem + st * kStage);
+          const uint32_t b0 = a0 + S * kAplane;
+          if (pass == 0) {
+#pragma unroll
+            for (int d = 0; d < D1; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + d * BN, sdesc_sw32(a0 + p * kAplane),
+                         sdesc_sw32(b0 + (d - p) * kBplane), idesc, (kb > 0 || p > 0) ? 1u : 0u);
+          } else {
+#pragma unroll
+            for (int d = D1; d < S; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + (d - D1) * BN, sdesc_sw32(a0 + p * kAplane),
+                         sdesc_sw32(b0 + (d - p) * kBplane), idesc, (kb > 0 || p > 0) ? 1u : 0u);
+          }
+          mma_commit_mc(&empty[st], mask_rel);  // the stage is free here and at every sender
+        }
+        mma_commit(&accf[pass]);
+      }
+      if (*abort_flag) {
+        uint64_t t0 = gtimer();
+        while (!mbar_try(&accf[last], 0) && gtimer() - t0 < 1000000000ull) {
+        }
+      }
+    }
+  } else {
+    const int q4 = warp & 3;
+    const int m = m0 + q4 * 32 + lane;
+    const bool row_ok = valid && m < M;
+    const int emr = row_ok ? ea[z * Mpad + m] : 0;
+    double* Cz = C + (size_t)(valid ? z : 0) * strideC;
+    for (int pass = 0; pass < 2; ++pass) {
+      const bool ok = mbar_wait(&accf[pass], 0, abort_flag, err, 13, 1000);
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (!ok) break;
+      const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        long long v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0;
+        for (int d = d0; d < d1; ++d) {
+          float f[16];
+          tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (d - d0) * BN + c0, f);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = (v[j] << w) + (long long)__float2int_rn(f[j]);
+        }
+        if (row_ok) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < Nc) {
+              const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
+              double* dst = Cz + (size_t)n * ldc + m;
+              const double part = ldexp((double)v[j], E);
+              *dst = pass ? *dst + part : part;
+            }
+          }
+        }
+      }
+      if (pass == 0) {
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (*abort_flag) {
+    // copies a peer issued into this CTA before the abort land within
+    // microseconds; give them 20 ms before the shared memory goes away
+    const uint64_t t0 = gtimer();
+    while (gtimer() - t0 < 20000000ull) {
+    }
+  }
+  cluster_sync_all();  // no peer signals or writes this CTA after it exits
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
+
+// Grouped-layout two-pass kernel.  TMA moves 32-byte rows at about a third
+// of the rate of 128-byte rows into shared memory (16.7 vs 48.3 B/clk/SM
+// measured on GB300), and the digit GEMM needs all s planes of a 16-wide K
+// slice per stage.  In the grouped layout every 128-byte row holds that K slice
+// for four planes (planes 4g..4g+3), so a stage is NQ = s/4 boxes of 128-byte
+// rows plus NT = s%4 boxes of 32-byte rows per operand, instead of s boxes of
+// 32-byte rows.  D1 = S runs the whole GEMM in one pass (all S accumulators in
+// tensor memory, BN <= 512/S).
+template <int S, int BN, int D1>
+__global__ void __launch_bounds__(kThreads, 1)
+    k_split_gemm_g(const __grid_constant__ CUtensorMap tmAq, const __grid_constant__ CUtensorMap tmAt,
+                   const __grid_constant__ CUtensorMap tmBq, const __grid_constant__ CUtensorMap tmBt,
+                   const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
+                   int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
+                   int nN, int GA, int* err) {
+  constexpr int NQ = S / 4, NT = S % 4;
+  constexpr int NPASS = D1 < S ? 2 : 1;
+  static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
+  static_assert((BN * 128) % 1024 == 0, "128-byte-swizzle tiles stay 1024-byte aligned");
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t kAq = kBM * 128, kAt = kBM * 32, kBq = BN * 128, kBt = BN * 32;
+  constexpr uint32_t kAbytes = NQ * kAq + NT * kAt;
+  constexpr uint32_t kStage = stage_bytes_g(S, BN);  // rounded up to 1024 bytes
+  static_assert(kAbytes % 1024 == 0 && kStage >= kAbytes + NQ * kBq + NT * kBt, "stage layout");
+  constexpr int ST = kStages2;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
+  uint64_t* empty = full + ST;
+  uint64_t* accf = empty + ST;
+  uint64_t* tfree = accf + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tfree + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int t = blockIdx.x;
+  const int grp = t / (GA * nN);
+  const int r = t - grp * GA * nN;
+  const int gsz = min(GA, nA - grp * GA);
+  const int ai = grp * GA + r % gsz;
+  const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
+  const int nk = K / kBK;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ST; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&accf[0], 1);
+    mbar_init(&accf[1], 1);
+    mbar_init(tfree, 128);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     sptr(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer: both passes, one continuous stage ring
+      int issued = 0;
+      for (int it = 0; it < NPASS * nk; ++it) {
+        const int pass = it >= nk, kb = it - pass * nk, st = it % ST;
+        const int np = pass ? S : D1;
+        const int gq = min(NQ, (np + 3) / 4), tq = max(0, np - 4 * NQ);
+        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 21, 64))
+          break;
+        unsigned char* sa = smem + st * kStage;
+        unsigned char* sb = sa + kAbytes;
+        mbar_expect_tx(&full[st], gq * (kAq + kBq) + tq * (kAt + kBt));
+        for (int g = 0; g < gq; ++g) {
+          tma_load_3d(sa + g * kAq, &tmAq, &full[st], kb * 64, z * Mpad + m0, g);
+          tma_load_3d(sb + g * kBq, &tmBq, &full[st], kb * 64, n0, g);
+        }
+        for (int q = 0; q < tq; ++q) {
+          tma_load_3d(sa + NQ * kAq + q * kAt, &tmAt, &full[st], kb * kBK, z * Mpad + m0, q);
+          tma_load_3d(sb + NQ * kBq + q * kBt, &tmBt, &full[st], kb * kBK, n0, q);
+        }
+        issued = it + 1;
+      }
+      if (*abort_flag) {
+        for (int it = (issued > ST ? issued - ST : 0); it < issued; ++it) {
+          uint64_t t0 = gtimer();
+          while (!mbar_try(&full[it % ST], (it / ST) & 1) && gtimer() - t0 < 1000000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = idesc_bf16(kBM, BN);
+      bool ok = true;
+      int last = 0;
+      for (int pass = 0; pass < NPASS && ok; ++pass) {
+        last = pass;
+        if (pass == 1) {
+          ok = mbar_wait(tfree, 0, abort_flag, err, 24);
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          if (!ok) break;
+        }
+        for (int kb = 0; kb < nk; ++kb) {
+          const int it = pass * nk + kb, st = it % ST;
+          if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 22)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          const uint32_t a0 = sptr(smem + st * kStage);
+          const uint32_t b0 = a0 + kAbytes;
+          auto adesc = [&](int p) {
+            return p < 4 * NQ ? sdesc_sw128(a0 + (p >> 2) * kAq + (p & 3) * 32)
+                              : sdesc_sw32(a0 + NQ * kAq + (p - 4 * NQ) * kAt);
+          };
+          auto bdesc = [&](int p) {
+            return p < 4 * NQ ? sdesc_sw128(b0 + (p >> 2) * kBq + (p & 3) * 32)
+                              : sdesc_sw32(b0 + NQ * kBq + (p - 4 * NQ) * kBt);
+          };
+          if (pass == 0) {
+#pragma unroll
+            for (int d = 0; d < D1; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + d * BN, adesc(p), bdesc(d - p), idesc,
+                         (kb > 0 || p > 0) ? 1u : 0u);
+          } else {
+#pragma unroll
+            for (int d = D1; d < S; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + (d - D1) * BN, adesc(p), bdesc(d - p), idesc,
+                         (kb > 0 || p > 0) ? 1u : 0u);
+          }
+          mma_commit(&empty[st]);
+        }
+        mma_commit(&accf[pass]);
+      }
+      if (*abort_flag) {
+        uint64_t t0 = gtimer();
+        while (!mbar_try(&accf[last], 0) && gtimer() - t0 < 1000000000ull) {
+        }
+      }
+    }
+  } else {
+    const int q4 = warp & 3;
+    const int m = m0 + q4 * 32 + lane;
+    const int emr = (m < M) ? ea[z * Mpad + m] : 0;
+    double* Cz = C + (size_t)z * strideC;
+    for (int pass = 0; pass < NPASS; ++pass) {
+      const bool ok = mbar_wait(&accf[pass], 0, abort_flag, err, 23, 1000);
+      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+      if (!ok) break;
+      const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
+      for (int c0 = 0; c0 < BN; c0 += 16) {
+        long long v[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) v[j] = 0;
+        for (int d = d0; d < d1; ++d) {
+          float f[16];
+          tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (d - d0) * BN + c0, f);
+#pragma unroll
+          for (int j = 0; j < 16; ++j) v[j] = (v[j] << w) + (long long)__float2int_rn(f[j]);
+        }
+        if (m < M) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int n = n0 + c0 + j;
+            if (n < Nc) {
+              const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
+              double* dst = Cz + (size_t)n * ldc + m;
+              const double part = ldexp((double)v[j], E);
+              *dst = pass ? *dst + part : part;
+            }
+          }
+        }
+      }
+      if (pass == 0 && NPASS == 2) {
+        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
 // ------------------------------------------------------------------ slicing
 // FP64 arithmetic is scarce on this GPU, so the digits are cut with integer
 // operations on the bit pattern.  For a row with exponent e (max|x| < 2^e),
@@ -537,9 +977,21 @@ __device__ __forceinline__ uint16_t bf16_of_int(int a) {
 
 // One warp per row, two elements per lane: out[p][r][k] (plane-major) and the
 // row exponent.  Rows beyond `rows` are zero; K is even.
+// Element offset of digit (plane p, row r, element k) in a [s][rows][K] plane
+// set: plain, or grouped (planes 4g..4g+3 interleaved per 16-element K slice in
+// one 4K-wide row, the s % 4 remaining planes plain after them).
+__host__ __device__ __forceinline__ size_t digit_offset(bool grouped, int s, int p, size_t r,
+                                                        int k, int K, size_t rows) {
+  const int nq = grouped ? s / 4 : 0;
+  if (p < 4 * nq)
+    return ((size_t)(p >> 2) * rows + r) * 4 * (size_t)K + (size_t)(k >> 4) * 64 + (p & 3) * 16 +
+           (k & 15);
+  return (size_t)4 * nq * rows * K + ((size_t)(p - 4 * nq) * rows + r) * K + k;
+}
+
 __global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, int K,
                              int rows_pad, int s, int w, uint32_t* __restrict__ out,
-                             size_t plane, int32_t* __restrict__ e_out) {
+                             int grouped, int32_t* __restrict__ e_out) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= rows_pad) return;
@@ -558,7 +1010,6 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, in
   if (lane == 0) e_out[r] = e;
   const int ws = w * s;
   const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
-  uint32_t* o = out + ((size_t)r * K >> 1);
   for (int k = lane; k < K2; k += 32) {
     long long X0 = 0, X1 = 0;
     if (r < rows) {
@@ -566,15 +1017,17 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, in
       X0 = fixed_point(v.x, e, ws);
       X1 = fixed_point(v.y, e, ws);
     }
+    // elements 2k and 2k+1 are adjacent in both layouts: one 32-bit store
     for (int p = s - 1; p >= 1; --p) {
       const long long a0 = ((X0 + half) & mask) - half;
       const long long a1 = ((X1 + half) & mask) - half;
       X0 = (X0 - a0) >> w;
       X1 = (X1 - a1) >> w;
-      o[(size_t)p * (plane >> 1) + k] =
+      out[digit_offset(grouped, s, p, r, 2 * k, K, rows_pad) >> 1] =
           (uint32_t)bf16_of_int((int)a0) | ((uint32_t)bf16_of_int((int)a1) << 16);
     }
-    o[k] = (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
+    out[digit_offset(grouped, s, 0, r, 2 * k, K, rows_pad) >> 1] =
+        (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
   }
 }
 
@@ -611,12 +1064,30 @@ bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int bo
             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
+// 3-D map over the grouped layout's four-plane groups [nq][rows][4K]: a box is
+// the 64 elements (four planes x 16) of one K slice for box_rows rows, in
+// 128-byte rows with the 128-byte swizzle.
+bool make_map_groups(CUtensorMap* map, const void* base, int K, int rows, int nq, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)K * 4, (cuuint64_t)rows, (cuuint64_t)nq};
+  cuuint64_t strides[2] = {(cuuint64_t)K * 8, (cuuint64_t)K * rows * 8};
+  cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 1};
+  cuuint32_t es[3] = {1, 1, 1};
+  return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
+            es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 // One launch configuration of the split GEMM: the kernel (one pass with all
 // diagonals in tensor memory, or two passes with wider tiles) and the L2
 // raster group (row tiles whose digit planes share about ga_mb MB of L2).
 struct GemmConfig {
   int kind = 1;  // 0: k_split_gemm (one pass); 1, 2: k_split_gemm2 (two passes,
-                 // diagonals split at s/2 or s - s/2)
+                 // diagonals split at s/2 or s - s/2); 3, 4, 5: k_split_gemm3 with
+                 // 2 x 1, 1 x 2, 2 x 2 clusters (row x column tiles); these read
+                 // the plain layout.  6, 7, 8: k_split_gemm_g on the grouped
+                 // layout (two passes split at s/2 or s - s/2, or one pass)
   int ga_mb = 64;
 };
 
@@ -628,18 +1099,38 @@ __host__ __device__ constexpr int d1b_of(int s) { return s - s / 2; }
 __host__ __device__ constexpr int bn2_of(int s) {
   return ((512 / (s - s / 2)) / 16 * 16) > 128 ? 128 : ((512 / (s - s / 2)) / 16 * 16);
 }
+size_t smemg_bytes(int s, int bn) {
+  const size_t need = (size_t)kStages2 * stage_bytes_g(s, bn) + 1024 + 256;
+  return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;  // one CTA per SM
+}
 size_t smem2_bytes(int s, int bn) {
   const size_t need = (size_t)kStages2 * s * (kBM + bn) * kBK * 2 + 1024 + 256;
   return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;  // one CTA per SM
 }
 
-int tile_n(int s, int kind) { return kind == 0 ? bn_for(s) : bn2_of(s); }
-bool kind_valid(int s, int kind) { return kind == 0 || kind == 1 || (kind == 2 && (s & 1)); }
+int tile_n(int s, int kind) { return (kind == 0 || kind == 8) ? bn_for(s) : bn2_of(s); }
+// Kernels that read the context's digit layout (grouped needs s >= 4; below
+// that the grouped layout is the plain one).
+bool kind_valid(int s, int kind, bool grouped) {
+  if (grouped && s >= 4) return kind == 6 || kind == 8 || (kind == 7 && (s & 1));
+  return kind == 0 || kind == 1 || (kind == 2 && (s & 1)) || (kind >= 3 && kind <= 5 && s >= 4);
+}
+GemmConfig default_config(int s, bool grouped) {
+  GemmConfig g;
+  g.kind = (grouped && s >= 4) ? 6 : 1;
+  return g;
+}
+struct Maps {
+  CUtensorMap a, b;    // plain planes, or the grouped layout's four-plane groups
+  CUtensorMap at, bt;  // grouped layout: the s % 4 plain planes after the groups
+};
+// the two-pass split point the cluster kernels use
+__host__ __device__ constexpr int d1c_of(int s) { return s - s / 2; }
 
 SplitShape shape_of(const Ctx* c) {
   int s = c->params.split_slices > 0 ? c->params.split_slices : kDefaultSlices;
   s = std::min(std::max(s, 2), kMaxSlices);
-  return SplitShape{s, kDefaultW, tile_n(s, 1)};
+  return SplitShape{s, kDefaultW, tile_n(s, 6)};
 }
 
 // Dynamic shared memory above 48 KB must be enabled per kernel, once, before
@@ -661,6 +1152,33 @@ cudaError_t set_attributes() {
       status = cudaFuncSetAttribute(k_split_gemm2<S, BN2, d1b_of(S)>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     (int)smem2_bytes(S, BN2));
+    if constexpr (S >= 4) {
+      if (status == cudaSuccess)
+        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN2, D1>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smemg_bytes(S, BN2));
+      if (status == cudaSuccess && d1b_of(S) != D1)
+        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN2, d1b_of(S)>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smemg_bytes(S, BN2));
+      if (status == cudaSuccess)
+        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN1, S>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smemg_bytes(S, BN1));
+      constexpr int DC = d1c_of(S);
+      if (status == cudaSuccess)
+        status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 1>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem2_bytes(S, BN2));
+      if (status == cudaSuccess)
+        status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 1, 2>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem2_bytes(S, BN2));
+      if (status == cudaSuccess)
+        status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 2>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem2_bytes(S, BN2));
+    }
   });
   return status;
 }
@@ -676,20 +1194,66 @@ cudaError_t kernel_attributes(int s) {
 }
 
 template <int S>
-cudaError_t launch_gemm(const GemmConfig& cfg, const CUtensorMap& tA, const CUtensorMap& tB,
-                        const int32_t* ea, const int32_t* eb, double* C, int ldc, size_t strideC,
-                        int M, int Mpad, int Nc, int K, int batch, int w, int* err,
-                        cudaStream_t st) {
-  const bool one = cfg.kind == 0;
+cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea,
+                        const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
+                        int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
+  const CUtensorMap& tA = mp.a;
+  const CUtensorMap& tB = mp.b;
+  const bool one = cfg.kind == 0 || cfg.kind == 8;
   constexpr int BN1 = bn_for(S), BN2 = bn2_of(S), D1 = d1_of(S);
   const int BN = one ? BN1 : BN2;
-  const size_t sm = one ? smem_bytes(S, BN1) : smem2_bytes(S, BN2);
+  const size_t sm = cfg.kind == 0 ? smem_bytes(S, BN1)
+                    : cfg.kind >= 6 ? smemg_bytes(S, BN) : smem2_bytes(S, BN);
   cudaError_t e = set_attributes<S>();
   if (e != cudaSuccess) return e;
   const int nM = (M + kBM - 1) / kBM, nN = (Nc + BN - 1) / BN, nA = nM * batch;
   // row tiles per L2 group: their digit planes (128 x K x S bf16 each) within ga_mb MB
   const size_t a_tile = (size_t)kBM * K * S * 2;
   const int GA = std::max(1, std::min(nA, (int)(((size_t)cfg.ga_mb << 20) / a_tile)));
+  if constexpr (S >= 4) {
+    if (cfg.kind >= 6 && cfg.kind <= 8) {
+      const int grid = nA * nN;
+      if (cfg.kind == 8)
+        k_split_gemm_g<S, BN1, S><<<grid, kThreads, sm, st>>>(
+            mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
+            err);
+      else if (cfg.kind == 7 && d1b_of(S) != D1)
+        k_split_gemm_g<S, BN2, d1b_of(S)><<<grid, kThreads, sm, st>>>(
+            mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
+            err);
+      else
+        k_split_gemm_g<S, BN2, D1><<<grid, kThreads, sm, st>>>(
+            mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
+            err);
+      return cudaGetLastError();
+    }
+    if (cfg.kind >= 3 && cfg.kind <= 5) {
+      const int CM = cfg.kind == 4 ? 1 : 2, CN = cfg.kind == 3 ? 1 : 2;
+      const int nAc = (nA + CM - 1) / CM, nNc = (nN + CN - 1) / CN;
+      const int GAc = std::max(1, std::min(nAc, (int)(((size_t)cfg.ga_mb << 20) / (a_tile * CM))));
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3((unsigned)(nAc * nNc * CM * CN));
+      lc.blockDim = dim3(kThreads);
+      lc.dynamicSmemBytes = smem2_bytes(S, BN2);
+      lc.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = CM * CN;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      lc.attrs = at;
+      lc.numAttrs = 1;
+      constexpr int DC = d1c_of(S);
+      if (cfg.kind == 3)
+        return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 2, 1>, tA, tB, ea, eb, C, ldc,
+                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, err);
+      if (cfg.kind == 4)
+        return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 1, 2>, tA, tB, ea, eb, C, ldc,
+                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, err);
+      return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 2, 2>, tA, tB, ea, eb, C, ldc,
+                                strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, err);
+    }
+  }
   if (one)
     k_split_gemm<S, BN1><<<nA * nN, kThreads, sm, st>>>(
         tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
@@ -702,15 +1266,13 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const CUtensorMap& tA, const CUte
   return cudaGetLastError();
 }
 
-cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const CUtensorMap& tA,
-                          const CUtensorMap& tB, const int32_t* ea, const int32_t* eb, double* C,
-                          int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int batch,
-                          int w, int* err, cudaStream_t st) {
+cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const Maps& mp, const int32_t* ea,
+                          const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
+                          int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
   switch (s) {
-#define GI_S(SS)                                                                          \
-  case SS:                                                                                \
-    return launch_gemm<SS>(cfg, tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, \
-                           err, st);
+#define GI_S(SS)                                                                                \
+  case SS:                                                                                      \
+    return launch_gemm<SS>(cfg, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, err, st);
     GI_S(2) GI_S(3) GI_S(4) GI_S(5) GI_S(6) GI_S(7) GI_S(8) GI_S(9) GI_S(10)
 #undef GI_S
   }
@@ -718,13 +1280,20 @@ cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const CUtensorMap& tA,
 }
 
 cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s, int w,
-                  uint16_t* out, int32_t* e, cudaStream_t st) {
+                  bool grouped, uint16_t* out, int32_t* e, cudaStream_t st) {
   if (rows_pad <= 0) return cudaSuccess;
   const int wpb = 8;
-  if (K & 1) return cudaErrorInvalidValue;
+  if ((K & 1) || (grouped && (K & 15))) return cudaErrorInvalidValue;
   k_slice_rows<<<(rows_pad + wpb - 1) / wpb, wpb * 32, 0, st>>>(
-      X, ldx, rows, K, rows_pad, s, w, reinterpret_cast<uint32_t*>(out), (size_t)rows_pad * K, e);
+      X, ldx, rows, K, rows_pad, s, w, reinterpret_cast<uint32_t*>(out), grouped ? 1 : 0, e);
   return cudaGetLastError();
+}
+
+// Digit layout of a context: grouped (128-byte TMA rows) unless
+// GI_SPLIT_LAYOUT=plain asks for the plain plane-by-plane layout.
+bool grouped_layout() {
+  const char* e = getenv("GI_SPLIT_LAYOUT");
+  return !(e && std::strcmp(e, "plain") == 0);
 }
 
 }  // namespace
@@ -732,6 +1301,7 @@ cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s
 // Per-context state of the split path.
 struct SplitState {
   int s = 0, w = 0;
+  bool grouped = true;                        // digit layout of every operand
   int N = -1;                                 // dipole the slices belong to
   DevArray<uint16_t> mu_slices;      // [s][3*Mpad][Kp]
   DevArray<int32_t> mu_exp;                   // [3*Mpad]
@@ -776,9 +1346,12 @@ gi_status split_prepare(Ctx* c) {
     S->w = P->w;
     S->N = P->N;
     S->Mpad = P->Mpad;
+    S->grouped = P->grouped;
     return GI_OK;
   }
-  if (S->N == c->N && S->s == sh.s && S->w == sh.w) return GI_OK;
+  const bool grouped = grouped_layout();
+  if (S->N == c->N && S->s == sh.s && S->w == sh.w && S->grouped == grouped) return GI_OK;
+  S->grouped = grouped;
   // digit planes of the dipole: rows = 3 components x Mpad, K = Kp
   S->s = sh.s;
   S->w = sh.w;
@@ -797,17 +1370,31 @@ gi_status split_prepare(Ctx* c) {
   if (g != GI_OK) return g;
   g = check(c, texp.alloc(S->Mpad), "dipole exp temp");
   if (g != GI_OK) return g;
+  // per component into tmp ([s][Mpad][Kp] planes or groups), then each
+  // group / plane block to its row range comp * Mpad of the [3 Mpad] set
+  const int nq = grouped ? sh.s / 4 : 0;
+  const size_t blk = (size_t)S->Mpad * c->Kp;  // one plane of one component
   for (int comp = 0; comp < 3; ++comp) {
     g = check(c,
               slice(c->d_mu.p + (size_t)comp * c->N * c->Kp, c->Kp, c->N, c->Kp, S->Mpad, sh.s,
-                    sh.w, tmp.p, texp.p, c->stream),
+                    sh.w, grouped, tmp.p, texp.p, c->stream),
               "slice dipole");
     if (g != GI_OK) return g;
-    for (int p = 0; p < sh.s; ++p) {
+    for (int q = 0; q < nq; ++q) {  // groups of four planes: [q][rows][4 Kp]
       g = check(c,
-                cudaMemcpyAsync(S->mu_slices.p + ((size_t)p * rows + (size_t)comp * S->Mpad) * c->Kp,
-                                tmp.p + (size_t)p * S->Mpad * c->Kp,
-                                sizeof(uint16_t) * S->Mpad * c->Kp,
+                cudaMemcpyAsync(S->mu_slices.p + ((size_t)q * rows + (size_t)comp * S->Mpad) * 4 *
+                                                     c->Kp,
+                                tmp.p + (size_t)q * 4 * blk, sizeof(uint16_t) * 4 * blk,
+                                cudaMemcpyDeviceToDevice, c->stream),
+                "copy dipole groups");
+      if (g != GI_OK) return g;
+    }
+    for (int p = 4 * nq; p < sh.s; ++p) {  // plain planes after the groups
+      const size_t t = p - 4 * nq;
+      g = check(c,
+                cudaMemcpyAsync(S->mu_slices.p + (size_t)4 * nq * rows * c->Kp +
+                                    (t * rows + (size_t)comp * S->Mpad) * c->Kp,
+                                tmp.p + (size_t)4 * nq * blk + t * blk, sizeof(uint16_t) * blk,
                                 cudaMemcpyDeviceToDevice, c->stream),
                 "copy dipole planes");
       if (g != GI_OK) return g;
@@ -829,11 +1416,11 @@ gi_status split_prepare(Ctx* c) {
 // power-of-two column bucket, K).  With tuning on, the first GEMM of a class
 // times every candidate on its real operands with CUDA events and keeps the
 // fastest; the table lives for the process and, given a path, in a text file
-// ("s nA nbucket K kind ga_mb ms" per line).
+// ("s nA nbucket K layout kind ga_mb ms" per line).
 struct TuneKey {
-  int s, nA, nbucket, K;
+  int s, nA, nbucket, K, layout;
   bool operator<(const TuneKey& o) const {
-    return std::tie(s, nA, nbucket, K) < std::tie(o.s, o.nA, o.nbucket, o.K);
+    return std::tie(s, nA, nbucket, K, layout) < std::tie(o.s, o.nA, o.nbucket, o.K, o.layout);
   }
 };
 struct TuneEntry {
@@ -850,8 +1437,10 @@ static Tuner& tuner() {
   static Tuner t;
   return t;
 }
-static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16},
-                                         {2, 64}, {2, 32}, {0, 64}, {0, 32}};
+static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16}, {2, 64},
+                                         {2, 32}, {0, 64}, {0, 32}, {3, 32}, {4, 32},
+                                         {5, 32}, {6, 64}, {6, 32}, {6, 128}, {7, 64},
+                                         {7, 32}, {8, 64}, {8, 32}};
 
 static void tune_load(Tuner& t, const std::string& path) {
   t.loaded = path;
@@ -859,9 +1448,9 @@ static void tune_load(Tuner& t, const std::string& path) {
   if (!f) return;
   TuneKey k;
   TuneEntry e;
-  while (fscanf(f, "%d %d %d %d %d %d %f", &k.s, &k.nA, &k.nbucket, &k.K, &e.cfg.kind,
-                &e.cfg.ga_mb, &e.ms) == 7)
-    if (kind_valid(k.s, e.cfg.kind) && e.cfg.ga_mb > 0) t.table[k] = e;
+  while (fscanf(f, "%d %d %d %d %d %d %d %f", &k.s, &k.nA, &k.nbucket, &k.K, &k.layout,
+                &e.cfg.kind, &e.cfg.ga_mb, &e.ms) == 8)
+    if (kind_valid(k.s, e.cfg.kind, k.layout != 0) && e.cfg.ga_mb > 0) t.table[k] = e;
   fclose(f);
   t.version++;
 }
@@ -871,8 +1460,8 @@ static void tune_save(const Tuner& t, const std::string& path) {
   FILE* f = fopen(tmp.c_str(), "w");
   if (!f) return;
   for (const auto& kv : t.table)
-    fprintf(f, "%d %d %d %d %d %d %.4f\n", kv.first.s, kv.first.nA, kv.first.nbucket, kv.first.K,
-            kv.second.cfg.kind, kv.second.cfg.ga_mb, kv.second.ms);
+    fprintf(f, "%d %d %d %d %d %d %d %.4f\n", kv.first.s, kv.first.nA, kv.first.nbucket,
+            kv.first.K, kv.first.layout, kv.second.cfg.kind, kv.second.cfg.ga_mb, kv.second.ms);
   fclose(f);
   rename(tmp.c_str(), path.c_str());
 }
@@ -887,22 +1476,42 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
                       int Mpad, const uint16_t* Bslices, int Brows, const int32_t* eb,
                       double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch) {
   SplitState* S = state(c);
+  const bool grouped = S->grouped && S->s >= 4;
   auto run = [&](const GemmConfig& g) -> cudaError_t {
-    CUtensorMap tA, tB;
-    const int planes = g.kind == 0 ? S->s : 1;  // the two-pass kernel loads plane by plane
-    if (!make_map(&tA, Aslices, K, Arows_total, S->s, kBM, planes) ||
-        !make_map(&tB, Bslices, K, Brows, S->s, tile_n(S->s, g.kind), planes))
-      return cudaErrorInvalidValue;
-    return launch_gemm_s(S->s, g, tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, S->w,
+    Maps mp;
+    const int bn = tile_n(S->s, g.kind);
+    if (grouped) {
+      const int nq = S->s / 4, nt = S->s % 4;
+      const uint16_t* At = Aslices + (size_t)4 * nq * Arows_total * K;
+      const uint16_t* Bt = Bslices + (size_t)4 * nq * Brows * K;
+      if (!make_map_groups(&mp.a, Aslices, K, Arows_total, nq, kBM) ||
+          !make_map_groups(&mp.b, Bslices, K, Brows, nq, bn))
+        return cudaErrorInvalidValue;
+      if (nt) {
+        if (!make_map(&mp.at, At, K, Arows_total, nt, kBM, 1) ||
+            !make_map(&mp.bt, Bt, K, Brows, nt, bn, 1))
+          return cudaErrorInvalidValue;
+      } else {
+        mp.at = mp.a;  // no plain planes: never read
+        mp.bt = mp.b;
+      }
+    } else {
+      const int planes = g.kind == 0 ? S->s : 1;  // the two-pass kernels load plane by plane
+      if (!make_map(&mp.a, Aslices, K, Arows_total, S->s, kBM, planes) ||
+          !make_map(&mp.b, Bslices, K, Brows, S->s, bn, planes))
+        return cudaErrorInvalidValue;
+    }
+    return launch_gemm_s(S->s, g, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, S->w,
                          S->err.p, c->stream);
   };
-  const TuneKey key{S->s, ((M + kBM - 1) / kBM) * batch, col_bucket(Nc), K};
-  GemmConfig cfg;
+  const TuneKey key{S->s, ((M + kBM - 1) / kBM) * batch, col_bucket(Nc), K, (int)grouped};
+  GemmConfig cfg = default_config(S->s, grouped);
   bool known = false;
   // GI_SPLIT_FORCE="kind:ga_mb" pins one configuration (parity tests of every kernel)
   if (const char* f = getenv("GI_SPLIT_FORCE")) {
     GemmConfig g;
-    if (sscanf(f, "%d:%d", &g.kind, &g.ga_mb) == 2 && kind_valid(S->s, g.kind) && g.ga_mb > 0)
+    if (sscanf(f, "%d:%d", &g.kind, &g.ga_mb) == 2 && kind_valid(S->s, g.kind, grouped) &&
+        g.ga_mb > 0)
       return check(c, run(g), "split GEMM launch");
   }
   Tuner& t = tuner();
@@ -926,7 +1535,7 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
     GemmConfig best_cfg = cfg;
     for (const GemmConfig& cand : kCandidates) {
       if (g != GI_OK) break;
-      if (!kind_valid(S->s, cand.kind)) continue;
+      if (!kind_valid(S->s, cand.kind, grouped)) continue;
       g = check(c, cudaEventRecord(a, c->stream), "tuning event");
       if (g == GI_OK) g = check(c, run(cand), "tuning launch");
       if (g == GI_OK) g = check(c, cudaEventRecord(b, c->stream), "tuning event");
@@ -959,7 +1568,7 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
   g = check(c, S->b_exp.reserve(ncol), "Y exponents");
   if (g != GI_OK) return g;
   g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-              return slice(Y, ldy, ncol, K, ncol, S->s, S->w, S->b_slices.p, S->b_exp.p,
+              return slice(Y, ldy, ncol, K, ncol, S->s, S->w, S->grouped, S->b_slices.p, S->b_exp.p,
                            c->stream);
             }),
             "slice Y");
@@ -986,13 +1595,13 @@ static gi_status block_digits(Ctx* c, Block& fb, int K, bool wait) {
   const int vpad = round_up(nvec, kBM);
   gi_status g;
   std::lock_guard<std::mutex> lk(c->mmu());
-  if (fb.digits_s != S->s || fb.digits_w != S->w) {
+  if (fb.digits_s != S->s || fb.digits_w != S->w || fb.digits_layout != (int)S->grouped) {
     g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
     if (g != GI_OK) return g;
     g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
     if (g != GI_OK) return g;
     g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-                return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, fb.d_digits.p,
+                return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, S->grouped, fb.d_digits.p,
                              fb.d_digit_exp.p, c->stream);
               }),
               "slice V");
@@ -1005,6 +1614,7 @@ static gi_status block_digits(Ctx* c, Block& fb, int K, bool wait) {
     if (g != GI_OK) return g;
     fb.digits_s = S->s;
     fb.digits_w = S->w;
+    fb.digits_layout = (int)S->grouped;
   }
   if (wait && fb.digits_ev) {
     // inside a graph capture the cut precedes the capture on this stream
@@ -1047,7 +1657,7 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
   g = check(c, S->b_exp.reserve(ncol), "H exponents");
   if (g != GI_OK) return g;
   g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-              return slice(H, ldh, ncol, K, ncol, S->s, S->w, S->b_slices.p, S->b_exp.p,
+              return slice(H, ldh, ncol, K, ncol, S->s, S->w, S->grouped, S->b_slices.p, S->b_exp.p,
                            c->stream);
             }),
             "slice H");

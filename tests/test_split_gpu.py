@@ -57,17 +57,25 @@ def test_autotuner_table_and_results(pkg, synth, tmp_path):
         eng.run()
         got = np.sort(eng.lines(), order=["level_i", "level_f"])
     rows = [l.split() for l in open(path).read().splitlines()]
-    assert len(rows) >= 2 and all(len(r) == 7 for r in rows)
-    assert all(r[4] in ("0", "1", "2") for r in rows)
+    assert len(rows) >= 2 and all(len(r) == 8 for r in rows)
+    assert all(r[5] in ("6", "7", "8") for r in rows)  # the grouped layout's kernels
     assert np.array_equal(got[["level_i", "level_f"]], ref[["level_i", "level_f"]])
     assert np.allclose(got["S"], ref["S"], rtol=1e-12, atol=0)
 
 
-@pytest.mark.parametrize("config", ["0:64", "1:16", "1:128", "2:32"])
+@pytest.mark.parametrize("config", ["plain/0:64", "plain/1:16", "plain/1:128", "plain/2:32",
+                                    "plain/3:32", "plain/4:32", "plain/5:32", "plain/5:1",
+                                    "grouped/6:64", "grouped/6:1", "grouped/7:32",
+                                    "grouped/8:64"])
 def test_every_split_kernel_matches_oracle(pkg, synth, oracle, monkeypatch, config):
     """Each launch configuration the autotuner can pick (one-pass, two-pass at
-    either split point, several L2 groups), pinned with GI_SPLIT_FORCE."""
-    monkeypatch.setenv("GI_SPLIT_FORCE", config)
+    either split point, the multicast cluster kernels, the grouped-layout
+    kernels, several L2 groups), pinned with GI_SPLIT_FORCE on its digit layout.
+    Row and column tile counts are odd here, so the cluster kernels run tiles
+    past the edge too."""
+    layout, force = config.split("/")
+    monkeypatch.setenv("GI_SPLIT_LAYOUT", layout)
+    monkeypatch.setenv("GI_SPLIT_FORCE", force)
     prob = synth.make_c3v(13, 40, [0, 1, 2, 3], nvec_max=20)
     got, _ = run(pkg, prob)
     res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
