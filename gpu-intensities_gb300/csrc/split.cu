@@ -140,6 +140,20 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release;\nbarrier.cluster.wait.acquire;\n" ::: "memory");
 }
+// v * 2^E for an integer |v| < 2^53 (so the double is exact), built from the
+// bits with integer instructions: FP64 throughput is low on this GPU and the
+// epilogues convert every output element.  Results outside the normal range
+// take ldexp.
+__device__ __forceinline__ double scaled_int(long long v, int E) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int msb = 63 - __clzll((long long)a);
+  const int ex = 1023 + msb + E;
+  if (msb > 52 || ex <= 0 || ex >= 2047) return ldexp((double)v, E);
+  const unsigned long long mant = (a << (52 - msb)) & ((1ull << 52) - 1);
+  return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | mant));
+}
 // Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 32
 // bytes (16 elements) with the 32-byte swizzle: 8-row groups 256 bytes apart.
 __device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr) {
@@ -349,8 +363,8 @@ __global__ void __launch_bounds__(kThreads, 1)
             const int n = n0 + c0 + j;
             if (n < Nc) {
               const int E = emr + eb[n] - 2 * w;
-              const double v = ldexp((double)hi[j], E - w * (kHi - 1)) +
-                               ldexp((double)lo[j], E - w * (S - 1));
+              const double v = scaled_int(hi[j], E - w * (kHi - 1)) +
+                               scaled_int(lo[j], E - w * (S - 1));
               Cz[(size_t)n * ldc + m] = v;
             }
           }
@@ -530,7 +544,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (n < Nc) {
               const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
               double* dst = Cz + (size_t)n * ldc + m;
-              const double part = ldexp((double)v[j], E);
+              const double part = scaled_int(v[j], E);
               *dst = pass ? *dst + part : part;
             }
           }
@@ -715,7 +729,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             if (n < Nc) {
               const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
               double* dst = Cz + (size_t)n * ldc + m;
-              const double part = ldexp((double)v[j], E);
+              const double part = scaled_int(v[j], E);
               *dst = pass ? *dst + part : part;
             }
           }
@@ -744,16 +758,37 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 
-// Grouped-layout two-pass kernel.  TMA moves 32-byte rows at about a third
-// of the rate of 128-byte rows into shared memory (16.7 vs 48.3 B/clk/SM
-// measured on GB300), and the digit GEMM needs all s planes of a 16-wide K
-// slice per stage.  In the grouped layout every 128-byte row holds that K slice
-// for four planes (planes 4g..4g+3), so a stage is NQ = s/4 boxes of 128-byte
-// rows plus NT = s%4 boxes of 32-byte rows per operand, instead of s boxes of
-// 32-byte rows.  D1 = S runs the whole GEMM in one pass (all S accumulators in
-// tensor memory, BN <= 512/S).
+// Grouped-layout kernel.  TMA moves 32-byte rows at about a third of the rate
+// of 128-byte rows into shared memory (16.7 vs 48.3 B/clk/SM measured on
+// GB300), and the digit GEMM needs all s planes of a 16-wide K slice per
+// stage.  In the grouped layout every 128-byte row holds that K slice for four
+// planes (planes 4g..4g+3), so a stage is NQ = s/4 boxes of 128-byte rows plus
+// NT = s%4 boxes of 32-byte rows per operand.  D1 = S runs the whole GEMM in
+// one pass (all S accumulators in tensor memory, BN <= 512/S).
+//
+// Timeline of a tile (two passes): pass 0 (diagonals < D1) holds only D1
+// planes per K slice, so when they fit twice a ring slot carries PK = 2 K
+// slices and the MMA issuer stays ahead of the barrier round trip.  The eight
+// epilogue warps (two per 32-lane TMEM quadrant, half the columns each) read
+// all diagonals of a column chunk with one wait, fold them into exact int64
+// sums, keep pass 0's sums in registers and release the tensor memory at once;
+// pass 1's epilogue adds the two parts (one FP64 add per element) and stores.
+constexpr int kThreadsG = 320;  // warp 0 TMA, warp 1 MMA, warps 2..9 epilogue
+constexpr int kChunkG = 8;      // columns per tcgen05.ld in the epilogue
+
+__device__ __forceinline__ void tmem_ld8_nowait(uint32_t taddr, uint32_t* r) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];\n"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7])
+      : "r"(taddr));
+}
+__device__ __forceinline__ void tmem_wait_ld() {
+  asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
+}
+
 template <int S, int BN, int D1>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(kThreadsG, 1)
     k_split_gemm_g(const __grid_constant__ CUtensorMap tmAq, const __grid_constant__ CUtensorMap tmAt,
                    const __grid_constant__ CUtensorMap tmBq, const __grid_constant__ CUtensorMap tmBt,
                    const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
@@ -761,8 +796,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                    int nN, int GA, int* err) {
   constexpr int NQ = S / 4, NT = S % 4;
   constexpr int NPASS = D1 < S ? 2 : 1;
+  constexpr int HALF = BN / 2;                     // columns per epilogue warp
+  constexpr int NCH = HALF / kChunkG;              // chunks per epilogue warp
   static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
   static_assert((BN * 128) % 1024 == 0, "128-byte-swizzle tiles stay 1024-byte aligned");
+  static_assert(HALF % kChunkG == 0, "epilogue chunks");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -770,6 +808,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   constexpr uint32_t kAbytes = NQ * kAq + NT * kAt;
   constexpr uint32_t kStage = stage_bytes_g(S, BN);  // rounded up to 1024 bytes
   static_assert(kAbytes % 1024 == 0 && kStage >= kAbytes + NQ * kBq + NT * kBt, "stage layout");
+  // pass 0 of a two-pass tile: D1 <= 4 planes are group 0 alone; two K slices
+  // of it share a slot when they fit
+  constexpr int PK = (NPASS == 2 && D1 <= 4 && 2 * (kAq + kBq) <= kStage) ? 2 : 1;
   constexpr int ST = kStages2;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
   uint64_t* empty = full + ST;
@@ -786,6 +827,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int ai = grp * GA + r % gsz;
   const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
   const int nk = K / kBK;
+  const int nk0 = nk / PK;  // ring slots of pass 0 (K is a multiple of 64)
+  const int nslots = nk0 + (NPASS == 2 ? nk : 0);
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < ST; ++i) {
@@ -794,7 +837,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     mbar_init(&accf[0], 1);
     mbar_init(&accf[1], 1);
-    mbar_init(tfree, 128);
+    mbar_init(tfree, 256);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
@@ -809,24 +852,35 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = *tmem_slot;
 
   if (warp == 0) {
-    if (lane == 0) {  // TMA producer: both passes, one continuous stage ring
+    if (lane == 0) {  // TMA producer: both passes, one continuous slot ring
       int issued = 0;
-      for (int it = 0; it < NPASS * nk; ++it) {
-        const int pass = it >= nk, kb = it - pass * nk, st = it % ST;
-        const int np = pass ? S : D1;
-        const int gq = min(NQ, (np + 3) / 4), tq = max(0, np - 4 * NQ);
-        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 21, 64))
+      for (int it = 0; it < nslots; ++it) {
+        const int pass = it >= nk0, st = it % ST;
+        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 21))
           break;
         unsigned char* sa = smem + st * kStage;
-        unsigned char* sb = sa + kAbytes;
-        mbar_expect_tx(&full[st], gq * (kAq + kBq) + tq * (kAt + kBt));
-        for (int g = 0; g < gq; ++g) {
-          tma_load_3d(sa + g * kAq, &tmAq, &full[st], kb * 64, z * Mpad + m0, g);
-          tma_load_3d(sb + g * kBq, &tmBq, &full[st], kb * 64, n0, g);
-        }
-        for (int q = 0; q < tq; ++q) {
-          tma_load_3d(sa + NQ * kAq + q * kAt, &tmAt, &full[st], kb * kBK, z * Mpad + m0, q);
-          tma_load_3d(sb + NQ * kBq + q * kBt, &tmBt, &full[st], kb * kBK, n0, q);
+        if (pass == 0 && PK == 2) {
+          mbar_expect_tx(&full[st], 2 * (kAq + kBq));
+          for (int h = 0; h < 2; ++h) {
+            const int kb = 2 * it + h;
+            unsigned char* sh = sa + h * (kAq + kBq);
+            tma_load_3d(sh, &tmAq, &full[st], kb * 64, z * Mpad + m0, 0);
+            tma_load_3d(sh + kAq, &tmBq, &full[st], kb * 64, n0, 0);
+          }
+        } else {
+          const int kb = pass ? it - nk0 : it;
+          const int np = pass ? S : D1;
+          const int gq = min(NQ, (np + 3) / 4), tq = max(0, np - 4 * NQ);
+          unsigned char* sb = sa + kAbytes;
+          mbar_expect_tx(&full[st], gq * (kAq + kBq) + tq * (kAt + kBt));
+          for (int g = 0; g < gq; ++g) {
+            tma_load_3d(sa + g * kAq, &tmAq, &full[st], kb * 64, z * Mpad + m0, g);
+            tma_load_3d(sb + g * kBq, &tmBq, &full[st], kb * 64, n0, g);
+          }
+          for (int q = 0; q < tq; ++q) {
+            tma_load_3d(sa + NQ * kAq + q * kAt, &tmAt, &full[st], kb * kBK, z * Mpad + m0, q);
+            tma_load_3d(sb + NQ * kBq + q * kBt, &tmBt, &full[st], kb * kBK, n0, q);
+          }
         }
         issued = it + 1;
       }
@@ -843,22 +897,35 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t idesc = idesc_bf16(kBM, BN);
       bool ok = true;
       int last = 0;
-      for (int pass = 0; pass < NPASS && ok; ++pass) {
-        last = pass;
-        if (pass == 1) {
+      for (int it = 0; it < nslots && ok; ++it) {
+        const int pass = it >= nk0, st = it % ST;
+        if (pass == 1 && it == nk0) {  // pass 1 reuses pass 0's tensor memory
+          mma_commit(&accf[0]);
+          last = 1;
           ok = mbar_wait(tfree, 0, abort_flag, err, 24);
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
           if (!ok) break;
         }
-        for (int kb = 0; kb < nk; ++kb) {
-          const int it = pass * nk + kb, st = it % ST;
-          if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 22)) {
-            ok = false;
-            break;
+        if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 22)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+        const uint32_t sa = sptr(smem + st * kStage);
+        if (pass == 0 && PK == 2) {
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const uint32_t a0 = sa + h * (kAq + kBq), b0 = a0 + kAq;
+            const bool first = it == 0 && h == 0;
+#pragma unroll
+            for (int d = 0; d < D1; ++d)
+#pragma unroll
+              for (int p = 0; p <= d; ++p)
+                mma_bf16(tmem + d * BN, sdesc_sw128(a0 + p * 32), sdesc_sw128(b0 + (d - p) * 32),
+                         idesc, (!first || p > 0) ? 1u : 0u);
           }
-          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-          const uint32_t a0 = sptr(smem + st * kStage);
-          const uint32_t b0 = a0 + kAbytes;
+        } else {
+          const uint32_t a0 = sa, b0 = sa + kAbytes;
           auto adesc = [&](int p) {
             return p < 4 * NQ ? sdesc_sw128(a0 + (p >> 2) * kAq + (p & 3) * 32)
                               : sdesc_sw32(a0 + NQ * kAq + (p - 4 * NQ) * kAt);
@@ -867,6 +934,7 @@ __global__ void __launch_bounds__(kThreads, 1)
             return p < 4 * NQ ? sdesc_sw128(b0 + (p >> 2) * kBq + (p & 3) * 32)
                               : sdesc_sw32(b0 + NQ * kBq + (p - 4 * NQ) * kBt);
           };
+          const int kb = pass ? it - nk0 : it;
           if (pass == 0) {
 #pragma unroll
             for (int d = 0; d < D1; ++d)
@@ -882,10 +950,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 mma_bf16(tmem + (d - D1) * BN, adesc(p), bdesc(d - p), idesc,
                          (kb > 0 || p > 0) ? 1u : 0u);
           }
-          mma_commit(&empty[st]);
         }
-        mma_commit(&accf[pass]);
+        mma_commit(&empty[st]);
       }
+      if (ok) mma_commit(&accf[NPASS - 1]);
       if (*abort_flag) {
         uint64_t t0 = gtimer();
         while (!mbar_try(&accf[last], 0) && gtimer() - t0 < 1000000000ull) {
@@ -893,39 +961,54 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else {
-    const int q4 = warp & 3;
+    // warps 2..9: TMEM lane quadrant (warp % 4), column half (warp - 2) / 4
+    const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int m = m0 + q4 * 32 + lane;
     const int emr = (m < M) ? ea[z * Mpad + m] : 0;
     double* Cz = C + (size_t)z * strideC;
-    for (int pass = 0; pass < NPASS; ++pass) {
-      const bool ok = mbar_wait(&accf[pass], 0, abort_flag, err, 23, 1000);
+    const uint32_t lanes = (uint32_t)(q4 * 32) << 16;
+    long long v0[NCH][kChunkG];  // pass 0's exact sums of this thread's columns
+    bool ok = true;
+    for (int pass = 0; pass < NPASS && ok; ++pass) {
+      ok = mbar_wait(&accf[pass], 0, abort_flag, err, 23, 256);
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       if (!ok) break;
       const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        long long v[16];
 #pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = 0;
-        for (int d = d0; d < d1; ++d) {
-          float f[16];
-          tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (d - d0) * BN + c0, f);
+      for (int ch = 0; ch < NCH; ++ch) {
+        const int c0 = half * HALF + ch * kChunkG;
+        uint32_t f[(D1 > S - D1 ? D1 : S - D1)][kChunkG];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = (v[j] << w) + (long long)__float2int_rn(f[j]);
-        }
-        if (m < M) {
+        for (int d = 0; d < (D1 > S - D1 ? D1 : S - D1); ++d)
+          if (d < d1 - d0) tmem_ld8_nowait(tmem + lanes + d * BN + c0, f[d]);
+        tmem_wait_ld();
+        long long v[kChunkG];
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+        for (int j = 0; j < kChunkG; ++j) v[j] = 0;
+#pragma unroll
+        for (int d = 0; d < (D1 > S - D1 ? D1 : S - D1); ++d)
+          if (d < d1 - d0) {
+#pragma unroll
+            for (int j = 0; j < kChunkG; ++j)
+              v[j] = (v[j] << w) + (long long)__float2int_rn(__uint_as_float(f[d][j]));
+          }
+        if (pass == 0 && NPASS == 2) {
+#pragma unroll
+          for (int j = 0; j < kChunkG; ++j) v0[ch][j] = v[j];
+        } else if (m < M) {
+#pragma unroll
+          for (int j = 0; j < kChunkG; ++j) {
             const int n = n0 + c0 + j;
             if (n < Nc) {
-              const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
-              double* dst = Cz + (size_t)n * ldc + m;
-              const double part = ldexp((double)v[j], E);
-              *dst = pass ? *dst + part : part;
+              const int base = emr + eb[n] - 2 * w;
+              double out = scaled_int(v[j], base - w * (d1 - 1));
+              if (NPASS == 2) out = scaled_int(v0[ch][j], base - w * (D1 - 1)) + out;
+              Cz[(size_t)n * ldc + m] = out;
             }
           }
         }
       }
-      if (pass == 0 && NPASS == 2) {
+      if (pass == 0 && NPASS == 2) {  // all reads done: pass 1 may overwrite the columns
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
         asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
       }
@@ -1214,15 +1297,15 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
     if (cfg.kind >= 6 && cfg.kind <= 8) {
       const int grid = nA * nN;
       if (cfg.kind == 8)
-        k_split_gemm_g<S, BN1, S><<<grid, kThreads, sm, st>>>(
+        k_split_gemm_g<S, BN1, S><<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       else if (cfg.kind == 7 && d1b_of(S) != D1)
-        k_split_gemm_g<S, BN2, d1b_of(S)><<<grid, kThreads, sm, st>>>(
+        k_split_gemm_g<S, BN2, d1b_of(S)><<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       else
-        k_split_gemm_g<S, BN2, D1><<<grid, kThreads, sm, st>>>(
+        k_split_gemm_g<S, BN2, D1><<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       return cudaGetLastError();
