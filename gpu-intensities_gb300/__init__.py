@@ -93,6 +93,21 @@ class gi_serve_stats(C.Structure):
 
 
 GI_JOB_QUEUED, GI_JOB_RUNNING, GI_JOB_DONE, GI_JOB_FAILED = range(4)
+GI_TROVE_MAXQ = 17
+GI_TROVE_ALL_J = 1
+
+
+class gi_deck(C.Structure):
+    _fields_ = [("sym_type", C.c_int32), ("nmodes", C.c_int32), ("jvals", C.c_int32 * 2),
+                ("params", gi_params)]
+
+
+class gi_trove_level(C.Structure):
+    _fields_ = [("irec", C.c_int32 * 2), ("ilevel", C.c_int32), ("ndeg", C.c_int32),
+                ("krot", C.c_int32), ("taurot", C.c_int32), ("large_coef", C.c_int32),
+                ("reserved", C.c_int32), ("energy", C.c_double),
+                ("quanta", C.c_int32 * GI_TROVE_MAXQ), ("cgamma", C.c_int32 * GI_TROVE_MAXQ),
+                ("normal", C.c_int32 * GI_TROVE_MAXQ)]
 
 
 class GiError(RuntimeError):
@@ -147,6 +162,18 @@ def lib():
         L.gi_set_block_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.c_void_p, f64p, i32p]
         L.gi_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]
+        L.gi_deck_parse.argtypes = [C.c_char_p, C.POINTER(gi_deck), C.c_char_p, C.c_size_t]
+        L.gi_trove_read_basis.argtypes = [C.c_char_p, C.c_int, C.c_int, i32p, i32p, i32p, i32p,
+                                          i32p, i32p, i32p, C.POINTER(f64p), C.c_char_p,
+                                          C.c_size_t]
+        L.gi_trove_read_dipole.argtypes = [C.c_char_p, C.c_int, f64p, C.c_char_p, C.c_size_t]
+        L.gi_trove_read_levels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int,
+                                           C.c_int, i32p, i32p, C.POINTER(gi_trove_level),
+                                           C.c_int32, C.c_char_p, C.c_size_t]
+        L.gi_load_trove.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(gi_deck), C.c_int]
+        L.gi_format_lines.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_char_p, C.c_size_t,
+                                      C.POINTER(C.c_size_t)]
+        L.gi_partition_function.argtypes = [C.c_void_p, C.c_double, f64p]
         L.gi_serve_start.argtypes = [C.c_void_p, C.POINTER(gi_serve_config)]
         L.gi_serve_stop.argtypes = [C.c_void_p]
         L.gi_submit.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -157,6 +184,7 @@ def lib():
         L.gi_serve_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_serve_stats)]
         L.gi_serve_reset_stats.argtypes = [C.c_void_p]
         L.gi_get_lines.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
+        L.gi_sort_lines.argtypes = [C.c_void_p]
         L.gi_num_levels.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.gi_get_levels.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
         L.gi_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_stats)]
@@ -219,6 +247,67 @@ def make_params(p, precision: int = GI_PREC_FP64, split_slices: int = 0) -> gi_p
     g.thresh_linestrength = p.thresh_linestrength
     g.thresh_intensity = p.thresh_intensity
     return g
+
+
+def _host_err(st: int, err) -> None:
+    if st != GI_OK:
+        raise GiError(st, err.value.decode(errors="replace"))
+
+
+def parse_deck(text: str) -> gi_deck:
+    """The reference's input deck (gi_deck_parse), host only."""
+    d = gi_deck()
+    err = C.create_string_buffer(512)
+    _host_err(lib().gi_deck_parse(text.encode(), C.byref(d), err, 512), err)
+    return d
+
+
+def trove_read_basis(directory: str, J: int, sym_type: int, nrep: int, degen) -> Dict:
+    """j0eigen_quanta<J>.chk (with J=0's for the root correlation), host only."""
+    L = lib()
+    err = C.create_string_buffer(512)
+    dims = np.zeros(6, np.int32)
+    d = directory.encode()
+    _host_err(L.gi_trove_read_basis(d, J, sym_type, _p(dims, i32p), None, None, None, None, None,
+                                    None, None, err, 512), err)
+    D, ncase, maxdeg, mat, ncls, N = (int(x) for x in dims)
+    out = {"D": D, "ncase": ncase, "max_deg_size": maxdeg, "mat_size": mat, "nclasses": ncls,
+           "N": N, "k": np.zeros(D, np.int32), "ktau": np.zeros(D, np.int32),
+           "iroot": np.zeros(D, np.int32), "icontr2icase": np.zeros(2 * D, np.int32),
+           "Nsym": np.zeros(nrep * ncase, np.int32), "Ntotal": np.zeros(nrep, np.int32)}
+    # sizes of repres need Ntotal: a second call fills it, a third the tables
+    _host_err(L.gi_trove_read_basis(d, J, sym_type, _p(dims, i32p), None, None, None, None, None,
+                                    _p(out["Ntotal"], i32p), None, err, 512), err)
+    out["repres"] = [np.zeros(int(out["Ntotal"][g]) * degen[g] * mat, np.float64)
+                     for g in range(nrep)]
+    rp = (f64p * nrep)(*[_p(r, f64p) for r in out["repres"]])
+    _host_err(L.gi_trove_read_basis(d, J, sym_type, _p(dims, i32p), _p(out["k"], i32p),
+                                    _p(out["ktau"], i32p), _p(out["iroot"], i32p),
+                                    _p(out["icontr2icase"], i32p), _p(out["Nsym"], i32p),
+                                    _p(out["Ntotal"], i32p), rp, err, 512), err)
+    return out
+
+
+def trove_read_dipole(directory: str, N: int) -> np.ndarray:
+    mu = np.zeros(3 * N * N, np.float64)
+    err = C.create_string_buffer(512)
+    _host_err(lib().gi_trove_read_dipole(directory.encode(), N, _p(mu, f64p), err, 512), err)
+    return mu.reshape(3, N * N)
+
+
+def trove_read_levels(directory: str, J: int, gamma: int, sym_type: int, nmodes: int,
+                      nclasses: int):
+    """Levels of j0eigen_descr<J>_<gamma+1>.chk and its basis dimension."""
+    L = lib()
+    err = C.create_string_buffer(512)
+    n, dim = C.c_int32(0), C.c_int32(0)
+    d = directory.encode()
+    _host_err(L.gi_trove_read_levels(d, J, gamma, sym_type, nmodes, nclasses, C.byref(n),
+                                     C.byref(dim), None, 0, err, 512), err)
+    out = (gi_trove_level * max(n.value, 1))()
+    _host_err(L.gi_trove_read_levels(d, J, gamma, sym_type, nmodes, nclasses, C.byref(n),
+                                     C.byref(dim), out, n.value, err, 512), err)
+    return list(out)[:n.value], dim.value
 
 
 class Engine:
@@ -343,6 +432,10 @@ class Engine:
             self._ck(self._L.gi_get_lines(self._h, offset, count, out.ctypes.data))
         return out
 
+    def sort_lines(self):
+        """Order the last run's lines by (initial level, final level)."""
+        self._ck(self._L.gi_sort_lines(self._h))
+
     def levels(self) -> np.ndarray:
         n = C.c_int32(0)
         self._ck(self._L.gi_num_levels(self._h, C.byref(n)))
@@ -359,6 +452,28 @@ class Engine:
         out["seconds_phase"] = dict(zip(PHASES, list(s.seconds_phase)))
         out["launches_phase"] = dict(zip(PHASES, list(s.launches_phase)))
         return out
+
+    # TROVE jobs and the reference's line list ---------------------------------
+    def load_trove(self, directory: str, deck, all_j: bool = False):
+        d = parse_deck(deck) if isinstance(deck, str) else deck
+        self._ck(self._L.gi_load_trove(self._h, directory.encode(), C.byref(d),
+                                       GI_TROVE_ALL_J if all_j else 0))
+        self._deck = d
+
+    def format_lines(self, offset: int = 0, count: Optional[int] = None) -> str:
+        if count is None:
+            count = self.stats()["nlines"] - offset
+        used = C.c_size_t(0)
+        self._ck(self._L.gi_format_lines(self._h, offset, count, None, 0, C.byref(used)))
+        buf = C.create_string_buffer(used.value + 1)
+        self._ck(self._L.gi_format_lines(self._h, offset, count, buf, used.value + 1,
+                                         C.byref(used)))
+        return buf.value.decode()
+
+    def partition_function(self, temperature: float) -> float:
+        q = C.c_double(0.0)
+        self._ck(self._L.gi_partition_function(self._h, temperature, C.byref(q)))
+        return q.value
 
     # serving ---------------------------------------------------------------
     def serve_start(self, slots: int = 3, budget: int = 0, slot_workspace: int = 0):

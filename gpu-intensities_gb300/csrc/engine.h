@@ -133,6 +133,7 @@ struct Level {
 
 struct SplitState;  // split-precision state (split.cu)
 struct Server;      // serving loop (serve.cu)
+struct TroveMeta;   // level descriptors of a TROVE job (trove.cu)
 
 // One pair job of the serving loop: the lines of block (jI, gI) -> (jF, gF)
 // under the filters of the whole loaded job (its ZPE and J range).
@@ -149,6 +150,7 @@ struct Ctx {
   std::string tune_path;
   Ctx* parent = nullptr;      // a serving worker shares its parent's model state
   Server* server = nullptr;
+  TroveMeta* trove = nullptr;
   std::mutex model_mu;        // guards lazily derived shared state (digits)
   std::mutex& mmu() { return parent ? parent->model_mu : model_mu; }
   JobSel job;
@@ -254,6 +256,7 @@ gi_status ensure_ycsr(Ctx* c, Basis& b);
 gi_status server_make_room(Ctx* c, size_t bytes, Block* keep);
 // Stops the serving loop of c (if any): fails queued jobs, joins the workers.
 gi_status server_stop(Ctx* c);
+void trove_meta_release(Ctx* c);
 
 // ------------------------------------------------------------------ kernels
 struct EpiParams {

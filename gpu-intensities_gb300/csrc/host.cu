@@ -892,6 +892,7 @@ gi_status gi_destroy(gi_ctx* h) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   cudaSetDevice(c->device);
   server_stop(c);
+  trove_meta_release(c);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   cudaStreamSynchronize(c->stream);
   split_release(c);
@@ -1137,6 +1138,28 @@ gi_status gi_get_lines(gi_ctx* h, int64_t offset, int64_t count, gi_line* out) {
   } else {
     std::memcpy(out, c->h_lines + offset, sizeof(gi_line) * count);
   }
+  return GI_OK;
+}
+
+gi_status gi_sort_lines(gi_ctx* h) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c) return GI_ERR_ARG;
+  if (c->server) return fail(c, GI_ERR_STATE, "gi_sort_lines while serving");
+  const size_t n = (size_t)c->nlines;
+  if (n < 2) return GI_OK;
+  cudaSetDevice(c->device);
+  std::vector<gi_line> tmp;
+  gi_line* L = c->h_lines;
+  if (c->lines_on_device) {
+    tmp.resize(n);
+    GI_CUDA(c, cudaMemcpy(tmp.data(), c->d_lines.p, sizeof(gi_line) * n, cudaMemcpyDeviceToHost));
+    L = tmp.data();
+  }
+  std::sort(L, L + n, [](const gi_line& a, const gi_line& b) {
+    return a.level_i != b.level_i ? a.level_i < b.level_i : a.level_f < b.level_f;
+  });
+  if (c->lines_on_device)
+    GI_CUDA(c, cudaMemcpy(c->d_lines.p, tmp.data(), sizeof(gi_line) * n, cudaMemcpyHostToDevice));
   return GI_OK;
 }
 

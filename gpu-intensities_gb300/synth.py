@@ -479,3 +479,131 @@ def load(path: str) -> Problem:
             blocks[(J, g)] = Block(J, g, z[k], z[f"block{J}_{g}_energies"],
                                    z[f"block{J}_{g}_quanta"])
     return Problem(sym, int(z["N"]), z["mu"], bases, blocks, params, name=str(z["name"]))
+
+
+# ---------------------------------------------------------------- TROVE files
+def _fortran_record(f, payload: bytes) -> None:
+    n = np.int32(len(payload)).tobytes()
+    f.write(n)
+    f.write(payload)
+    f.write(n)
+
+
+def write_trove(prob: Problem, directory: str, thresh_linestrength: float = 0.0) -> str:
+    """Write a Problem as the TROVE checkpoints the reference reads and return
+    the matching input deck text.
+
+    Files (formats as the reference's readers parse them): j0_extfield.chk
+    (Fortran records, trove_functions.cpp:113-205), j0eigen_quanta<J>.chk
+    (trove_functions.cpp:401-679), j0eigen_descr<J>_<G>.chk and
+    j0eigen_vectors<J>_<G>.chk (trove_functions.cpp:1075-1429,
+    cuda_host.cu:1196).  The contracted basis is written with one vibrational
+    class: a case's class label is the J=0 case its roots correlate with and a
+    lambda's label the J=0 lambda, so correlate_index recovers
+    iroot_correlat_j0; every case is its own rotational level and
+    rot_index(case, lambda) carries (J, k, tau) of that root.  Every level of a
+    block is written once per degenerate component (records ndeg*i + ideg).
+    """
+    import os
+    if 0 not in prob.bases:
+        raise ValueError("a TROVE job needs the J=0 basis")
+    os.makedirs(directory, exist_ok=True)
+    info = SYM_INFO[prob.sym_type]
+    degen, labels = info["degen"], info["labels"]
+    nrep = len(degen)
+    b0 = prob.bases[0]
+    D0 = b0.Maxcontracts
+    c0 = np.asarray(b0.icontr2icase[:D0])
+    l0 = np.asarray(b0.icontr2icase[D0:])
+    for J, b in sorted(prob.bases.items()):
+        D = b.Maxcontracts
+        cases = np.asarray(b.icontr2icase[:D])
+        lams = np.asarray(b.icontr2icase[D:])
+        ncase = b.Maxsymcoeffs
+        ir = np.asarray(b.iroot_correlat_j0)
+        vib_case = np.full(ncase, -1)
+        lines = ["Start Primitive basis set",
+                 f"{ncase:8d}{b.max_deg_size:8d}{D:8d}{1:8d}"]
+        rot = []
+        r = 0
+        for c in range(ncase):
+            roots = np.nonzero(cases == c)[0]
+            if len(roots) == 0:
+                raise ValueError(f"J={J}: case {c} has no roots")
+            vc = set(int(c0[ir[x]]) for x in roots)
+            if len(vc) != 1:
+                raise ValueError(f"J={J}: case {c} correlates with several J=0 cases")
+            vib_case[c] = vc.pop()
+            lines.append(f"{len(roots):8d}{c + 1:6d}{vib_case[c] + 1:6d}")
+            for x in roots:
+                if x != r:
+                    raise ValueError(f"J={J}: roots are not ordered by case and lambda")
+                lam = int(lams[x])
+                lines.append(f"{x + 1:8d}{lam + 1:6d}{int(l0[ir[x]]) + 1:6d}")
+                rot.append((c, lam, int(b.k[x]), int(b.ktau[x]) & 1))
+                r += 1
+        lines.append(f"{ncase:8d}{b.max_deg_size:8d}")
+        for c, lam, k, tau in rot:
+            lines.append(f"{c + 1:8d}{lam + 1:8d}{J:8d}{k:8d}{tau:8d}")
+        lines += ["End Primitive basis set", "Start irreducible transformation",
+                  f"{b.mat_size:8d}", "".join(f"{int(n):8d}" for n in b.Ntotal)]
+        Nsym = np.asarray(b.Nsym)
+        for g in range(nrep):
+            for c in range(ncase):
+                lines.append(f"{int(Nsym[g + c * nrep]):8d}")
+            nt, dg = int(b.Ntotal[g]), degen[g]
+            rep = np.asarray(b.repres[g], np.float64)
+            for s in range(nt):
+                for d in range(dg):
+                    lines.append(" ".join(repr(float(rep[s + d * nt + i * nt * dg]))
+                                          for i in range(b.mat_size)))
+        lines.append("End irreducible transformation")
+        with open(os.path.join(directory, f"j0eigen_quanta{J}.chk"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+    N = prob.N
+    with open(os.path.join(directory, "j0_extfield.chk"), "wb") as f:
+        _fortran_record(f, b"Start external field")
+        _fortran_record(f, np.int32(N).tobytes())
+        mu = np.asarray(prob.mu, np.float64).reshape(3, N * N)
+        for c in range(3):
+            _fortran_record(f, np.int32(c + 1).tobytes())
+            _fortran_record(f, mu[c].tobytes())
+        _fortran_record(f, b"End external field")
+    nq = prob.params.nmodes + 1
+    for (J, g), blk in sorted(prob.blocks.items()):
+        dg = degen[g]
+        lines = [f"fingerprint J={J} gamma={labels[g]}", "Start Quantum numbers and energies",
+                 "   irec gamma ilevel ideg energy quanta", "",
+                 f"{blk.nvec * dg:8d}{blk.nsize:8d}"]
+        for i in range(blk.nvec):
+            q = " ".join(str(int(x)) for x in blk.quanta[i, :nq])
+            for ideg in range(1, dg + 1):
+                lines.append(f"{i * dg + ideg:8d}{g + 1:4d}{i + 1:8d}{ideg:4d} "
+                             f"{repr(float(blk.energies[i]))} {q} 1 {g + 1} {g + 1} {q}")
+        lines.append("End Quantum numbers and energies")
+        with open(os.path.join(directory, f"j0eigen_descr{J}_{g + 1}.chk"), "w") as f:
+            f.write("\n".join(lines) + "\n")
+        with open(os.path.join(directory, f"j0eigen_vectors{J}_{g + 1}.chk"), "wb") as f:
+            v = np.ascontiguousarray(blk.vecs, np.float64)
+            for i in range(blk.nvec):
+                for _ in range(dg):
+                    f.write(v[i].tobytes())
+    p = prob.params
+    js = sorted(prob.bases)
+    ql, qu = p.windows()
+    deck = [f"NMODES {p.nmodes}", f"SYMGROUP {info['name']}", "INTENSITY",
+            f"  TEMPERATURE {p.temperature!r}", f"  QSTAT {p.q_stat!r}", f"  ZPE {p.ZPE!r}",
+            f"  J {js[0]}, {js[-1]}",
+            f"  FREQ-WINDOW {p.freq_window[0]!r} {p.freq_window[1]!r}",
+            f"  ENERGY LOW {p.erange_lower[0]!r} {p.erange_lower[1]!r}, "
+            f"UPPER {p.erange_upper[0]!r} {p.erange_upper[1]!r}",
+            "  GNS " + " ".join(repr(float(x)) for x in p.gns[:nrep]),
+            "  SELECTION (pairs) " + " ".join(str(int(x)) for x in p.isym_pairs[:nrep]),
+            f"  THRESH_LINE {thresh_linestrength!r}"]
+    for m in range(p.nmodes):
+        deck.append(f"  V {m + 1} lower {int(ql[0][m])} {int(ql[1][m])} "
+                    f"upper {int(qu[0][m])} {int(qu[1][m])}")
+    if p.reduced:
+        deck.append("  SYMMETRY REDUCED")
+    deck.append("END")
+    return "\n".join(deck) + "\n"

@@ -211,6 +211,10 @@ gi_status gi_set_block_device(gi_ctx* ctx, int J, int gamma, int nsize, int nvec
    filters).  *nlines receives the count. */
 gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);
 gi_status gi_get_lines(gi_ctx* ctx, int64_t offset, int64_t count, gi_line* out);
+/* Orders the last run's lines by (initial level, final level), the order of
+   the reference's single-device loop (cuda_host.cu:1174-1473); the run
+   itself appends lines in the order its blocks finish. */
+gi_status gi_sort_lines(gi_ctx* ctx);
 gi_status gi_num_levels(gi_ctx* ctx, int32_t* n);
 gi_status gi_get_levels(gi_ctx* ctx, int32_t cap, gi_level* out);
 gi_status gi_get_stats(gi_ctx* ctx, gi_stats* out);
@@ -242,6 +246,73 @@ gi_status gi_half_ls(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF, const do
 #define GI_NOALLOC_SCRATCH_BYTES ((16u << 20) + (52u << 10))
 gi_status gi_half_ls_noalloc(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF,
                              const double* vsym_dev, double* half_ls_dev, void* stream);
+
+/* TROVE job files and the reference's text interfaces ----------------------- */
+/* The input deck (read_fields / read_intensities, fields.cpp:11-282): NMODES,
+ * SYMGROUP and the INTENSITY block (TEMPERATURE, QSTAT, ZPE, J, FREQ-WINDOW,
+ * ENERGY LOW/UPPER, GNS, SELECTION, THRESH_LINE, V n LOWER/UPPER, SYMMETRY
+ * REDUCED).  Fields the deck leaves out get open windows, g_ns = 1,
+ * T = 296 K, QSTAT = 1 and no threshold (the reference leaves them
+ * uninitialised).  Host only; err (optional) receives a message. */
+typedef struct {
+  int32_t sym_type;  /* 1 C2V(M), 2 C3V(M), 3 D3H(M) */
+  int32_t nmodes;
+  int32_t jvals[2];  /* the deck's "J j0 j1" */
+  gi_params params;
+} gi_deck;
+gi_status gi_deck_parse(const char* text, gi_deck* deck, char* err, size_t err_cap);
+
+#define GI_TROVE_MAXQ 17 /* quanta(0:nmodes) entries kept per level */
+typedef struct {
+  int32_t irec[2];     /* records of the degenerate components, 1-based */
+  int32_t ilevel;      /* level index within its file, 0-based */
+  int32_t ndeg;
+  int32_t krot, taurot;
+  int32_t large_coef;
+  int32_t reserved;
+  double energy;
+  int32_t quanta[GI_TROVE_MAXQ];  /* quanta(0:nmodes); quanta(0) the rotational index */
+  int32_t cgamma[GI_TROVE_MAXQ];  /* symmetry of each class (0:nclasses), 0-based */
+  int32_t normal[GI_TROVE_MAXQ];  /* normal-mode quanta (0:nmodes) */
+} gi_trove_level;
+
+/* Host-only readers of TROVE checkpoints in `dir` (no GPU needed):
+ *   gi_trove_read_basis   j0eigen_quanta<J>.chk with J=0's for the root
+ *                         correlation (bset_contr_factory + correlate_index,
+ *                         trove_functions.cpp:401-858).  dims receives
+ *                         {D, ncase, max_deg_size, mat_size, nclasses, N}; the
+ *                         arrays (any may be NULL) have gi_set_basis's layout.
+ *   gi_trove_read_dipole  j0_extfield.chk (trove_functions.cpp:113-205), in
+ *                         gi_set_dipole's record order.
+ *   gi_trove_read_levels  j0eigen_descr<J>_<gamma+1>.chk (read_eigenvalues,
+ *                         trove_functions.cpp:1075-1429): one entry per level
+ *                         (ideg = 1 line) in file order; call with out = NULL
+ *                         for the count. */
+gi_status gi_trove_read_basis(const char* dir, int J, int sym_type, int32_t* dims, int32_t* k,
+                              int32_t* ktau, int32_t* iroot_correlat_j0, int32_t* icontr2icase,
+                              int32_t* Nsym, int32_t* Ntotal, double* const* repres, char* err,
+                              size_t err_cap);
+gi_status gi_trove_read_dipole(const char* dir, int N, double* mu, char* err, size_t err_cap);
+gi_status gi_trove_read_levels(const char* dir, int J, int gamma, int sym_type, int nmodes,
+                               int nclasses, int32_t* n, int32_t* dim_basis, gi_trove_level* out,
+                               int32_t cap_levels, char* err, size_t err_cap);
+
+#define GI_TROVE_ALL_J 1 /* load every J in [j0, j1], not only j0 and j1 */
+/* Loads a TROVE job into the context: symmetry and parameters from the deck
+ * (keeping the context's precision choice), the J=0 basis, the bases of the
+ * deck's J values, the dipole, and one block per (J, gamma) with g_ns > 0 holding
+ * every level of its descr file (ideg = 1 record of each, from the vectors
+ * file).  Replaces dipole_initialise_cpu + the per-level fread
+ * (cuda_host.cu:837-898, 1196-1199). */
+gi_status gi_load_trove(gi_ctx* ctx, const char* dir, const gi_deck* deck, int flags);
+/* The lines [offset, offset+count) of the last gi_run (lines with level-table
+   ids) as the reference prints them (cuda_host.cu:1444-1473), one per text
+   line; *used receives the bytes needed (without the final NUL). */
+gi_status gi_format_lines(gi_ctx* ctx, int64_t offset, int64_t count, char* buf, size_t cap,
+                          size_t* used);
+/* Partition function over the loaded levels: sum of g_ns(gamma) (2J+1) ndeg
+   exp(-c2 (E - ZPE) / T); the reference takes it from the deck (QSTAT). */
+gi_status gi_partition_function(gi_ctx* ctx, double temperature, double* q);
 
 /* Serving ----------------------------------------------------------------- */
 /* No counterpart in the reference, which processes one (J, J+1) job per

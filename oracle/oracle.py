@@ -131,8 +131,57 @@ def ref():
                                   C.c_double, C.c_int, i32p, i32p, i32p]
         R.ref_degeneracy_filter.restype = C.c_int
         R.ref_degeneracy_filter.argtypes = [C.POINTER(or_job), C.c_int, C.c_int, C.c_int, C.c_int]
+        R.ref_read_quanta.restype = C.c_int
+        R.ref_read_quanta.argtypes = [C.c_char_p, C.c_int, C.c_int, i32p, i32p, i32p, i32p, i32p,
+                                      i32p, i32p, i32p, C.POINTER(f64p)]
+        R.ref_read_levels.restype = C.c_int
+        R.ref_read_levels.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, C.c_int, i32p,
+                                      C.c_int, C.c_int, C.c_double, C.c_double, C.c_double, f64p,
+                                      C.c_int, C.c_int, C.c_void_p]
         _ref = R
     return _ref
+
+
+REF_LEVEL = np.dtype([("jval", np.int32), ("igamma", np.int32), ("ilevel", np.int32),
+                      ("ndeg", np.int32), ("irec0", np.int32), ("irec1", np.int32),
+                      ("krot", np.int32), ("taurot", np.int32), ("energy", np.float64),
+                      ("quanta", np.int32, (17,)), ("normal", np.int32, (17,)),
+                      ("cgamma", np.int32, (17,))], align=True)  # the C struct's padding
+
+
+def ref_trove_basis(directory: str, J: int, degen) -> dict:
+    """The reference's bset_contr_factory + correlate_index on TROVE files."""
+    R = ref()
+    nrep = len(degen)
+    dg = np.asarray(degen, np.int32)
+    dims = np.zeros(5, np.int32)
+    nt = np.zeros(nrep, np.int32)
+    R.ref_read_quanta(directory.encode(), J, nrep, ptr(dg, i32p), ptr(dims, i32p), None, None,
+                      None, None, None, ptr(nt, i32p), None)
+    D, ncase, _, mat, _ = (int(x) for x in dims)
+    out = {"k": np.zeros(D, np.int32), "ktau": np.zeros(D, np.int32),
+           "iroot": np.zeros(D, np.int32), "icontr2icase": np.zeros(2 * D, np.int32),
+           "Nsym": np.zeros(nrep * ncase, np.int32), "Ntotal": nt,
+           "repres": [np.zeros(int(nt[g]) * degen[g] * mat) for g in range(nrep)],
+           "dims": dims}
+    rp = (f64p * nrep)(*[ptr(r, f64p) for r in out["repres"]])
+    R.ref_read_quanta(directory.encode(), J, nrep, ptr(dg, i32p), ptr(dims, i32p),
+                      ptr(out["k"], i32p), ptr(out["ktau"], i32p), ptr(out["iroot"], i32p),
+                      ptr(out["icontr2icase"], i32p), ptr(out["Nsym"], i32p), ptr(nt, i32p), rp)
+    return out
+
+
+def ref_trove_levels(directory: str, jvals, sym_type: int, degen, nmodes: int, nclasses: int,
+                     zpe: float, erange, gns, maxcontracts: int, cap: int = 100000) -> np.ndarray:
+    """The reference's read_eigenvalues over the descr files of (j0, j1)."""
+    R = ref()
+    dg = np.asarray(degen, np.int32)
+    g = np.asarray(gns, np.float64)
+    out = np.zeros(cap, REF_LEVEL)
+    n = R.ref_read_levels(directory.encode(), jvals[0], jvals[1], sym_type, len(degen),
+                          ptr(dg, i32p), nmodes, nclasses, zpe, erange[0], erange[1],
+                          ptr(g, f64p), maxcontracts, cap, out.ctypes.data)
+    return out[:n]
 
 
 def ptr(a: np.ndarray, t):

@@ -5,6 +5,7 @@
 #include <cuda_runtime_api.h>  // the host stand-in in oracle/ref/inc
 
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -237,6 +238,111 @@ int ref_degeneracy_filter(const or_job* j, int gI, int gF, int idegI, int idegF)
   int r = degeneracy_filter(f, gI, gF, idegI, idegF);
   drop_job(f, keep);
   return r;
+}
+
+
+// bset_contr_factory + correlate_index (trove_functions.cpp:401-858) on the
+// j0eigen_quanta files in dir.  dims receives {D, ncase, max_deg, mat_size,
+// nclasses}; with k == NULL only dims and Ntotal (when given) are filled.
+int ref_read_quanta(const char* dir, int J, int nrep, const int* degen, int* dims, int* k,
+                    int* ktau, int* iroot, int* icontr2icase, int* Nsym, int* Ntotal,
+                    double** repres) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof(cwd))) return -1;
+  if (chdir(dir) != 0) return -2;
+  TO_bset_contrT b0, b;
+  std::memset((void*)&b0, 0, sizeof(b0));
+  std::memset((void*)&b, 0, sizeof(b));
+  bset_contr_factory(&b0, 0, const_cast<int*>(degen), nrep);
+  TO_bset_contrT* t = &b0;
+  if (J != 0) {
+    bset_contr_factory(&b, J, const_cast<int*>(degen), nrep);
+    t = &b;
+  }
+  correlate_index(b0, *t);
+  int rc = chdir(cwd);
+  (void)rc;
+  const int D = t->Maxcontracts;
+  dims[0] = D;
+  dims[1] = t->Maxsymcoeffs;
+  dims[2] = t->max_deg_size;
+  dims[3] = t->mat_size;
+  dims[4] = t->Nclasses;
+  if (Ntotal) std::memcpy(Ntotal, t->Ntotal, sizeof(int) * nrep);
+  if (!k) return 0;
+  std::memcpy(k, t->k, sizeof(int) * D);
+  std::memcpy(ktau, t->ktau, sizeof(int) * D);
+  std::memcpy(iroot, t->iroot_correlat_j0, sizeof(int) * D);
+  std::memcpy(icontr2icase, t->icontr2icase, sizeof(int) * 2 * D);
+  for (int g = 0; g < nrep; g++) {
+    for (int ic = 0; ic < t->Maxsymcoeffs; ic++) Nsym[g + ic * nrep] = t->irr[g].N[ic];
+    std::memcpy(repres[g], t->irr[g].repres,
+                sizeof(double) * (size_t)t->Ntotal[g] * degen[g] * t->mat_size);
+  }
+  return 0;
+}
+
+// read_eigenvalues (trove_functions.cpp:1075-1429) for jvals (j0, j1) on the
+// descr files in dir; the level fields as ref_level records.
+struct ref_level {
+  int jval, igamma, ilevel, ndeg, irec0, irec1, krot, taurot;
+  double energy;
+  int quanta[17], normal[17], cgamma[17];
+};
+
+int ref_read_levels(const char* dir, int j0, int j1, int sym_type, int nrep, const int* degen,
+                    int nmodes, int nclasses, double zpe, double elow, double ehigh,
+                    const double* gns, int maxcontracts, int cap, ref_level* out) {
+  char cwd[4096];
+  if (!getcwd(cwd, sizeof(cwd))) return -1;
+  if (chdir(dir) != 0) return -2;
+  FintensityJob f;
+  std::memset((void*)&f, 0, sizeof(f));
+  f.jvals[0] = j0;
+  f.jvals[1] = j1;
+  f.ZPE = zpe;
+  f.erange[0] = elow;
+  f.erange[1] = ehigh;
+  f.molec.nmodes = nmodes;
+  f.molec.nclasses = nclasses;
+  f.molec.sym_nrepres = nrep;
+  f.molec.sym_degen = const_cast<int*>(degen);
+  f.molec.sym_type = sym_type;
+  f.molec.c_sym = new char*[nrep];
+  for (int g = 0; g < nrep; g++) {
+    f.molec.c_sym[g] = new char[4];
+    std::snprintf(f.molec.c_sym[g], 4, "%d", g);
+  }
+  f.isym_do = new bool[nrep];
+  for (int g = 0; g < nrep; g++) f.isym_do[g] = gns[g] > 0.00000001;
+  for (int i = 0; i < 3; i++) {
+    f.bset_contr[i].Maxcontracts = maxcontracts;
+    f.bset_contr[i].nsize = new int[nrep];
+  }
+  read_eigenvalues(f);
+  int rc = chdir(cwd);
+  (void)rc;
+  const int n = std::min(cap, f.Neigenlevels);
+  for (int i = 0; i < n; i++) {
+    const TO_PTeigen& e = f.eigen[i];
+    ref_level& r = out[i];
+    std::memset(&r, 0, sizeof(r));
+    r.jval = e.jval;
+    r.igamma = e.igamma;
+    r.ilevel = e.ilevel;
+    r.ndeg = e.ndeg;
+    r.irec0 = e.irec[0];
+    r.irec1 = e.ndeg > 1 ? e.irec[1] : 0;
+    r.krot = e.krot;
+    r.taurot = e.taurot;
+    r.energy = e.energy;
+    for (int q = 0; q <= nmodes && q < 17; q++) {
+      r.quanta[q] = e.quanta[q];
+      r.normal[q] = e.normal[q];
+    }
+    for (int q = 0; q <= nclasses && q < 17; q++) r.cgamma[q] = std::atoi(e.cgamma[q]);
+  }
+  return f.Neigenlevels;
 }
 
 }  // extern "C"

@@ -118,6 +118,30 @@ def filter_fixture(prob, name, R, O):
                         quanta_upper=qu, jvals=np.array([js[0], js[-1]]))
 
 
+def trove_fixture(prob, name, O):
+    """A small TROVE job (files as the reference reads them) and what the
+    reference's own readers make of it: bset_contr_factory + correlate_index
+    per J and read_eigenvalues."""
+    synth = sys.modules["gpu_intensities_gb300.synth"]
+    d = os.path.join(HERE, f"trove_{name}")
+    deck = synth.write_trove(prob, d)
+    with open(os.path.join(d, "job.inp"), "w") as f:
+        f.write(deck)
+    out = {}
+    for J in prob.jlist:
+        b = O.ref_trove_basis(d, J, prob.degen)
+        for key in ("k", "ktau", "iroot", "icontr2icase", "Nsym", "Ntotal", "dims"):
+            out[f"basis{J}_{key}"] = b[key]
+        for g, r in enumerate(b["repres"]):
+            out[f"basis{J}_repres{g}"] = r
+    js = prob.jlist
+    lv = O.ref_trove_levels(d, (js[0], js[-1]), prob.sym_type, prob.degen,
+                            prob.params.nmodes, 1, prob.params.ZPE, (-1e300, 1e300),
+                            prob.params.gns, max(b.Maxcontracts for b in prob.bases.values()))
+    out["levels"] = lv
+    np.savez_compressed(os.path.join(HERE, f"trove_{name}_ref.npz"), **out)
+
+
 def main():
     G.build()
     G.load_package()
@@ -147,6 +171,7 @@ def main():
                         degen.append((prob.sym_type, int(prob.params.reduced), gI, gF, dI, dF,
                                       R.ref_degeneracy_filter(C.byref(job), gI, gF, dI, dF)))
     np.save(os.path.join(HERE, "degeneracy_filter.npy"), np.array(degen, np.int32))
+    trove_fixture(synth.make_c3v(6, 12, [0, 1], nvec_max=3), "c3v", O)
     print("fixtures written to", HERE)
 
 
