@@ -142,6 +142,7 @@ struct JobSel {
   int jI = 0, gI = 0, jF = 0, gF = 0;
   double zpe = 0.0;
   int jmin = 0, jmax = 0;
+  double qstat = 0.0;  // partition function of the whole job (when QSTAT <= 0)
 };
 
 struct Ctx {
@@ -247,6 +248,8 @@ gi_status fail(Ctx* c, gi_status s, const char* fmt, ...);
                         "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
   } while (0)
 
+// Sum of g_ns (2J+1) ndeg exp(-c2 (E - zpe) / T) over the loaded levels.
+double partition_sum(const Ctx* c, double temperature, double zpe);
 // Runs every block pair of the loaded job (or the one pair of c->job).
 gi_status run_job(Ctx* c, int flags, int64_t* nlines_out);
 // Builds the (slot, v) -> roots table of a basis for the context's dipole size.

@@ -16,6 +16,20 @@
 
 namespace gi {
 
+double partition_sum(const Ctx* c, double temperature, double zpe) {
+  const double planck = 6.62606896e-27, vellgt = 2.99792458e10, boltz = 1.380658e-16;
+  const double beta = planck * vellgt / (boltz * temperature);
+  double sum = 0.0;
+  for (const auto& kv : c->blocks) {
+    const int J = kv.first.first, g = kv.first.second;
+    const double gns = c->params.gns[g];
+    if (!(gns > 0.0)) continue;
+    const double w = gns * (2.0 * J + 1.0) * c->degen[g];
+    for (double E : kv.second->energies) sum += w * std::exp(-(E - zpe) * beta);
+  }
+  return sum;
+}
+
 uint64_t next_uid() {
   static std::atomic<uint64_t> n{1};
   return n++;
@@ -468,6 +482,10 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
 
   Phys ph;
   const double beta = ph.planck * ph.vellgt / (ph.boltz * P.temperature);
+  // QSTAT <= 0: the partition function of the loaded levels (FP64)
+  const double qstat = P.q_stat > 0 ? P.q_stat
+                       : (c->job.on ? c->job.qstat : partition_sum(c, P.temperature, zpe));
+  if (!(qstat > 0)) return fail(c, GI_ERR_ARG, "partition function is not positive");
 
   // capacities
   size_t cap_total = 0;
@@ -724,7 +742,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         ep.gns = P.gns[u.I->blk->gamma];
         ep.zpe = zpe;
         ep.beta = beta;
-        ep.q_stat = P.q_stat;
+        ep.q_stat = qstat;
         ep.fw0 = P.freq_window[0];
         ep.fw1 = P.freq_window[1];
         ep.thresh_S = P.thresh_linestrength;

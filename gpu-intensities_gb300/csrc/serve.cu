@@ -39,6 +39,7 @@ struct JobRec {
   gi_params params{};
   double zpe = 0.0;
   int jmin = 0, jmax = 0;
+  double qstat = 0.0;
   int state = GI_JOB_QUEUED;
   gi_status status = GI_OK;
   std::string err;
@@ -224,7 +225,7 @@ static void worker_main(Server* s, int slot) {
     w->threej = c->threej;
     w->threej_jmax = c->threej_jmax;
     w->threej_user = c->threej_user;
-    w->job = JobSel{true, j->jI, j->gI, j->jF, j->gF, j->zpe, j->jmin, j->jmax};
+    w->job = JobSel{true, j->jI, j->gI, j->jF, j->gF, j->zpe, j->jmin, j->jmax, j->qstat};
     lk.unlock();
     int64_t n = 0;
     std::string err;
@@ -422,6 +423,8 @@ gi_status gi_submit(gi_ctx* h, int jI, int gammaI, int jF, int gammaF, uint64_t*
         !it->second->energies.empty())
       zpe = it->second->energies[0];
     j->zpe = zpe;
+    j->qstat = c->params.q_stat > 0 ? c->params.q_stat
+                                    : partition_sum(c, c->params.temperature, zpe);
     j->id = s->next_id++;
     s->jobs[j->id] = j;
     s->queue.push_back(j);

@@ -754,20 +754,11 @@ gi_status gi_partition_function(gi_ctx* h, double temperature, double* q) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c || !q || !(temperature > 0)) return GI_ERR_ARG;
   if (!c->have_params) return fail(c, GI_ERR_STATE, "gi_set_params not called");
-  const double planck = 6.62606896e-27, vellgt = 2.99792458e10, boltz = 1.380658e-16;
-  const double beta = planck * vellgt / (boltz * temperature);
   double zpe = c->params.ZPE;
   auto it0 = c->blocks.find({0, 0});
   if (zpe < 0 && it0 != c->blocks.end() && !it0->second->energies.empty())
     zpe = it0->second->energies[0];
-  double sum = 0.0;
-  for (auto& kv : c->blocks) {
-    const int J = kv.first.first, g = kv.first.second;
-    const double gns = c->params.gns[g];
-    if (!(gns > 0.0)) continue;
-    const double w = gns * (2.0 * J + 1.0) * c->degen[g];
-    for (double E : kv.second->energies) sum += w * std::exp(-(E - zpe) * beta);
-  }
+  const double sum = partition_sum(c, temperature, zpe);
   *q = sum;
   return GI_OK;
 }

@@ -311,7 +311,8 @@ gi_status gi_load_trove(gi_ctx* ctx, const char* dir, const gi_deck* deck, int f
 gi_status gi_format_lines(gi_ctx* ctx, int64_t offset, int64_t count, char* buf, size_t cap,
                           size_t* used);
 /* Partition function over the loaded levels: sum of g_ns(gamma) (2J+1) ndeg
-   exp(-c2 (E - ZPE) / T); the reference takes it from the deck (QSTAT). */
+   exp(-c2 (E - ZPE) / T); the reference takes it from the deck (QSTAT).  A run
+   whose q_stat is <= 0 uses this value at its temperature. */
 gi_status gi_partition_function(gi_ctx* ctx, double temperature, double* q);
 
 /* Serving ----------------------------------------------------------------- */

@@ -92,3 +92,23 @@ def test_gi_main_process(pkg, synth, tmp_path):
     assert len(body.splitlines()) > 10
     key = ln["level_i"].astype(np.int64) * (1 << 32) + ln["level_f"]
     assert np.all(np.diff(key) > 0)
+
+
+def test_computed_partition_function_in_the_run(pkg, synth):
+    """q_stat <= 0: the run divides by the partition function of the loaded
+    levels, as if that value had been given."""
+    prob = synth.make_c2v(34, 24, [0, 1, 2], nvec_max=6)
+    with pkg.Engine(0) as eng:
+        eng.load(prob)
+        q = eng.partition_function(prob.params.temperature)
+        p = prob.params
+        p.q_stat = q
+        eng.set_params(p)
+        eng.run()
+        want = np.sort(eng.lines(), order=KEY)
+        p.q_stat = 0.0
+        eng.set_params(p)
+        eng.run()
+        got = np.sort(eng.lines(), order=KEY)
+    assert len(want) > 50
+    assert np.array_equal(got["I"], want["I"]) and np.array_equal(got["S"], want["S"])
