@@ -7,9 +7,11 @@ seed with the shapes, sizes and value distributions of the named workloads:
 * ``c2v_small``   triatomic C2v, J=0..2, Nvib=200, all eigenvectors (CPU-sized)
 * ``c2v_plain``   triatomic C2v, J=0..10, Nvib=2000, lowest 1000 vectors per
                   (J, Gamma) under 15000 cm^-1 (the throughput workload)
-* ``c2v_precision`` C2v, J=20,21, Nvib=5000, ~26k per Gamma, 2000 vectors,
+* ``c2v_precision`` C2v, J=20,21, Nvib=5000, ~26k per Gamma (the J>0 bases
+                  built on the lowest 2500 J=0 functions), 2000 vectors,
                   dipole magnitudes log-uniform 1e-8..1
-* ``c3v_batched`` tetratomic C3v (A1, A2, E), uneven blocks, T=500 K
+* ``c3v_batched`` tetratomic C3v (A1, A2, E), Nvib=3000, J=0..40 (blocks up
+                  to ~60k), <=1500 vectors under 12000 cm^-1, T=500 K
 
 The contracted basis is the product form TROVE produces for a rigid-rotor
 factor: for each J the "cases" are (k, vibrational function) with
@@ -341,9 +343,14 @@ def make_block(rng: np.random.Generator, J: int, g: int, nsize: int, nmodes: int
         e = e[e < ecut]
     nvec = len(e) if nvec_max is None else min(nvec_max, len(e))
     e = e[:nvec].copy()
-    if nvec > 0:
+    if nvec > 0 and nsize * nvec <= 20_000_000:
         q, r = np.linalg.qr(rng.standard_normal((nsize, nvec)))
         vecs = np.ascontiguousarray((q * np.sign(np.diag(r))[None, :]).T)
+    elif nvec > 0:
+        # large blocks: unit Gaussian vectors (nearly orthogonal at these sizes;
+        # a QR would take minutes and changes nothing the intensity path sees)
+        vecs = rng.standard_normal((nvec, nsize))
+        vecs /= np.linalg.norm(vecs, axis=1, keepdims=True)
     else:
         vecs = np.zeros((0, nsize))
     quanta = np.zeros((nvec, nmodes + 1), np.int32)
@@ -369,8 +376,11 @@ def make_c2v(seed: int, N: int, jlist: List[int], nvec_max: Optional[int] = None
     mu = make_dipole(rng, N, dipole)
     vib = _c2v_vib_syms(rng, N)
     bases, blocks = {}, {}
+    # nsize_scale < 1: the J > 0 bases use the lowest part of the J = 0
+    # functions, as a contracted TROVE basis truncated by energy does
+    M = max(1, int(round(N * nsize_scale)))
     for J in jlist:
-        b = make_c2v_basis(J, vib, rng)
+        b = make_c2v_basis(J, vib if J == 0 else vib[:M], rng)
         bases[J] = b
         for g in range(4):
             nsize = int(b.Ntotal[g])
@@ -425,6 +435,18 @@ def workload(name: str, seed: int = 1, **kw) -> Problem:
                         name=name, **kw)
     if name == "c3v_small":
         return make_c3v(seed, kw.pop("N", 60), kw.pop("jlist", [0, 1, 2, 3]), name=name, **kw)
+    if name == "c2v_precision":
+        # one large pair J = 20 -> 21, Nvib = 5000, ~26k functions per Gamma,
+        # 2000 vectors per block, dipole magnitudes log-uniform in [1e-8, 1]
+        return make_c2v(seed, kw.pop("N", 5000), kw.pop("jlist", [20, 21]),
+                        nvec_max=kw.pop("nvec_max", 2000), dipole="loguniform",
+                        nsize_scale=kw.pop("nsize_scale", 0.5), name=name, **kw)
+    if name == "c3v_batched":
+        # tetratomic C3v, Nvib = 3000, blocks up to ~60k functions (J = 40),
+        # up to 1500 vectors under 12000 cm^-1, T = 500 K; jlist selects J
+        return make_c3v(seed, kw.pop("N", 3000), kw.pop("jlist", list(range(41))),
+                        nvec_max=kw.pop("nvec_max", 1500), ecut=kw.pop("ecut", 12000.0),
+                        name=name, **kw)
     raise KeyError(name)
 
 
