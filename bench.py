@@ -68,6 +68,8 @@ def parse():
                     help="serving: pair jobs of the J <= jmax part of the workload")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: Poisson jobs/s")
     ap.add_argument("--serve-slots", type=int, default=3)
+    ap.add_argument("--tune-table", default=None,
+                    help="autotuner table file: read if present, extended and written")
     return ap.parse_args()
 
 
@@ -324,7 +326,8 @@ def main_ours(args):
     eng.load(prob, precision=prec, split_slices=args.slices)
     # the warm-up steps also tune the split GEMM launch configurations
     import tempfile
-    tune_path = os.path.join(tempfile.gettempdir(), f"gi_tune_{os.getpid()}.txt")
+    tune_path = args.tune_table or os.path.join(tempfile.gettempdir(),
+                                                f"gi_tune_{os.getpid()}.txt")
     eng.set_tuning(1, tune_path)
     # the engine's launches go to this stream, so its CUDA events bracket them
     stream = torch.cuda.Stream(device=local)

@@ -982,12 +982,23 @@ __global__ void __launch_bounds__(kThreadsG, 1)
         for (int d = 0; d < (D1 > S - D1 ? D1 : S - D1); ++d)
           if (d < d1 - d0) tmem_ld8_nowait(tmem + lanes + d * BN + c0, f[d]);
         tmem_wait_ld();
-        long long v[kChunkG];
+        // exact int64 sums: Horner in 2^w over at most SPLIT diagonals each
+        // (a single pass keeps two of them, hi = d < SPLIT and lo = the rest,
+        // so that no sum exceeds 2^63)
+        constexpr int SPLIT = NPASS == 2 ? S : (S + 1) / 2;
+        long long v[kChunkG], hi[kChunkG];
 #pragma unroll
-        for (int j = 0; j < kChunkG; ++j) v[j] = 0;
+        for (int j = 0; j < kChunkG; ++j) v[j] = hi[j] = 0;
 #pragma unroll
         for (int d = 0; d < (D1 > S - D1 ? D1 : S - D1); ++d)
           if (d < d1 - d0) {
+            if (NPASS == 1 && d == SPLIT) {
+#pragma unroll
+              for (int j = 0; j < kChunkG; ++j) {
+                hi[j] = v[j];
+                v[j] = 0;
+              }
+            }
 #pragma unroll
             for (int j = 0; j < kChunkG; ++j)
               v[j] = (v[j] << w) + (long long)__float2int_rn(__uint_as_float(f[d][j]));
@@ -1003,6 +1014,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
               const int base = emr + eb[n] - 2 * w;
               double out = scaled_int(v[j], base - w * (d1 - 1));
               if (NPASS == 2) out = scaled_int(v0[ch][j], base - w * (D1 - 1)) + out;
+              else out = scaled_int(hi[j], base - w * (SPLIT - 1)) + out;
               Cz[(size_t)n * ldc + m] = out;
             }
           }

@@ -80,3 +80,23 @@ def test_every_split_kernel_matches_oracle(pkg, synth, oracle, monkeypatch, conf
     got, _ = run(pkg, prob)
     res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
     print(config, res)
+
+
+@pytest.mark.parametrize("config", ["plain/0:64", "plain/1:64", "plain/2:64", "plain/3:32",
+                                    "plain/5:32", "grouped/6:64", "grouped/7:64",
+                                    "grouped/8:64"])
+def test_every_split_kernel_large_k(pkg, synth, monkeypatch, config):
+    """Each configuration at contraction lengths of 1216 (half line strength)
+    to ~2100 (final states), where the exact integer diagonal sums reach the
+    int64 range, against the FP64 GPU path on the same job."""
+    layout, force = config.split("/")
+    prob = synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12)
+    with pkg.Engine(0) as eng:
+        eng.load(prob, precision=pkg.GI_PREC_FP64)
+        eng.run()
+        want = pkg.keyed(eng.lines(), eng.levels())
+    monkeypatch.setenv("GI_SPLIT_LAYOUT", layout)
+    monkeypatch.setenv("GI_SPLIT_FORCE", force)
+    got, _ = run(pkg, prob)
+    res = compare(got, want, rtol_S=1e-10, norm_tol=1e-12)
+    print(config, res)
