@@ -42,10 +42,10 @@ import __graft_entry__ as G  # noqa: E402
 
 METRIC = "linestrengths/s"
 THRESH_I = 1e-30  # cm/molecule
-# DRAM bytes (read + write) of one half-line-strength k_split_gemm2 launch per Y
-# column: ncu on the J <= 4 part of c2v_plain measured 71.35 GB + 9.13 GB for a
+# DRAM bytes (read + write) of one half-line-strength k_split_gemm_g launch per Y
+# column: ncu on the J <= 4 part of c2v_plain measured 62.14 GB + 6.54 GB for a
 # launch of 1000 x 96-column tiles.
-SPLIT_HALFLS_DRAM_BYTES_PER_COL = (71.346804e9 + 9.126300e9) / 96000
+SPLIT_HALFLS_DRAM_BYTES_PER_COL = (62.136866e9 + 6.543222e9) / 96000
 
 
 def parse():
@@ -387,7 +387,7 @@ def main_ours(args):
     except OSError:
         pass
     if args.precision == "split":
-        # the dominant launch: the half-line-strength split GEMM (k_split_gemm2),
+        # the dominant launch: the half-line-strength split GEMM (k_split_gemm_g),
         # one launch per step; digit-pair products x 2 x 3 x N x N x Y columns
         dom = "halfls_gemm"
         pairs = ps["flops_tensor"] / max(ps["flops_halfls"] + ps["flops_final"], 1.0)
@@ -395,8 +395,8 @@ def main_ours(args):
         ncol = ps["flops_halfls"] / (6.0 * prob.N * prob.N)
         peak = peaks.get("bf16_tflops", 1900.0)
         achieved = flops / sp[dom] / 1e12 if sp[dom] else 0.0
-        roof = {"bound": "tensor", "kernel": "k_split_gemm2 (tcgen05 bf16 digit GEMM, "
-                                             "half line strength)",
+        roof = {"bound": "tensor", "kernel": "k_split_gemm_g (tcgen05 bf16 digit GEMM, "
+                                             "grouped digit layout, half line strength)",
                 "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                 "frac": achieved / peak,
                 "traffic": SPLIT_HALFLS_DRAM_BYTES_PER_COL * ncol / lp[dom],
