@@ -431,18 +431,28 @@ def main_ours(args):
         h2d = mu.numel() * 8 + sum(v.numel() * 8 for v in pin.values())
         ne = args.e2e_steps or args.steps
 
+        parts = {"upload_ms": 0.0, "run_ms": 0.0}
+
         def step():
+            t0 = time.perf_counter()
             eng.set_dipole(prob.N, mu.numpy())
             for (J, g), b in sorted(prob.blocks.items()):
                 eng.set_block(J, g, pin[(J, g)].numpy(), b.energies, b.quanta)
-            return eng.run(lines_on_device=False, graph=True)
+            t1 = time.perf_counter()
+            n = eng.run(lines_on_device=False, graph=True)
+            parts["upload_ms"] += 1e3 * (t1 - t0)
+            parts["run_ms"] += 1e3 * (time.perf_counter() - t1)
+            return n
 
         step()
+        parts["upload_ms"] = parts["run_ms"] = 0.0
         te, n = timed_steps(ne, step)
         st = eng.stats()
         e2e = {"value": world * st["nlines_filtered"] / te, "unit": METRIC,
                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(n * 80 + 16),
-               "ms_per_step": 1e3 * te, "steps": ne}
+               "ms_per_step": 1e3 * te, "steps": ne,
+               "host_wall_ms_per_step": {k: v / ne for k, v in parts.items()},
+               "last_run_ms": {"wall": 1e3 * st["seconds_total"], "device": 1e3 * st["seconds_gpu"]}}
 
     # the plain FP64 GPU path on the same job, and per-line accuracy of the
     # split path against it on the J <= 3 part of the workload

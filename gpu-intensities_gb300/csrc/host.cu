@@ -977,12 +977,13 @@ gi_status gi_set_dipole(gi_ctx* h, int N, const double* mu) {
   if (c->server) return fail(c, GI_ERR_STATE, "gi_set_dipole while serving (gi_serve_stop first)");
   cudaSetDevice(c->device);
   const int Kp = round_up(N, 64);
-  std::vector<double> hbuf((size_t)3 * N * Kp, 0.0);
-  for (int comp = 0; comp < 3; comp++)
-    for (int f = 0; f < N; f++)
-      std::memcpy(&hbuf[((size_t)comp * N + f) * Kp], mu + (size_t)comp * N * N + (size_t)f * N,
-                  sizeof(double) * N);
-  GI_CUDA(c, c->d_mu.upload(hbuf));
+  // record order mu_c(i, f) at c*N*N + i + f*N is already "row f = mu_c(:, f)":
+  // one pitched copy pads the rows to Kp (the padding is zeroed first)
+  if (c->d_mu.n != (size_t)3 * N * Kp) GI_CUDA(c, c->d_mu.alloc((size_t)3 * N * Kp));
+  GI_CUDA(c, cudaMemset(c->d_mu.p, 0, sizeof(double) * c->d_mu.n));
+  GI_CUDA(c, cudaMemcpy2D(c->d_mu.p, sizeof(double) * Kp, mu, sizeof(double) * N,
+                          sizeof(double) * N, (size_t)3 * N, cudaMemcpyHostToDevice));
+  GI_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));
   c->N = N;
   c->Kp = Kp;
   split_invalidate(c);
