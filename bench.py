@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-path comparison")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-stream", action="store_true",
+                    help="skip the streamed-dipole measurement")
     ap.add_argument("--serve-jmax", type=int, default=4,
                     help="serving: pair jobs of the J <= jmax part of the workload")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: Poisson jobs/s")
@@ -454,6 +456,25 @@ def main_ours(args):
                "host_wall_ms_per_step": {k: v / ne for k, v in parts.items()},
                "last_run_ms": {"wall": 1e3 * st["seconds_total"], "device": 1e3 * st["seconds_gpu"]}}
 
+    # the same job with the dipole kept in host memory and streamed through
+    # the device in four panels per half-ls GEMM (copies overlap the GEMMs)
+    streamed = None
+    if not args.no_stream:
+        rows = -(-prob.N // 4)
+        rows = -(-rows // 128) * 128
+        eng.set_dipole_streamed(prob.N, prob.mu, panel_rows=rows)
+        eng.run(lines_on_device=True)  # warm-up (and tuning of the panel GEMM shapes)
+        ts, _ = timed_steps(1, lambda: eng.run(lines_on_device=True))
+        ss = eng.stats()
+        nr = ss["launches_phase"]["halfls_gemm"] // -(-prob.N // rows)  # GEMM rounds per step
+        streamed = {"value": world * ss["nlines_filtered"] / ts, "unit": METRIC,
+                    "ms_per_step": 1e3 * ts, "steps": 1, "warmup": 1, "panel_rows": rows,
+                    "panels": -(-prob.N // rows), "rounds": int(nr),
+                    "h2d_bytes_per_step": int(nr * 3 * prob.N * prob.N * 8),
+                    "vs_resident": (ss["nlines_filtered"] / ts) / (lines_pre / dt),
+                    "graph": "eager launches (a streamed dipole is not captured)"}
+        eng.set_dipole(prob.N, prob.mu)
+
     # the plain FP64 GPU path on the same job, and per-line accuracy of the
     # split path against it on the J <= 3 part of the workload
     fp64 = accuracy = None
@@ -491,6 +512,7 @@ def main_ours(args):
                "gpu_launches": launches, "graph": "each step is one CUDA graph launch (captured "
                "in warm-up, replayed)", "autotune": autotune, "roofline": roof, "e2e": e2e,
                "fp64_path": fp64, "accuracy": accuracy, "serving": serving,
+               "dipole_streamed": streamed,
                "clocks": clk.summary()}
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline(prob)

@@ -95,6 +95,8 @@ class gi_serve_stats(C.Structure):
 GI_JOB_QUEUED, GI_JOB_RUNNING, GI_JOB_DONE, GI_JOB_FAILED = range(4)
 GI_TROVE_MAXQ = 17
 GI_TROVE_ALL_J = 1
+GI_TROVE_STREAM_DIPOLE = 2
+GI_DIPOLE_BORROW = 1
 
 
 class gi_deck(C.Structure):
@@ -154,6 +156,8 @@ def lib():
         L.gi_set_params.argtypes = [C.c_void_p, C.POINTER(gi_params)]
         L.gi_set_dipole.argtypes = [C.c_void_p, C.c_int, f64p]
         L.gi_set_dipole_flipped.argtypes = [C.c_void_p, C.c_int, f64p]
+        L.gi_set_dipole_streamed.argtypes = [C.c_void_p, C.c_int, f64p, C.c_int, C.c_int]
+        L.gi_dipole_panel_rows.argtypes = [C.c_void_p]
         L.gi_set_basis.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    i32p, i32p, i32p, i32p, i32p, i32p, C.POINTER(f64p)]
         L.gi_set_threej.argtypes = [C.c_void_p, C.c_int, f64p]
@@ -374,6 +378,23 @@ class Engine:
             raise ValueError("dip must hold 3*N*N doubles")
         self._ck(self._L.gi_set_dipole_flipped(self._h, N, _p(m, f64p)))
 
+    def set_dipole_streamed(self, N: int, mu: np.ndarray, panel_rows: int = 0,
+                            borrow: bool = False):
+        """Dipole kept in host memory and streamed through the device in panels
+        of `panel_rows` rows f (0: the engine's default).  With borrow=True the
+        engine page-locks and reads this array (kept alive by the Engine)."""
+        m = np.ascontiguousarray(mu, np.float64).reshape(-1)
+        if m.size != 3 * N * N:
+            raise ValueError("mu must hold 3*N*N doubles")
+        self._ck(self._L.gi_set_dipole_streamed(self._h, N, _p(m, f64p), panel_rows,
+                                                GI_DIPOLE_BORROW if borrow else 0))
+        self._borrowed = m if borrow else None
+
+    @property
+    def dipole_panel_rows(self) -> int:
+        """Rows per panel of a streamed dipole; 0 when the dipole is resident."""
+        return int(self._L.gi_dipole_panel_rows(self._h))
+
     def set_basis(self, b):
         arrs = [np.ascontiguousarray(getattr(b, n), np.int32) for n in
                 ("icontr2icase", "iroot_correlat_j0", "k", "ktau", "Nsym", "Ntotal")]
@@ -404,11 +425,16 @@ class Engine:
         self._ck(self._L.gi_set_block_device(self._h, J, gamma, nsize, nvec,
                                              C.c_void_p(vecs_dev_ptr), _p(e, f64p), _p(q, i32p)))
 
-    def load(self, prob, precision: int = GI_PREC_FP64, split_slices: int = 0):
-        """Hand a synth.Problem (or any object with the same fields) to the engine."""
+    def load(self, prob, precision: int = GI_PREC_FP64, split_slices: int = 0,
+             panel_rows: Optional[int] = None):
+        """Hand a synth.Problem (or any object with the same fields) to the engine;
+        panel_rows (not None) streams the dipole from host memory in panels."""
         self.set_symmetry(prob.sym_type)
         self.set_params(prob.params, precision, split_slices)
-        self.set_dipole(prob.N, prob.mu)
+        if panel_rows is None:
+            self.set_dipole(prob.N, prob.mu)
+        else:
+            self.set_dipole_streamed(prob.N, prob.mu, panel_rows)
         for J in sorted(prob.bases):
             self.set_basis(prob.bases[J])
         for (J, g), b in sorted(prob.blocks.items()):
@@ -454,10 +480,11 @@ class Engine:
         return out
 
     # TROVE jobs and the reference's line list ---------------------------------
-    def load_trove(self, directory: str, deck, all_j: bool = False):
+    def load_trove(self, directory: str, deck, all_j: bool = False,
+                   stream_dipole: bool = False):
         d = parse_deck(deck) if isinstance(deck, str) else deck
-        self._ck(self._L.gi_load_trove(self._h, directory.encode(), C.byref(d),
-                                       GI_TROVE_ALL_J if all_j else 0))
+        flags = (GI_TROVE_ALL_J if all_j else 0) | (GI_TROVE_STREAM_DIPOLE if stream_dipole else 0)
+        self._ck(self._L.gi_load_trove(self._h, directory.encode(), C.byref(d), flags))
         self._deck = d
 
     def format_lines(self, offset: int = 0, count: Optional[int] = None) -> str:

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <functional>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -134,6 +135,7 @@ struct Level {
 struct SplitState;  // split-precision state (split.cu)
 struct Server;      // serving loop (serve.cu)
 struct TroveMeta;   // level descriptors of a TROVE job (trove.cu)
+struct DipoleStream;  // dipole kept in host memory, streamed in panels (stream.cu)
 
 // One pair job of the serving loop: the lines of block (jI, gI) -> (jF, gF)
 // under the filters of the whole loaded job (its ZPE and J range).
@@ -171,6 +173,8 @@ struct Ctx {
   int N = 0, Kp = 0;          // dipole size and padded row stride
   DevArray<double> d_mu;      // [3][N rows f][Kp]: row f holds mu_c(:, f)
   const double* mu() const { return parent ? parent->d_mu.p : d_mu.p; }
+  DipoleStream* dstream = nullptr;  // set: the dipole stays in host memory
+  bool streamed() const { return (parent ? parent->dstream : dstream) != nullptr; }
 
   std::map<int, std::shared_ptr<Basis>> bases;
   std::map<std::pair<int, int>, std::shared_ptr<Block>> blocks;
@@ -260,6 +264,20 @@ gi_status server_make_room(Ctx* c, size_t bytes, Block* keep);
 // Stops the serving loop of c (if any): fails queued jobs, joins the workers.
 gi_status server_stop(Ctx* c);
 void trove_meta_release(Ctx* c);
+
+// The dipole in panels of rows f: fn(panel, component stride, rows, f0) is
+// called in order, with stream `st` ordered after the panel's [3][rows][Kp]
+// doubles are on the device.  A resident dipole is one panel of N rows.
+using PanelFn = std::function<gi_status(const double*, size_t, int, int)>;
+gi_status for_each_dipole_panel(Ctx* c, cudaStream_t st, const PanelFn& fn);
+// Z_c = mu_c^T Y in FP64 (rows f of Z at ldz, components zc apart).
+gi_status dipole_gemm_fp64(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zc,
+                           int ncol, cudaStream_t st);
+// Makes `pinned` (cudaMallocHost, [3][N][N] record order) the context's
+// streamed dipole; the context frees it.
+gi_status dipole_stream_adopt(Ctx* c, int N, double* pinned, int panel_rows);
+void dipole_stream_release(Ctx* c);
+int dipole_panel_rows(const Ctx* c);
 
 // ------------------------------------------------------------------ kernels
 struct EpiParams {

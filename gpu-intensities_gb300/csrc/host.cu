@@ -608,7 +608,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   c->timing = (flags & GI_RUN_PHASE_TIMING) != 0;
   c->ev_used = 0;
   c->phase_recs.clear();
-  const bool use_graph = (flags & GI_RUN_GRAPH) && !c->timing && !c->parent;
+  // a streamed dipole's copy stream is not part of a capture: eager runs
+  const bool use_graph = (flags & GI_RUN_GRAPH) && !c->timing && !c->parent && !c->streamed();
   if (P.precision == GI_PREC_SPLIT) {
     gi_status s = split_prepare(c);
     if (s != GI_OK) return s;
@@ -691,10 +692,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY);
       if (s != GI_OK) return s;
     } else {
-      GI_CUDA(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
-                return gemm_fp64_nt(c->mu(), Kp, (size_t)N * Kp, c->w_y.p, Kp, c->w_z.p, Kp,
-                                    zc, N, (int)R.ncolY, Kp, 3, c->stream);
-              }));
+      gi_status s = dipole_gemm_fp64(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY, c->stream);
+      if (s != GI_OK) return s;
     }
     fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
 
@@ -914,6 +913,7 @@ gi_status gi_destroy(gi_ctx* h) {
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   cudaStreamSynchronize(c->stream);
   split_release(c);
+  dipole_stream_release(c);
   if (c->h_lines) cudaFreeHost(c->h_lines);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
@@ -977,6 +977,7 @@ gi_status gi_set_dipole(gi_ctx* h, int N, const double* mu) {
   if (c->server) return fail(c, GI_ERR_STATE, "gi_set_dipole while serving (gi_serve_stop first)");
   cudaSetDevice(c->device);
   const int Kp = round_up(N, 64);
+  dipole_stream_release(c);
   // record order mu_c(i, f) at c*N*N + i + f*N is already "row f = mu_c(:, f)":
   // one pitched copy pads the rows to Kp (the padding is zeroed first)
   if (c->d_mu.n != (size_t)3 * N * Kp) GI_CUDA(c, c->d_mu.alloc((size_t)3 * N * Kp));
@@ -996,6 +997,7 @@ gi_status gi_set_dipole_flipped(gi_ctx* h, int N, const double* dip) {
   if (c->server) return fail(c, GI_ERR_STATE, "gi_set_dipole_flipped while serving");
   cudaSetDevice(c->device);
   const int Kp = round_up(N, 64);
+  dipole_stream_release(c);
   std::vector<double> hbuf((size_t)3 * N * Kp, 0.0);
   // dip[f + i*N + c*N*N] = mu_c(i, f); device row f holds mu_c(:, f)
   for (int comp = 0; comp < 3; comp++)
@@ -1251,8 +1253,8 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
   GI_CUDA(c, hh.alloc(bF.D));
   GI_CUDA(c, launch_build_y(v.p, ld, iv.p, 1, ndeg, bI, gammaI, ndeg, c->N, c->Kp, y.p, c->stream));
   const size_t zc = (size_t)ncol * c->Kp;
-  GI_CUDA(c, gemm_fp64_nt(c->d_mu.p, c->Kp, (size_t)c->N * c->Kp, y.p, c->Kp, z.p, c->Kp, zc, c->N,
-                          ncol, c->Kp, 3, c->stream));
+  s = dipole_gemm_fp64(c, y.p, c->Kp, z.p, c->Kp, zc, ncol, c->stream);
+  if (s != GI_OK) return s;
   GI_CUDA(c, launch_half_ls_prim(z.p + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF, dst.p,
                                  dstn.p, 6, hh.p, c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -158,9 +158,15 @@ extern "C" gi_status gi_half_ls_noalloc(gi_ctx* h, int jI, int gammaI, int ideg,
   }
   const int ncol = ndeg * bI.nslot;
   const size_t zc = (size_t)ncol * c->Kp;
-  if (e == cudaSuccess)
-    e = gemm_fp64_nt(c->d_mu.p, c->Kp, (size_t)c->N * c->Kp, Y, c->Kp, Z, c->Kp, zc, c->N, ncol,
-                     c->Kp, 3, s);
+  if (e == cudaSuccess) {
+    // a streamed dipole passes through its preallocated staging panels
+    const gi_status g = for_each_dipole_panel(c, s, [&](const double* mu, size_t ms, int rows,
+                                                         int f0) {
+      e = gemm_fp64_nt(mu, c->Kp, ms, Y, c->Kp, Z + f0, c->Kp, zc, rows, ncol, c->Kp, 3, s);
+      return e == cudaSuccess ? GI_OK : GI_ERR_CUDA;
+    });
+    if (g != GI_OK && e == cudaSuccess) return g;  // a stream/event call failed (c->err set)
+  }
   if (e == cudaSuccess)
     e = launch_half_ls_prim(Z + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF, d_st, d_stn, 6,
                             half_ls_dev, s);

@@ -324,6 +324,7 @@ gi_status gi_serve_start(gi_ctx* h, const gi_serve_config* cfg) {
   if (c->server) return fail(c, GI_ERR_STATE, "serving already started");
   if (c->nrep == 0 || !c->have_params || c->N == 0 || c->bases.empty())
     return fail(c, GI_ERR_STATE, "symmetry, parameters, dipole and bases precede gi_serve_start");
+  if (c->dstream) return fail(c, GI_ERR_STATE, "serving needs a resident dipole (gi_set_dipole)");
   cudaSetDevice(c->device);
   gi_serve_config cf{};
   if (cfg) cf = *cfg;

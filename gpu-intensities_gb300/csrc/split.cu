@@ -1071,7 +1071,9 @@ __device__ __forceinline__ uint16_t bf16_of_int(int a) {
 }
 
 // One warp per row, two elements per lane: out[p][r][k] (plane-major) and the
-// row exponent.  Rows beyond `rows` are zero; K is even.
+// row exponent.  Rows beyond `rows` are zero; K is even.  blockIdx.y selects
+// one of gridDim.y stacked operands (X + y * xstride), whose rows go to rows
+// [y * rows_pad, (y + 1) * rows_pad) of a plane set of gridDim.y * rows_pad rows.
 // Element offset of digit (plane p, row r, element k) in a [s][rows][K] plane
 // set: plain, or grouped (planes 4g..4g+3 interleaved per 16-element K slice in
 // one 4K-wide row, the s % 4 remaining planes plain after them).
@@ -1084,13 +1086,16 @@ __host__ __device__ __forceinline__ size_t digit_offset(bool grouped, int s, int
   return (size_t)4 * nq * rows * K + ((size_t)(p - 4 * nq) * rows + r) * K + k;
 }
 
-__global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, int K,
-                             int rows_pad, int s, int w, uint32_t* __restrict__ out,
+__global__ void k_slice_rows(const double* __restrict__ X, int ldx, size_t xstride, int rows,
+                             int K, int rows_pad, int s, int w, uint32_t* __restrict__ out,
                              int grouped, int32_t* __restrict__ e_out) {
   const int r = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   if (r >= rows_pad) return;
-  const double2* x2 = reinterpret_cast<const double2*>(X + (size_t)r * ldx);
+  const size_t rset = (size_t)gridDim.y * rows_pad;         // rows of the plane set
+  const size_t ro = (size_t)blockIdx.y * rows_pad + r;      // this row in the set
+  const double2* x2 =
+      reinterpret_cast<const double2*>(X + blockIdx.y * xstride + (size_t)r * ldx);
   const int K2 = K >> 1;
   unsigned long long mx = 0;
   if (r < rows)
@@ -1102,7 +1107,7 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, in
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
   const int e = row_exponent(mx);
-  if (lane == 0) e_out[r] = e;
+  if (lane == 0) e_out[ro] = e;
   const int ws = w * s;
   const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
   for (int k = lane; k < K2; k += 32) {
@@ -1118,10 +1123,10 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, int rows, in
       const long long a1 = ((X1 + half) & mask) - half;
       X0 = (X0 - a0) >> w;
       X1 = (X1 - a1) >> w;
-      out[digit_offset(grouped, s, p, r, 2 * k, K, rows_pad) >> 1] =
+      out[digit_offset(grouped, s, p, ro, 2 * k, K, rset) >> 1] =
           (uint32_t)bf16_of_int((int)a0) | ((uint32_t)bf16_of_int((int)a1) << 16);
     }
-    out[digit_offset(grouped, s, 0, r, 2 * k, K, rows_pad) >> 1] =
+    out[digit_offset(grouped, s, 0, ro, 2 * k, K, rset) >> 1] =
         (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
   }
 }
@@ -1375,12 +1380,15 @@ cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const Maps& mp, const in
 }
 
 cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s, int w,
-                  bool grouped, uint16_t* out, int32_t* e, cudaStream_t st) {
+                  bool grouped, uint16_t* out, int32_t* e, cudaStream_t st, int nstack = 1,
+                  size_t xstride = 0) {
   if (rows_pad <= 0) return cudaSuccess;
   const int wpb = 8;
-  if ((K & 1) || (grouped && (K & 15))) return cudaErrorInvalidValue;
-  k_slice_rows<<<(rows_pad + wpb - 1) / wpb, wpb * 32, 0, st>>>(
-      X, ldx, rows, K, rows_pad, s, w, reinterpret_cast<uint32_t*>(out), grouped ? 1 : 0, e);
+  if ((K & 1) || (grouped && (K & 15)) || nstack < 1 || nstack > 65535)
+    return cudaErrorInvalidValue;
+  const dim3 grid((rows_pad + wpb - 1) / wpb, nstack);
+  k_slice_rows<<<grid, wpb * 32, 0, st>>>(X, ldx, xstride, rows, K, rows_pad, s, w,
+                                          reinterpret_cast<uint32_t*>(out), grouped ? 1 : 0, e);
   return cudaGetLastError();
 }
 
@@ -1398,6 +1406,7 @@ struct SplitState {
   int s = 0, w = 0;
   bool grouped = true;                        // digit layout of every operand
   int N = -1;                                 // dipole the slices belong to
+  int panel = 0;                              // rows per panel of a streamed dipole
   DevArray<uint16_t> mu_slices;      // [s][3*Mpad][Kp]
   DevArray<int32_t> mu_exp;                   // [3*Mpad]
   int Mpad = 0;
@@ -1445,61 +1454,31 @@ gi_status split_prepare(Ctx* c) {
     return GI_OK;
   }
   const bool grouped = grouped_layout();
-  if (S->N == c->N && S->s == sh.s && S->w == sh.w && S->grouped == grouped) return GI_OK;
+  const int P = dipole_panel_rows(c);  // 0: the dipole is resident
+  if (S->N == c->N && S->s == sh.s && S->w == sh.w && S->grouped == grouped && S->panel == P)
+    return GI_OK;
   S->grouped = grouped;
-  // digit planes of the dipole: rows = 3 components x Mpad, K = Kp
   S->s = sh.s;
   S->w = sh.w;
-  S->Mpad = round_up(c->N, kBM);
+  S->panel = P;
+  // digit planes of the dipole (of one panel when streamed): rows = 3
+  // components x Mpad, K = Kp
+  S->Mpad = round_up(P ? P : c->N, kBM);
   const size_t rows = (size_t)3 * S->Mpad;
   g = check(c, S->mu_slices.alloc((size_t)sh.s * rows * c->Kp), "dipole slices");
   if (g != GI_OK) return g;
   g = check(c, S->mu_exp.alloc(rows), "dipole exponents");
   if (g != GI_OK) return g;
-  // slice all three components at once: the padded dipole is [3][N][Kp]; the
-  // planes want [3][Mpad] rows, so slice component by component into a
-  // temporary plane set and copy row blocks
-  DevArray<uint16_t> tmp;
-  DevArray<int32_t> texp;
-  g = check(c, tmp.alloc((size_t)sh.s * S->Mpad * c->Kp), "dipole slice temp");
-  if (g != GI_OK) return g;
-  g = check(c, texp.alloc(S->Mpad), "dipole exp temp");
-  if (g != GI_OK) return g;
-  // per component into tmp ([s][Mpad][Kp] planes or groups), then each
-  // group / plane block to its row range comp * Mpad of the [3 Mpad] set
-  const int nq = grouped ? sh.s / 4 : 0;
-  const size_t blk = (size_t)S->Mpad * c->Kp;  // one plane of one component
-  for (int comp = 0; comp < 3; ++comp) {
-    g = check(c,
-              slice(c->d_mu.p + (size_t)comp * c->N * c->Kp, c->Kp, c->N, c->Kp, S->Mpad, sh.s,
-                    sh.w, grouped, tmp.p, texp.p, c->stream),
-              "slice dipole");
-    if (g != GI_OK) return g;
-    for (int q = 0; q < nq; ++q) {  // groups of four planes: [q][rows][4 Kp]
-      g = check(c,
-                cudaMemcpyAsync(S->mu_slices.p + ((size_t)q * rows + (size_t)comp * S->Mpad) * 4 *
-                                                     c->Kp,
-                                tmp.p + (size_t)q * 4 * blk, sizeof(uint16_t) * 4 * blk,
-                                cudaMemcpyDeviceToDevice, c->stream),
-                "copy dipole groups");
-      if (g != GI_OK) return g;
-    }
-    for (int p = 4 * nq; p < sh.s; ++p) {  // plain planes after the groups
-      const size_t t = p - 4 * nq;
-      g = check(c,
-                cudaMemcpyAsync(S->mu_slices.p + (size_t)4 * nq * rows * c->Kp +
-                                    (t * rows + (size_t)comp * S->Mpad) * c->Kp,
-                                tmp.p + (size_t)4 * nq * blk + t * blk, sizeof(uint16_t) * blk,
-                                cudaMemcpyDeviceToDevice, c->stream),
-                "copy dipole planes");
-      if (g != GI_OK) return g;
-    }
-    g = check(c,
-              cudaMemcpyAsync(S->mu_exp.p + (size_t)comp * S->Mpad, texp.p,
-                              sizeof(int32_t) * S->Mpad, cudaMemcpyDeviceToDevice, c->stream),
-              "copy dipole exponents");
-    if (g != GI_OK) return g;
+  if (P) {  // a streamed panel is cut before its GEMM
+    S->N = c->N;
+    return GI_OK;
   }
+  // all three components in one launch: [3][N][Kp] -> the [3 Mpad]-row set
+  g = check(c,
+            slice(c->d_mu.p, c->Kp, c->N, c->Kp, S->Mpad, sh.s, sh.w, grouped, S->mu_slices.p,
+                  S->mu_exp.p, c->stream, 3, (size_t)c->N * c->Kp),
+            "slice dipole");
+  if (g != GI_OK) return g;
   g = check(c, cudaStreamSynchronize(c->stream), "slice dipole sync");
   if (g != GI_OK) return g;
   S->N = c->N;
@@ -1670,6 +1649,24 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
   if (g != GI_OK) return g;
   // algorithmic count: the true contraction length N, not the padded K
   c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * c->N * 3;
+  if (S->panel) {
+    // streamed dipole: cut each panel's digits, then its rows [f0, f0 + rows) of Z
+    return for_each_dipole_panel(c, c->stream, [&](const double* mu, size_t ms, int rows,
+                                                   int f0) -> gi_status {
+      gi_status q = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                            return slice(mu, K, rows, K, S->Mpad, S->s, S->w, S->grouped,
+                                         S->mu_slices.p, S->mu_exp.p, c->stream, 3, ms);
+                          }),
+                          "slice dipole panel");
+      if (q != GI_OK) return q;
+      timed(c, GI_PHASE_HALFLS_GEMM, [&] {
+        q = gemm(c, S->mu_slices.p, 3 * S->Mpad, S->mu_exp.p, S->Mpad, S->b_slices.p, ncol,
+                 S->b_exp.p, Z + f0, ldz, zstride, rows, ncol, K, 3);
+        return cudaSuccess;
+      });
+      return q;
+    });
+  }
   gi_status r = GI_OK;
   cudaError_t e = timed(c, GI_PHASE_HALFLS_GEMM, [&] {
     const SplitState* D = c->parent ? c->parent->split : S;  // owner of the dipole digits

@@ -693,12 +693,32 @@ gi_status gi_load_trove(gi_ctx* h, const char* dir, const gi_deck* d, int flags)
                       rep.data());
     if (st != GI_OK) return st;
   }
-  // dipole (record order)
+  // dipole (record order); kept in host memory and streamed when asked or
+  // when its padded copy would take more than half of the device (the
+  // reference splits it above 5 GiB, cuda_host.cu:858-867)
   {
-    std::vector<double> mu((size_t)3 * N * N);
-    st = read_dipole(dir, N, mu.data(), err, sizeof(err));
-    if (st != GI_OK) return fail(c, st, "%s", err);
-    st = gi_set_dipole(h, N, mu.data());
+    const size_t bytes = sizeof(double) * 3 * (size_t)N * N;
+    bool streamed = (flags & GI_TROVE_STREAM_DIPOLE) != 0;
+    size_t free_b = 0, total_b = 0;
+    cudaSetDevice(c->device);
+    if (!streamed && cudaMemGetInfo(&free_b, &total_b) == cudaSuccess &&
+        sizeof(double) * 3.0 * N * round_up(N, 64) > 0.5 * (double)total_b)
+      streamed = true;
+    if (streamed) {
+      double* pinned = nullptr;
+      GI_CUDA(c, cudaMallocHost(&pinned, bytes));
+      st = read_dipole(dir, N, pinned, err, sizeof(err));
+      if (st != GI_OK) {
+        cudaFreeHost(pinned);
+        return fail(c, st, "%s", err);
+      }
+      st = dipole_stream_adopt(c, N, pinned, 0);
+    } else {
+      std::vector<double> mu((size_t)3 * N * N);
+      st = read_dipole(dir, N, mu.data(), err, sizeof(err));
+      if (st != GI_OK) return fail(c, st, "%s", err);
+      st = gi_set_dipole(h, N, mu.data());
+    }
     if (st != GI_OK) return st;
   }
   // blocks: one row per level of every symmetry with g_ns > 0

@@ -173,6 +173,25 @@ gi_status gi_set_dipole(gi_ctx* ctx, int N, const double* mu);
    read_dipole_flipped (trove_functions.cpp:113-205): dip[f + i*N + c*N*N] =
    mu_c(i, f), i.e. FintensityJob::dipole_me. */
 gi_status gi_set_dipole_flipped(gi_ctx* ctx, int N, const double* dip);
+/* A dipole that stays in host memory (N beyond what the device should hold):
+   the split-dipole path of the reference (read_dipole_flipped_blocks,
+   trove_functions.cpp:207-310; do_1st_half_ls_blocks, cuda_host.cu:783-817;
+   chosen above max_dipole_size, cuda_host.cu:10,858-867).  mu is in
+   gi_set_dipole's record order.  Every half-line-strength contraction streams
+   it through the device in panels of `panel_rows` rows f (all three
+   components), double-buffered on a copy stream so that the copy of panel
+   p+1 overlaps the contraction of panel p; 0 picks rows for about
+   GI_DIPOLE_PANEL_BYTES of device staging.  Results are bit-identical to the
+   resident dipole's.  By default the engine keeps a pinned copy of mu; with
+   GI_DIPOLE_BORROW it page-locks and reads the caller's array instead, which
+   must then stay valid and unchanged until the dipole is replaced or the
+   context destroyed.  Runs are issued eagerly (GI_RUN_GRAPH is ignored) and
+   a streamed dipole cannot be served (gi_serve_start fails). */
+#define GI_DIPOLE_BORROW 1
+#define GI_DIPOLE_PANEL_BYTES ((size_t)4 << 30)
+gi_status gi_set_dipole_streamed(gi_ctx* ctx, int N, const double* mu, int panel_rows, int flags);
+/* Rows per panel of a streamed dipole (0: resident dipole). */
+int gi_dipole_panel_rows(const gi_ctx* ctx);
 /* The per-J contracted basis (TO_bset_contrT):
      icontr2icase[2*D]:   [r] = case, [r+D] = lambda (degenerate component)
      iroot_correlat_j0[D], k[D], ktau[D] (= 2k+tau)
@@ -298,6 +317,10 @@ gi_status gi_trove_read_levels(const char* dir, int J, int gamma, int sym_type, 
                                int32_t cap_levels, char* err, size_t err_cap);
 
 #define GI_TROVE_ALL_J 1 /* load every J in [j0, j1], not only j0 and j1 */
+/* keep the dipole in host memory and stream it (gi_set_dipole_streamed with
+   the default panel); also chosen when the padded dipole would take more than
+   half of the device's memory */
+#define GI_TROVE_STREAM_DIPOLE 2
 /* Loads a TROVE job into the context: symmetry and parameters from the deck
  * (keeping the context's precision choice), the J=0 basis, the bases of the
  * deck's J values, the dipole, and one block per (J, gamma) with g_ns > 0 holding
