@@ -195,6 +195,8 @@ def lib():
         L.gi_half_ls.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p]
         L.gi_measure_fp64_peak.argtypes = [C.c_int, f64p]
         L.gi_measure_mma_cycles.argtypes = [C.c_int, C.c_int, f64p]
+        L.gi_probe_split_gemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p,
+                                          f64p]
         L.gi_half_ls_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                          C.c_void_p, C.c_void_p, C.c_void_p]
         for name in header_functions():
@@ -220,6 +222,22 @@ def measure_mma_cycles(device: int = 0, n: int = 128) -> float:
     if st != GI_OK:
         raise GiError(st, "gi_measure_mma_cycles failed")
     return v.value
+
+
+def split_gemm(A: np.ndarray, B: np.ndarray, slices: int = 0, device: int = 0) -> np.ndarray:
+    """A @ B.T through the split-precision GEMM alone (gi_probe_split_gemm)."""
+    a = np.ascontiguousarray(A, np.float64)
+    b = np.ascontiguousarray(B, np.float64)
+    M, K = a.shape
+    N = b.shape[0]
+    if b.shape[1] != K:
+        raise ValueError("A and B must have the same number of columns")
+    out = np.empty((N, M), np.float64)
+    st = lib().gi_probe_split_gemm(device, slices, M, N, K, _p(a, f64p), _p(b, f64p),
+                                   _p(out, f64p))
+    if st != GI_OK:
+        raise GiError(st, "gi_probe_split_gemm failed")
+    return out.T
 
 
 def _p(a: np.ndarray, t):

@@ -1079,9 +1079,10 @@ static gi_status set_block(Ctx* c, int J, int gamma, int nsize, int nvec, const 
   b->nsize = nsize;
   b->nvec = nvec;
   b->ld = round_up(nsize, 64);
-  b->digits_s = 0;  // new vectors: their split-precision digits are stale
-  b->d_digits.reset();
-  b->d_digit_exp.reset();
+  // new vectors: their split-precision digits are stale (recut into the same
+  // allocation at the next run; freeing it would synchronise the device and
+  // move the addresses a captured graph reads)
+  b->digits_s = 0;
   b->energies.assign(energies, energies + nvec);
   const int nq = c->params.nmodes + 1;
   b->quanta.assign(quanta, quanta + (size_t)nvec * nq);

@@ -3,16 +3,19 @@
 // C[z][n*ldc + m] = sum_k A[z][m][k] * B[n][k] in FP64 accuracy from bf16
 // tensor-core products (an Ozaki-style error-free splitting):
 //
-//   * every row r of A (and of B) is scaled by 2^-e_r so that |x| < 1 and
+//   * every row r of A (and of B) is scaled by 2^-e_r so that |x| < 1/2 and
 //     split into s integer digits of w bits,
-//       x = sum_p a_p 2^(-w(p+1)) + tail,  a_0 in [-2^w, 2^w],
-//       a_p in [-2^(w-1), 2^(w-1)] (p >= 1), |tail| <= 2^-(ws+1),
+//       x = sum_p a_p 2^(-w(p+1)) + tail,  a_p in [-2^(w-1), 2^(w-1)],
+//       |tail| <= 2^-(ws+1),
 //     each digit an exact bf16 integer;
 //   * the products a_p * b_q with p + q = d <= s-1 share the weight 2^(-wd);
 //     each diagonal d is accumulated in its own fp32 TMEM accumulator, where
-//     sums of integer products stay exact while they stay below 2^24 (for
-//     w = 6 and K <= 2048 that holds in the worst case for d <= 5; diagonals
-//     beyond carry weights <= 2^-36 so fp32 rounding there is negligible);
+//     sums of integer products stay exact while they stay at most 2^24: a
+//     product is at most 2^(2w-2) and diagonal d has d+1 of them per k, so
+//     for w = 6 and K <= 2048 the sum is at most (d+1) 2^21, exact in the
+//     worst case for d <= 7 (the last diagonal of s = 9 carries the weight
+//     2^-48, where fp32 rounding is negligible).  Longer K runs as launches
+//     over segments of 2048, each adding its FP64 result to the previous ones';
 //   * the epilogue combines the diagonals in FP64 (Horner in 2^-w) and
 //     rescales by 2^(e_m + e_n - 2w).
 //
@@ -35,12 +38,14 @@
 #include <tuple>
 
 #include "split.h"
+#include "../../include/gi_probe.h"
 
 namespace gi {
 namespace {
 
 constexpr int kBM = 128;       // tile rows (MMA M)
 constexpr int kBK = 16;        // K elements per stage (32 bytes: SWIZZLE_32B rows)
+constexpr int kKSeg = 2048;    // K per launch: the exactness bound of the diagonal sums
 constexpr int kStages = 4;
 constexpr int kThreads = 192;  // warp 0 TMA, warp 1 MMA, warps 2..5 epilogue
 constexpr int kMaxSlices = 10;
@@ -140,6 +145,15 @@ __device__ __forceinline__ uint32_t cluster_rank() {
 __device__ __forceinline__ void cluster_sync_all() {
   asm volatile("barrier.cluster.arrive.release;\nbarrier.cluster.wait.acquire;\n" ::: "memory");
 }
+// The earlier K segments' sum at an output element (K-segmented launches).
+// A volatile load: it stays inside its branch, so launches that do not
+// accumulate never read C.
+__device__ __forceinline__ double ld_acc(const double* p) {
+  double v;
+  asm volatile("ld.global.f64 %0, [%1];\n" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+
 // v * 2^E for an integer |v| < 2^53 (so the double is exact), built from the
 // bits with integer instructions: FP64 throughput is low on this GPU and the
 // epilogues convert every output element.  Results outside the normal range
@@ -228,7 +242,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_split_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                  const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
                  int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM,
-                 int nA, int nN, int GA, int* err) {
+                 int nA, int nN, int GA, int accum, int* err) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -365,7 +379,8 @@ __global__ void __launch_bounds__(kThreads, 1)
               const int E = emr + eb[n] - 2 * w;
               const double v = scaled_int(hi[j], E - w * (kHi - 1)) +
                                scaled_int(lo[j], E - w * (S - 1));
-              Cz[(size_t)n * ldc + m] = v;
+              double* dst = Cz + (size_t)n * ldc + m;
+              *dst = accum ? ld_acc(dst) + v : v;
             }
           }
         }
@@ -401,7 +416,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_split_gemm2(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
                   int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
-                  int nN, int GA, int* err) {
+                  int nN, int GA, int accum, int* err) {
   static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
@@ -545,7 +560,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
               double* dst = Cz + (size_t)n * ldc + m;
               const double part = scaled_int(v[j], E);
-              *dst = pass ? *dst + part : part;
+              *dst = (pass || accum) ? *dst + part : part;
             }
           }
         }
@@ -580,7 +595,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     k_split_gemm3(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                   const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
                   int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
-                  int nN, int GAc, int* err) {
+                  int nN, int GAc, int accum, int* err) {
   static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
   static_assert(CM * CN >= 2 && CM * CN <= 8, "portable cluster size");
   constexpr int CS = CM * CN;
@@ -730,7 +745,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
               double* dst = Cz + (size_t)n * ldc + m;
               const double part = scaled_int(v[j], E);
-              *dst = pass ? *dst + part : part;
+              *dst = (pass || accum) ? *dst + part : part;
             }
           }
         }
@@ -787,7 +802,9 @@ __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;\n" ::: "memory");
 }
 
-template <int S, int BN, int D1>
+// ACC: add to C (the later launches of a K-segmented GEMM); a template
+// argument, so the first launch's code carries no trace of it.
+template <int S, int BN, int D1, bool ACC>
 __global__ void __launch_bounds__(kThreadsG, 1)
     k_split_gemm_g(const __grid_constant__ CUtensorMap tmAq, const __grid_constant__ CUtensorMap tmAt,
                    const __grid_constant__ CUtensorMap tmBq, const __grid_constant__ CUtensorMap tmBt,
@@ -1015,7 +1032,9 @@ __global__ void __launch_bounds__(kThreadsG, 1)
               double out = scaled_int(v[j], base - w * (d1 - 1));
               if (NPASS == 2) out = scaled_int(v0[ch][j], base - w * (D1 - 1)) + out;
               else out = scaled_int(hi[j], base - w * (SPLIT - 1)) + out;
-              Cz[(size_t)n * ldc + m] = out;
+              double* dst = Cz + (size_t)n * ldc + m;
+              if constexpr (ACC) out += ld_acc(dst);
+              *dst = out;
             }
           }
         }
@@ -1036,11 +1055,11 @@ __global__ void __launch_bounds__(kThreadsG, 1)
 
 // ------------------------------------------------------------------ slicing
 // FP64 arithmetic is scarce on this GPU, so the digits are cut with integer
-// operations on the bit pattern.  For a row with exponent e (max|x| < 2^e),
+// operations on the bit pattern.  For a row with exponent e (max|x| < 2^(e-1)),
 // each element becomes the fixed-point integer X = round(x 2^(ws - e)),
-// |X| < 2^(ws), and X is split from the bottom into balanced base-2^w digits:
-// a_p in [-2^(w-1), 2^(w-1)) for p >= 1 and the remaining top digit
-// |a_0| <= 2^w, so X = sum_p a_p 2^(w(s-1-p)) exactly.
+// |X| <= 2^(ws-1), and X is split from the bottom into balanced base-2^w
+// digits: a_p in [-2^(w-1), 2^(w-1)) for p >= 1 and the remaining top digit
+// |a_0| <= 2^(w-1), so X = sum_p a_p 2^(w(s-1-p)) exactly.
 
 // Row exponent from the largest magnitude's bit pattern: 2^(e-1) <= max < 2^e.
 __device__ __forceinline__ int row_exponent(unsigned long long maxbits) {
@@ -1106,7 +1125,7 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, size_t xstri
     }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int e = row_exponent(mx);
+  const int e = row_exponent(mx) + 1;  // |x| < 2^(e-1): every digit within 2^(w-1)
   if (lane == 0) e_out[ro] = e;
   const int ws = w * s;
   const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
@@ -1151,12 +1170,14 @@ EncodeTiledFn encode_fn() {
 }
 
 // 3-D map over digit planes [s][rows][K] of bf16 with a (16, box_rows, box_planes) box.
+// K elements of each row starting at base, rows ldk elements apart (a K
+// segment of longer rows when ldk > K).
 bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int box_rows,
-              int box_planes) {
+              int box_planes, int ldk) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)s};
-  cuuint64_t strides[2] = {(cuuint64_t)K * 2, (cuuint64_t)K * rows * 2};
+  cuuint64_t strides[2] = {(cuuint64_t)ldk * 2, (cuuint64_t)ldk * rows * 2};
   cuuint32_t box[3] = {(cuuint32_t)kBK, (cuuint32_t)box_rows, (cuuint32_t)box_planes};
   cuuint32_t es[3] = {1, 1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
@@ -1167,11 +1188,12 @@ bool make_map(CUtensorMap* map, const void* base, int K, int rows, int s, int bo
 // 3-D map over the grouped layout's four-plane groups [nq][rows][4K]: a box is
 // the 64 elements (four planes x 16) of one K slice for box_rows rows, in
 // 128-byte rows with the 128-byte swizzle.
-bool make_map_groups(CUtensorMap* map, const void* base, int K, int rows, int nq, int box_rows) {
+bool make_map_groups(CUtensorMap* map, const void* base, int K, int rows, int nq, int box_rows,
+                     int ldk) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[3] = {(cuuint64_t)K * 4, (cuuint64_t)rows, (cuuint64_t)nq};
-  cuuint64_t strides[2] = {(cuuint64_t)K * 8, (cuuint64_t)K * rows * 8};
+  cuuint64_t strides[2] = {(cuuint64_t)ldk * 8, (cuuint64_t)ldk * rows * 8};
   cuuint32_t box[3] = {64, (cuuint32_t)box_rows, 1};
   cuuint32_t es[3] = {1, 1, 1};
   return fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(base), dims, strides, box,
@@ -1235,6 +1257,14 @@ SplitShape shape_of(const Ctx* c) {
 
 // Dynamic shared memory above 48 KB must be enabled per kernel, once, before
 // the first launch (and before any graph capture).
+template <class F>
+cudaError_t set_smem(F a, size_t bytes, F b) {
+  cudaError_t e = cudaFuncSetAttribute(a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  return e != cudaSuccess ? e
+                          : cudaFuncSetAttribute(b, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)bytes);
+}
+
 template <int S>
 cudaError_t set_attributes() {
   constexpr int BN1 = bn_for(S), BN2 = bn2_of(S), D1 = d1_of(S);
@@ -1254,17 +1284,11 @@ cudaError_t set_attributes() {
                                     (int)smem2_bytes(S, BN2));
     if constexpr (S >= 4) {
       if (status == cudaSuccess)
-        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN2, D1>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smemg_bytes(S, BN2));
+        status = set_smem(k_split_gemm_g<S, BN2, D1, false>, smemg_bytes(S, BN2), k_split_gemm_g<S, BN2, D1, true>);
       if (status == cudaSuccess && d1b_of(S) != D1)
-        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN2, d1b_of(S)>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smemg_bytes(S, BN2));
+        status = set_smem(k_split_gemm_g<S, BN2, d1b_of(S), false>, smemg_bytes(S, BN2), k_split_gemm_g<S, BN2, d1b_of(S), true>);
       if (status == cudaSuccess)
-        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN1, S>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smemg_bytes(S, BN1));
+        status = set_smem(k_split_gemm_g<S, BN1, S, false>, smemg_bytes(S, BN1), k_split_gemm_g<S, BN1, S, true>);
       constexpr int DC = d1c_of(S);
       if (status == cudaSuccess)
         status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 1>,
@@ -1296,7 +1320,8 @@ cudaError_t kernel_attributes(int s) {
 template <int S>
 cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea,
                         const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
-                        int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
+                        int Nc, int K, int batch, int w, int accum, int* err,
+                        cudaStream_t st) {
   const CUtensorMap& tA = mp.a;
   const CUtensorMap& tB = mp.b;
   const bool one = cfg.kind == 0 || cfg.kind == 8;
@@ -1314,15 +1339,15 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
     if (cfg.kind >= 6 && cfg.kind <= 8) {
       const int grid = nA * nN;
       if (cfg.kind == 8)
-        k_split_gemm_g<S, BN1, S><<<grid, kThreadsG, sm, st>>>(
+        (accum ? k_split_gemm_g<S, BN1, S, true> : k_split_gemm_g<S, BN1, S, false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       else if (cfg.kind == 7 && d1b_of(S) != D1)
-        k_split_gemm_g<S, BN2, d1b_of(S)><<<grid, kThreadsG, sm, st>>>(
+        (accum ? k_split_gemm_g<S, BN2, d1b_of(S), true> : k_split_gemm_g<S, BN2, d1b_of(S), false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       else
-        k_split_gemm_g<S, BN2, D1><<<grid, kThreadsG, sm, st>>>(
+        (accum ? k_split_gemm_g<S, BN2, D1, true> : k_split_gemm_g<S, BN2, D1, false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       return cudaGetLastError();
@@ -1346,33 +1371,35 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
       constexpr int DC = d1c_of(S);
       if (cfg.kind == 3)
         return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 2, 1>, tA, tB, ea, eb, C, ldc,
-                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, err);
+                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, accum, err);
       if (cfg.kind == 4)
         return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 1, 2>, tA, tB, ea, eb, C, ldc,
-                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, err);
+                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, accum, err);
       return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 2, 2>, tA, tB, ea, eb, C, ldc,
-                                strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, err);
+                                strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, accum, err);
     }
   }
   if (one)
     k_split_gemm<S, BN1><<<nA * nN, kThreads, sm, st>>>(
-        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
+        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, accum, err);
   else if (cfg.kind == 2 && d1b_of(S) != D1)
     k_split_gemm2<S, BN2, d1b_of(S)><<<nA * nN, kThreads, sm, st>>>(
-        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
+        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, accum, err);
   else
     k_split_gemm2<S, BN2, D1><<<nA * nN, kThreads, sm, st>>>(
-        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, err);
+        tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, accum, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const Maps& mp, const int32_t* ea,
                           const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
-                          int Nc, int K, int batch, int w, int* err, cudaStream_t st) {
+                          int Nc, int K, int batch, int w, int accum, int* err,
+                        cudaStream_t st) {
   switch (s) {
 #define GI_S(SS)                                                                                \
   case SS:                                                                                      \
-    return launch_gemm<SS>(cfg, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, err, st);
+    return launch_gemm<SS>(cfg, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, accum, err, \
+                            st);
     GI_S(2) GI_S(3) GI_S(4) GI_S(5) GI_S(6) GI_S(7) GI_S(8) GI_S(9) GI_S(10)
 #undef GI_S
   }
@@ -1465,10 +1492,14 @@ gi_status split_prepare(Ctx* c) {
   // components x Mpad, K = Kp
   S->Mpad = round_up(P ? P : c->N, kBM);
   const size_t rows = (size_t)3 * S->Mpad;
-  g = check(c, S->mu_slices.alloc((size_t)sh.s * rows * c->Kp), "dipole slices");
-  if (g != GI_OK) return g;
-  g = check(c, S->mu_exp.alloc(rows), "dipole exponents");
-  if (g != GI_OK) return g;
+  if (S->mu_slices.n != (size_t)sh.s * rows * c->Kp) {  // same shape: recut in place
+    g = check(c, S->mu_slices.alloc((size_t)sh.s * rows * c->Kp), "dipole slices");
+    if (g != GI_OK) return g;
+  }
+  if (S->mu_exp.n != rows) {
+    g = check(c, S->mu_exp.alloc(rows), "dipole exponents");
+    if (g != GI_OK) return g;
+  }
   if (P) {  // a streamed panel is cut before its GEMM
     S->N = c->N;
     return GI_OK;
@@ -1551,32 +1582,44 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
                       double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch) {
   SplitState* S = state(c);
   const bool grouped = S->grouped && S->s >= 4;
+  // K runs in segments of at most kKSeg, each a launch whose FP64 results
+  // the next adds to: within a segment every diagonal sum that carries weight
+  // stays an exact fp32 integer (the bound in the header); the segments are
+  // summed in FP64.
+  const int nseg = (K + kKSeg - 1) / kKSeg;
+  c->stats.kernel_launches += nseg - 1;
   auto run = [&](const GemmConfig& g) -> cudaError_t {
-    Maps mp;
     const int bn = tile_n(S->s, g.kind);
-    if (grouped) {
-      const int nq = S->s / 4, nt = S->s % 4;
-      const uint16_t* At = Aslices + (size_t)4 * nq * Arows_total * K;
-      const uint16_t* Bt = Bslices + (size_t)4 * nq * Brows * K;
-      if (!make_map_groups(&mp.a, Aslices, K, Arows_total, nq, kBM) ||
-          !make_map_groups(&mp.b, Bslices, K, Brows, nq, bn))
-        return cudaErrorInvalidValue;
-      if (nt) {
-        if (!make_map(&mp.at, At, K, Arows_total, nt, kBM, 1) ||
-            !make_map(&mp.bt, Bt, K, Brows, nt, bn, 1))
+    for (int k0 = 0; k0 < K; k0 += kKSeg) {
+      const int Kc = std::min(kKSeg, K - k0);
+      Maps mp;
+      if (grouped) {
+        // a K segment of the grouped rows starts 4 * k0 elements in (k0 % 16 == 0)
+        const int nq = S->s / 4, nt = S->s % 4;
+        const uint16_t* At = Aslices + (size_t)4 * nq * Arows_total * K + k0;
+        const uint16_t* Bt = Bslices + (size_t)4 * nq * Brows * K + k0;
+        if (!make_map_groups(&mp.a, Aslices + (size_t)4 * k0, Kc, Arows_total, nq, kBM, K) ||
+            !make_map_groups(&mp.b, Bslices + (size_t)4 * k0, Kc, Brows, nq, bn, K))
           return cudaErrorInvalidValue;
+        if (nt) {
+          if (!make_map(&mp.at, At, Kc, Arows_total, nt, kBM, 1, K) ||
+              !make_map(&mp.bt, Bt, Kc, Brows, nt, bn, 1, K))
+            return cudaErrorInvalidValue;
+        } else {
+          mp.at = mp.a;  // no plain planes: never read
+          mp.bt = mp.b;
+        }
       } else {
-        mp.at = mp.a;  // no plain planes: never read
-        mp.bt = mp.b;
+        const int planes = g.kind == 0 ? S->s : 1;  // the two-pass kernels load plane by plane
+        if (!make_map(&mp.a, Aslices + k0, Kc, Arows_total, S->s, kBM, planes, K) ||
+            !make_map(&mp.b, Bslices + k0, Kc, Brows, S->s, bn, planes, K))
+          return cudaErrorInvalidValue;
       }
-    } else {
-      const int planes = g.kind == 0 ? S->s : 1;  // the two-pass kernels load plane by plane
-      if (!make_map(&mp.a, Aslices, K, Arows_total, S->s, kBM, planes) ||
-          !make_map(&mp.b, Bslices, K, Brows, S->s, bn, planes))
-        return cudaErrorInvalidValue;
+      const cudaError_t e = launch_gemm_s(S->s, g, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, Kc,
+                                          batch, S->w, k0 > 0, S->err.p, c->stream);
+      if (e != cudaSuccess) return e;
     }
-    return launch_gemm_s(S->s, g, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, S->w,
-                         S->err.p, c->stream);
+    return cudaSuccess;
   };
   const TuneKey key{S->s, ((M + kBM - 1) / kBM) * batch, col_bucket(Nc), K, (int)grouped};
   GemmConfig cfg = default_config(S->s, grouped);
@@ -1688,10 +1731,15 @@ static gi_status block_digits(Ctx* c, Block& fb, int K, bool wait) {
   gi_status g;
   std::lock_guard<std::mutex> lk(c->mmu());
   if (fb.digits_s != S->s || fb.digits_w != S->w || fb.digits_layout != (int)S->grouped) {
-    g = check(c, fb.d_digits.alloc((size_t)S->s * vpad * K), "V digits");
-    if (g != GI_OK) return g;
-    g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
-    if (g != GI_OK) return g;
+    const size_t nd = (size_t)S->s * vpad * K;  // same shape: recut in place
+    if (fb.d_digits.n != nd) {
+      g = check(c, fb.d_digits.alloc(nd), "V digits");
+      if (g != GI_OK) return g;
+    }
+    if (fb.d_digit_exp.n != (size_t)vpad) {
+      g = check(c, fb.d_digit_exp.alloc(vpad), "V exponents");
+      if (g != GI_OK) return g;
+    }
     g = check(c, timed(c, GI_PHASE_SLICE, [&] {
                 return slice(fb.d_vecs.p, fb.ld, nvec, K, vpad, S->s, S->w, S->grouped, fb.d_digits.p,
                              fb.d_digit_exp.p, c->stream);
@@ -1802,3 +1850,60 @@ void split_release(Ctx* c) {
 }
 
 }  // namespace gi
+
+extern "C" gi_status gi_probe_split_gemm(int device, int slices, int M, int N, int K,
+                                          const double* A, const double* B, double* C) {
+  using namespace gi;
+  if (M <= 0 || N <= 0 || K <= 0 || !A || !B || !C) return GI_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return GI_ERR_CUDA;
+  if (!encode_fn()) return GI_ERR_CUDA;
+  Ctx c;
+  c.device = device;
+  c.params.split_slices = slices;
+  if (cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking) != cudaSuccess)
+    return GI_ERR_CUDA;
+  SplitState* S = state(&c);
+  const SplitShape sh = shape_of(&c);
+  S->s = sh.s;
+  S->w = sh.w;
+  S->grouped = grouped_layout();
+  const int Kp = round_up(K, 64), Mpad = round_up(M, kBM);
+  DevArray<double> dA, dB, dC;
+  DevArray<uint16_t> sa, sb;
+  DevArray<int32_t> xa, xb;
+  gi_status g = GI_OK;
+  auto ck = [&](cudaError_t e) {
+    if (g == GI_OK && e != cudaSuccess)
+      g = e == cudaErrorMemoryAllocation ? GI_ERR_NOMEM : GI_ERR_CUDA;
+  };
+  ck(dA.alloc((size_t)M * Kp));
+  ck(dB.alloc((size_t)N * Kp));
+  ck(dC.alloc((size_t)N * M));
+  ck(sa.alloc((size_t)S->s * Mpad * Kp));
+  ck(sb.alloc((size_t)S->s * N * Kp));
+  ck(xa.alloc(Mpad));
+  ck(xb.alloc(N));
+  ck(S->err.reserve(1));
+  if (g == GI_OK) {
+    ck(cudaMemset(dA.p, 0, sizeof(double) * dA.n));
+    ck(cudaMemset(dB.p, 0, sizeof(double) * dB.n));
+    ck(cudaMemset(S->err.p, 0, sizeof(int)));
+    ck(cudaMemcpy2D(dA.p, sizeof(double) * Kp, A, sizeof(double) * K, sizeof(double) * K, M,
+                    cudaMemcpyHostToDevice));
+    ck(cudaMemcpy2D(dB.p, sizeof(double) * Kp, B, sizeof(double) * K, sizeof(double) * K, N,
+                    cudaMemcpyHostToDevice));
+    ck(cudaDeviceSynchronize());
+  }
+  if (g == GI_OK) {
+    ck(slice(dA.p, Kp, M, Kp, Mpad, S->s, S->w, S->grouped, sa.p, xa.p, c.stream));
+    ck(slice(dB.p, Kp, N, Kp, N, S->s, S->w, S->grouped, sb.p, xb.p, c.stream));
+  }
+  if (g == GI_OK) g = gemm(&c, sa.p, Mpad, xa.p, Mpad, sb.p, N, xb.p, dC.p, M, 0, M, N, Kp, 1);
+  if (g == GI_OK) ck(cudaStreamSynchronize(c.stream));
+  if (g == GI_OK) g = split_check(&c);
+  if (g == GI_OK) ck(cudaMemcpy(C, dC.p, sizeof(double) * N * M, cudaMemcpyDeviceToHost));
+  cudaStreamSynchronize(c.stream);
+  split_release(&c);
+  cudaStreamDestroy(c.stream);
+  return g;
+}

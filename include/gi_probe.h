@@ -20,6 +20,12 @@ gi_status gi_measure_fp64_peak(int device, double* tflops);
    n in {32, 48, 64, 96, 128, 256}, issued back to back on every SM; the
    split-precision tile shapes follow from this rate. */
 gi_status gi_measure_mma_cycles(int device, int n, double* cycles);
+/* The split-precision GEMM alone on host arrays, for tests on arbitrary
+   operands: C[n*M + m] = sum_k A[m*K + k] * B[n*K + k] with `slices` bf16
+   digits per operand (0: the engine's default), on the kernel that the
+   engine's tuner table or GI_SPLIT_FORCE selects for the shape. */
+gi_status gi_probe_split_gemm(int device, int slices, int M, int N, int K, const double* A,
+                              const double* B, double* C);
 #ifdef __cplusplus
 }
 #endif
