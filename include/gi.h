@@ -11,7 +11,8 @@
  *   - Every call returns a gi_status; nothing exits the process.  The text of
  *     the last failure is available from gi_last_error().
  *   - All buffers are caller-owned; setters copy what they need (to device
- *     memory) before returning, so the caller may free its arrays afterwards.
+ *     memory) before returning, so the caller may free its arrays afterwards
+ *     (except a dipole passed with GI_DIPOLE_BORROW).
  *   - A context is used from one host thread at a time.
  *   - Indices are 0-based unless stated.  Symmetry indices gamma follow the
  *     reference's order for the group (e.g. C2V(M): A1, A2, B1, B2).
@@ -23,6 +24,8 @@
  *   gi_set_params          read_intensities / read_fields (fields.cpp:145-282)
  *   gi_set_dipole(_flipped) read_dipole_flipped + its upload
  *                          (trove_functions.cpp:113-205, cuda_host.cu:983)
+ *   gi_set_dipole_streamed read_dipole_flipped_blocks + do_1st_half_ls_blocks
+ *                          (trove_functions.cpp:207-310; cuda_host.cu:783-817)
  *   gi_set_basis           bset_contr_factory + correlate_index +
  *                          compute_ijterms + copy_bset_contr_to_gpu
  *                          (trove_functions.cpp:401-858, 927-966; cuda_host.cu:186-366)
