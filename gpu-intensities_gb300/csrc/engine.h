@@ -210,6 +210,14 @@ struct Ctx {
     return ev_pool[ev_used++];
   }
 
+  // Line read-back overlapped with the run: after each final block's
+  // epilogues the line count goes to ck_count[k] and ck_ev[k] is recorded; the
+  // host copies every finished stretch of lines on d2h while later blocks run
+  std::vector<cudaEvent_t> ck_ev;
+  unsigned long long* ck_count = nullptr;  // pinned
+  size_t ck_cap = 0;
+  cudaStream_t d2h = nullptr;
+
   // CUDA graph of the last captured launch sequence (GI_RUN_GRAPH) and the
   // plan it was captured for
   cudaGraphExec_t gexec = nullptr;
@@ -264,6 +272,9 @@ gi_status server_make_room(Ctx* c, size_t bytes, Block* keep);
 // Stops the serving loop of c (if any): fails queued jobs, joins the workers.
 gi_status server_stop(Ctx* c);
 void trove_meta_release(Ctx* c);
+// Frees a context's streams, events, pinned buffers and split state, then
+// the context itself (its device arrays go with it).
+void ctx_release(Ctx* c);
 
 // The dipole in panels of rows f: fn(panel, component stride, rows, f0) is
 // called in order, with stream `st` ordered after the panel's [3][rows][Kp]

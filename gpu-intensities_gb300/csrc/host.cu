@@ -629,6 +629,37 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     if (s != GI_OK) return s;
   }
 
+  // checkpoints of the line count (one per final block of every round) and,
+  // when the lines go to host memory, a pinned buffer for all of them, so that
+  // finished stretches can be copied while the run goes on (skipped when the
+  // capacity bound would pin more than 16 GiB: then the copy follows the run)
+  size_t nck = 0;
+  for (size_t r = 0; r < rounds.size(); r++)
+    if (!rounds[r].units.empty()) nck += targets[r].size();
+  if (c->ck_cap < nck) {
+    if (c->ck_count) cudaFreeHost(c->ck_count);
+    c->ck_count = nullptr;
+    c->ck_cap = 0;
+    GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->ck_count),
+                              sizeof(unsigned long long) * nck));
+    c->ck_cap = nck;
+  }
+  while (c->ck_ev.size() < nck) {
+    cudaEvent_t e = nullptr;
+    GI_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    c->ck_ev.push_back(e);
+  }
+  if (!c->d2h) GI_CUDA(c, cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking));
+  const size_t cap_lines = c->d_lines.n;
+  const bool overlap_d2h = !c->lines_on_device && cap_lines * sizeof(gi_line) <= ((size_t)16 << 30);
+  if (overlap_d2h && c->h_lines_cap < cap_lines) {
+    if (c->h_lines) cudaFreeHost(c->h_lines);
+    c->h_lines = nullptr;
+    c->h_lines_cap = 0;
+    GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_lines), sizeof(gi_line) * cap_lines));
+    c->h_lines_cap = cap_lines;
+  }
+
   // The plan's identity for graph replay: every pointer, size and value the
   // launch sequence passes to a kernel follows from these.
   uint64_t sig = 1469598103934665603ull;
@@ -646,6 +677,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
                     (void*)c->d_lines.p})
       mixv(q);
     mixv(c->d_lines.n);
+    mixv(c->ck_count);
     if (P.precision == GI_PREC_SPLIT) mixv(split_identity(c));
     for (size_t r = 0; r < rounds.size(); r++) {
       mixv(rounds[r].ncolY);
@@ -673,7 +705,9 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   int64_t npairs_checked = 0;
 
   // the launch sequence of the job, issued eagerly or under stream capture
+  bool capturing = false;
   auto issue = [&]() -> gi_status {
+  size_t ck = 0;
   for (size_t r = 0; r < rounds.size(); r++) {
     const Round& R = rounds[r];
     if (R.units.empty()) continue;
@@ -758,6 +792,12 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
                 }));
         npairs_checked += (int64_t)u.nI * Fp.nupper;
       }
+      // checkpoint: every line of this final block is written once this fires
+      GI_CUDA(c, cudaMemcpyAsync(c->ck_count + ck, c->w_counter.p, sizeof(unsigned long long),
+                                 cudaMemcpyDeviceToHost, c->stream));
+      GI_CUDA(c, cudaEventRecordWithFlags(c->ck_ev[ck], c->stream,
+                                          capturing ? cudaEventRecordExternal : 0));
+      ck++;
     }
   }
   return GI_OK;
@@ -789,7 +829,9 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     c->gsig = 0;
     const gi_stats pre = c->stats;
     GI_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+    capturing = true;
     gi_status st = issue();
+    capturing = false;
     cudaGraph_t graph = nullptr;
     const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
     if (st != GI_OK) {
@@ -816,6 +858,19 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     if (st != GI_OK) return st;
   }
   GI_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  // copy each finished stretch of lines while the rest of the run goes on
+  unsigned long long copied = 0;
+  if (overlap_d2h) {
+    for (size_t k = 0; k < nck; k++) {
+      GI_CUDA(c, cudaEventSynchronize(c->ck_ev[k]));
+      const unsigned long long n = std::min<unsigned long long>(c->ck_count[k], cap_lines);
+      if (n > copied) {
+        GI_CUDA(c, cudaMemcpyAsync(c->h_lines + copied, c->d_lines.p + copied,
+                                   sizeof(gi_line) * (n - copied), cudaMemcpyDeviceToHost, c->d2h));
+        copied = n;
+      }
+    }
+  }
   unsigned long long counts[2] = {0, 0};
   GI_CUDA(c, cudaMemcpyAsync(counts, c->w_counter.p, sizeof(counts), cudaMemcpyDeviceToHost, c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -826,7 +881,13 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   const unsigned long long count = counts[0];
   if (count > c->d_lines.n) return fail(c, GI_ERR_DEVICE, "line buffer overflow (%llu lines)", count);
   c->nlines = (int64_t)count;
-  if (!c->lines_on_device && count) {
+  if (overlap_d2h) {
+    if (count > copied)
+      GI_CUDA(c, cudaMemcpyAsync(c->h_lines + copied, c->d_lines.p + copied,
+                                 sizeof(gi_line) * (count - copied), cudaMemcpyDeviceToHost,
+                                 c->d2h));
+    GI_CUDA(c, cudaStreamSynchronize(c->d2h));
+  } else if (!c->lines_on_device && count) {
     if (c->h_lines_cap < count) {
       if (c->h_lines) cudaFreeHost(c->h_lines);
       c->h_lines = nullptr;
@@ -859,6 +920,23 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   *nlines_out = c->nlines;
   return GI_OK;
+}
+
+void ctx_release(Ctx* c) {
+  cudaStreamSynchronize(c->stream);
+  split_release(c);
+  if (c->h_lines) cudaFreeHost(c->h_lines);
+  if (c->d2h) {
+    cudaStreamSynchronize(c->d2h);
+    cudaStreamDestroy(c->d2h);
+  }
+  for (cudaEvent_t e : c->ck_ev) cudaEventDestroy(e);
+  if (c->ck_count) cudaFreeHost(c->ck_count);
+  for (cudaEvent_t e : c->ev_pool) cudaEventDestroy(e);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->own_stream) cudaStreamDestroy(c->own_stream);
+  delete c;
 }
 
 }  // namespace gi
@@ -912,13 +990,8 @@ gi_status gi_destroy(gi_ctx* h) {
   trove_meta_release(c);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   cudaStreamSynchronize(c->stream);
-  split_release(c);
   dipole_stream_release(c);
-  if (c->h_lines) cudaFreeHost(c->h_lines);
-  if (c->ev0) cudaEventDestroy(c->ev0);
-  if (c->ev1) cudaEventDestroy(c->ev1);
-  if (c->own_stream) cudaStreamDestroy(c->own_stream);
-  delete c;
+  ctx_release(c);
   return GI_OK;
 }
 

@@ -274,16 +274,7 @@ static Ctx* make_worker(Ctx* c, size_t slot_ws) {
   return w;
 }
 
-static void destroy_worker(Ctx* w) {
-  cudaStreamSynchronize(w->stream);
-  split_release(w);
-  if (w->h_lines) cudaFreeHost(w->h_lines);
-  for (cudaEvent_t e : w->ev_pool) cudaEventDestroy(e);
-  if (w->ev0) cudaEventDestroy(w->ev0);
-  if (w->ev1) cudaEventDestroy(w->ev1);
-  if (w->own_stream) cudaStreamDestroy(w->own_stream);
-  delete w;
-}
+static void destroy_worker(Ctx* w) { ctx_release(w); }
 
 static double pct(std::vector<double> v, double q) {
   if (v.empty()) return 0.0;

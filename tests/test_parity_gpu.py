@@ -156,3 +156,20 @@ def test_graph_replay_matches_eager(pkg, synth, precision):
         eager3, _ = lines(eng)
         g3, _ = lines(eng, graph=True)
         assert np.array_equal(g3, eager3)
+
+
+@pytest.mark.parametrize("budget", [0, 48 << 20])
+def test_host_readback_equals_device_lines(pkg, synth, budget):
+    """Lines read back to host memory while the run goes on (a copy per final
+    block, after its epilogues) equal the device-resident lines, eager and
+    replayed, in one round or many (a small HBM budget)."""
+    prob = synth.make_c3v(42, 40, [0, 1, 2, 3], nvec_max=12)
+    with pkg.Engine(0, hbm_budget=budget) as eng:
+        eng.load(prob, precision=1)
+        eng.run(lines_on_device=True)
+        ref = np.sort(eng.lines(), order=["level_i", "level_f"])
+        assert len(ref) > 500
+        for graph in (False, True, True):
+            n = eng.run(lines_on_device=False, graph=graph)
+            assert n == len(ref)
+            assert np.array_equal(np.sort(eng.lines(), order=["level_i", "level_f"]), ref)
