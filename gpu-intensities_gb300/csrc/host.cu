@@ -573,6 +573,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     std::vector<std::pair<const Unit*, PairPlan*>> parts;
     std::vector<size_t> hcol;
     size_t ncolH = 0;
+    size_t hoff = 0, toff = 0;  // H and T of this block within its group's workspace
   };
   std::vector<std::vector<Target>> targets(rounds.size());
   size_t max_y = 1, max_h = 1, max_t = 1;
@@ -584,7 +585,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         auto it = idx.find(pp->F);
         if (it == idx.end()) {
           idx[pp->F] = targets[r].size();
-          targets[r].push_back(Target{pp->F, {}, {}, 0});
+          targets[r].push_back(Target{pp->F, {}, {}, 0, 0, 0});
           it = idx.find(pp->F);
         }
         Target& T = targets[r][it->second];
@@ -602,30 +603,62 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   DevArray<double>& d_EI = c->w_EI;
   GI_CUDA(c, c->w_y.reserve(max_y));
   GI_CUDA(c, c->w_z.reserve(3 * max_y));
-  GI_CUDA(c, c->w_h.reserve(max_h));
-  GI_CUDA(c, c->w_t.reserve(max_t));
   c->stats = gi_stats{};
   c->timing = (flags & GI_RUN_PHASE_TIMING) != 0;
   c->ev_used = 0;
   c->phase_recs.clear();
   // a streamed dipole's copy stream is not part of a capture: eager runs
   const bool use_graph = (flags & GI_RUN_GRAPH) && !c->timing && !c->parent && !c->streamed();
+  bool grouped_final = false;
   if (P.precision == GI_PREC_SPLIT) {
     gi_status s = split_prepare(c);
     if (s != GI_OK) return s;
+    grouped_final = split_grouped_final(c);
+  }
+  // Final blocks go through the final-state GEMM in groups: with the persistent
+  // grouped launch, consecutive blocks of a round until the group has work for
+  // ~16 waves of the GPU (and at most the launch's problem count), so the lines
+  // of a group are read back while the next one computes; otherwise one block
+  // per group.  A group's H and T live side by side in the workspaces.
+  std::vector<std::vector<std::pair<size_t, size_t>>> groups(rounds.size());
+  size_t max_gh = 1, max_gcols = 1;  // the largest group's H elements and columns
+  max_h = max_t = 1;
+  for (size_t r = 0; r < rounds.size(); r++) {
+    size_t t0 = 0, items = 0, hs = 0, ts = 0, cols = 0;
+    for (size_t t = 0; t < targets[r].size(); t++) {
+      Target& T = targets[r][t];
+      T.hoff = hs;
+      T.toff = ts;
+      hs += T.ncolH * T.F->blk->ld;
+      ts += T.ncolH * round_up(T.F->blk->nvec, 2);
+      cols += T.ncolH;
+      items += grouped_final ? split_grouped_items(T.F->blk->nvec, (int)T.ncolH) : 0;
+      const bool close = !grouped_final || t + 1 == targets[r].size() ||
+                         items >= (size_t)16 * std::max(c->nsm, 1) ||
+                         (int)(t + 1 - t0) == split_grouped_max_jobs();
+      if (close) {
+        groups[r].push_back({t0, t + 1});
+        max_h = std::max(max_h, hs);
+        max_t = std::max(max_t, ts);
+        max_gh = std::max(max_gh, hs);
+        max_gcols = std::max(max_gcols, cols);
+        t0 = t + 1;
+        items = hs = ts = cols = 0;
+      }
+    }
+  }
+  GI_CUDA(c, c->w_h.reserve(max_h));
+  GI_CUDA(c, c->w_t.reserve(max_t));
+  if (P.precision == GI_PREC_SPLIT) {
     // every allocation of the launch sequence happens here, before it
-    size_t max_b = 1, max_cols = 1;
+    size_t max_b = max_gh, max_cols = max_gcols;
     std::vector<Block*> finals;
     for (size_t r = 0; r < rounds.size(); r++) {
       max_b = std::max(max_b, rounds[r].ncolY * Kp);
       max_cols = std::max(max_cols, rounds[r].ncolY);
-      for (const Target& T : targets[r]) {
-        max_b = std::max(max_b, T.ncolH * T.F->blk->ld);
-        max_cols = std::max(max_cols, T.ncolH);
-        finals.push_back(T.F->blk);
-      }
+      for (const Target& T : targets[r]) finals.push_back(T.F->blk);
     }
-    s = split_reserve(c, max_b, max_cols, finals);
+    gi_status s = split_reserve(c, max_b, max_cols, finals);
     if (s != GI_OK) return s;
   }
 
@@ -678,6 +711,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       mixv(q);
     mixv(c->d_lines.n);
     mixv(c->ck_count);
+    mixv(grouped_final);
     if (P.precision == GI_PREC_SPLIT) mixv(split_identity(c));
     for (size_t r = 0; r < rounds.size(); r++) {
       mixv(rounds[r].ncolY);
@@ -731,73 +765,104 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     }
     fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
 
-    for (const Target& T : targets[r]) {
-      BlockPlan& Fp = *T.F;
-      const Block& fb = *Fp.blk;
-      const Basis& bF = *c->bases[fb.J];
-      const int ndegF = c->degen[fb.gamma];
-      const int ldh = fb.ld;
-      const int ldt = round_up(fb.nvec, 2);
-      for (size_t k = 0; k < T.parts.size(); k++) {
-        const Unit& u = *T.parts[k].first;
-        const PairPlan* pp = T.parts[k].second;
-        const int ndegI = c->degen[u.I->blk->gamma];
-        const int nslot = c->bases[u.I->blk->J]->nslot;
-        GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
-                  return launch_build_h(c->w_z.p + u.ycol * Kp, zc, Kp, nslot, ndegI, u.nI, bF,
-                                        fb.gamma, ndegF, fb.nsize, ldh,
-                                        c->w_stencil.p + pp->st_off * 6,
-                                        c->w_stencil_n.p + pp->st_off, 6,
-                                        c->w_h.p + T.hcol[k] * ldh, c->stream);
-                }));
+    for (const auto& grp : groups[r]) {
+      // H of every final block of the group
+      for (size_t t = grp.first; t < grp.second; t++) {
+        const Target& T = targets[r][t];
+        const Block& fb = *T.F->blk;
+        const Basis& bF = *c->bases[fb.J];
+        const int ndegF = c->degen[fb.gamma];
+        const int ldh = fb.ld;
+        for (size_t k = 0; k < T.parts.size(); k++) {
+          const Unit& u = *T.parts[k].first;
+          const PairPlan* pp = T.parts[k].second;
+          const int ndegI = c->degen[u.I->blk->gamma];
+          const int nslot = c->bases[u.I->blk->J]->nslot;
+          GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
+                    return launch_build_h(c->w_z.p + u.ycol * Kp, zc, Kp, nslot, ndegI, u.nI, bF,
+                                          fb.gamma, ndegF, fb.nsize, ldh,
+                                          c->w_stencil.p + pp->st_off * 6,
+                                          c->w_stencil_n.p + pp->st_off, 6,
+                                          c->w_h.p + T.hoff + T.hcol[k] * ldh, c->stream);
+                  }));
+        }
       }
-      if (P.precision == GI_PREC_SPLIT) {
-        gi_status s = split_gemm_final(c, *Fp.blk, c->w_h.p, ldh, (int)T.ncolH, c->w_t.p, ldt);
+      // the final-state GEMMs: one persistent launch for the group, or one per block
+      if (grouped_final) {
+        std::vector<FinalJob> jobs;
+        for (size_t t = grp.first; t < grp.second; t++) {
+          const Target& T = targets[r][t];
+          Block& fb = *T.F->blk;
+          jobs.push_back(FinalJob{&fb, c->w_h.p + T.hoff, fb.ld, (int)T.ncolH, c->w_t.p + T.toff,
+                                  round_up(fb.nvec, 2)});
+        }
+        gi_status s = split_gemm_final_grouped(c, jobs);
         if (s != GI_OK) return s;
       } else {
-        GI_CUDA(c, timed(c, GI_PHASE_FINAL_GEMM, [&] {
-                  return gemm_fp64_nt(fb.d_vecs.p, fb.ld, 0, c->w_h.p, ldh, c->w_t.p, ldt, 0,
-                                      fb.nvec, (int)T.ncolH, ldh, 1, c->stream);
-                }));
+        for (size_t t = grp.first; t < grp.second; t++) {
+          const Target& T = targets[r][t];
+          const Block& fb = *T.F->blk;
+          const int ldh = fb.ld, ldt = round_up(fb.nvec, 2);
+          double* H = c->w_h.p + T.hoff;
+          double* Tm = c->w_t.p + T.toff;
+          if (P.precision == GI_PREC_SPLIT) {
+            gi_status s = split_gemm_final(c, *T.F->blk, H, ldh, (int)T.ncolH, Tm, ldt);
+            if (s != GI_OK) return s;
+          } else {
+            GI_CUDA(c, timed(c, GI_PHASE_FINAL_GEMM, [&] {
+                      return gemm_fp64_nt(fb.d_vecs.p, fb.ld, 0, H, ldh, Tm, ldt, 0, fb.nvec,
+                                          (int)T.ncolH, ldh, 1, c->stream);
+                    }));
+          }
+        }
       }
-      fl_final += 2.0 * fb.nsize * (double)fb.nvec * T.ncolH;
-      const auto off = farr[&Fp];
-      for (size_t k = 0; k < T.parts.size(); k++) {
-        const Unit& u = *T.parts[k].first;
-        const PairPlan* pp = T.parts[k].second;
-        EpiParams ep{};
-        ep.jI = u.I->blk->J;
-        ep.jF = fb.J;
-        ep.ndegI = c->degen[u.I->blk->gamma];
-        ep.ndegF = ndegF;
-        ep.reduced = P.reduced;
-        ep.combo_mask = pp->combo_mask;
-        ep.gns = P.gns[u.I->blk->gamma];
-        ep.zpe = zpe;
-        ep.beta = beta;
-        ep.q_stat = qstat;
-        ep.fw0 = P.freq_window[0];
-        ep.fw1 = P.freq_window[1];
-        ep.thresh_S = P.thresh_linestrength;
-        ep.thresh_I = P.thresh_intensity;
-        ep.A_coef = ph.A_coef;
-        ep.intens_cm_mol = ph.intens_cm_mol;
-        ep.avogno = ph.avogno;
-        const int32_t* d_lvI = c->w_ivec.p + 2 * u.off + u.nI;
-        GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
-                  return launch_epilogue(c->w_t.p + T.hcol[k] * ldt, ldt, u.nI, fb.nvec, d_lvI,
-                                         d_EI.p + u.off, c->w_int.p + off.first, fb.d_energies.p,
-                                         c->w_upper.p + off.second, ep, c->d_lines.p,
-                                         c->w_counter.p, (long long)c->d_lines.n, c->stream);
-                }));
-        npairs_checked += (int64_t)u.nI * Fp.nupper;
+      // epilogues, and a line-count checkpoint after each block's
+      for (size_t t = grp.first; t < grp.second; t++) {
+        const Target& T = targets[r][t];
+        BlockPlan& Fp = *T.F;
+        const Block& fb = *Fp.blk;
+        const int ndegF = c->degen[fb.gamma];
+        const int ldt = round_up(fb.nvec, 2);
+        fl_final += 2.0 * fb.nsize * (double)fb.nvec * T.ncolH;
+        const auto off = farr[&Fp];
+        for (size_t k = 0; k < T.parts.size(); k++) {
+          const Unit& u = *T.parts[k].first;
+          const PairPlan* pp = T.parts[k].second;
+          EpiParams ep{};
+          ep.jI = u.I->blk->J;
+          ep.jF = fb.J;
+          ep.ndegI = c->degen[u.I->blk->gamma];
+          ep.ndegF = ndegF;
+          ep.reduced = P.reduced;
+          ep.combo_mask = pp->combo_mask;
+          ep.gns = P.gns[u.I->blk->gamma];
+          ep.zpe = zpe;
+          ep.beta = beta;
+          ep.q_stat = qstat;
+          ep.fw0 = P.freq_window[0];
+          ep.fw1 = P.freq_window[1];
+          ep.thresh_S = P.thresh_linestrength;
+          ep.thresh_I = P.thresh_intensity;
+          ep.A_coef = ph.A_coef;
+          ep.intens_cm_mol = ph.intens_cm_mol;
+          ep.avogno = ph.avogno;
+          const int32_t* d_lvI = c->w_ivec.p + 2 * u.off + u.nI;
+          GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+                    return launch_epilogue(c->w_t.p + T.toff + T.hcol[k] * ldt, ldt, u.nI,
+                                           fb.nvec, d_lvI, d_EI.p + u.off,
+                                           c->w_int.p + off.first, fb.d_energies.p,
+                                           c->w_upper.p + off.second, ep, c->d_lines.p,
+                                           c->w_counter.p, (long long)c->d_lines.n, c->stream);
+                  }));
+          npairs_checked += (int64_t)u.nI * Fp.nupper;
+        }
+        // checkpoint: every line of this final block is written once this fires
+        GI_CUDA(c, cudaMemcpyAsync(c->ck_count + ck, c->w_counter.p, sizeof(unsigned long long),
+                                   cudaMemcpyDeviceToHost, c->stream));
+        GI_CUDA(c, cudaEventRecordWithFlags(c->ck_ev[ck], c->stream,
+                                            capturing ? cudaEventRecordExternal : 0));
+        ck++;
       }
-      // checkpoint: every line of this final block is written once this fires
-      GI_CUDA(c, cudaMemcpyAsync(c->ck_count + ck, c->w_counter.p, sizeof(unsigned long long),
-                                 cudaMemcpyDeviceToHost, c->stream));
-      GI_CUDA(c, cudaEventRecordWithFlags(c->ck_ev[ck], c->stream,
-                                          capturing ? cudaEventRecordExternal : 0));
-      ck++;
     }
   }
   return GI_OK;

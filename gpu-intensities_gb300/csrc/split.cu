@@ -1053,6 +1053,293 @@ __global__ void __launch_bounds__(kThreadsG, 1)
   }
 }
 
+// ------------------------------------------------------------------ grouped persistent
+// Persistent multi-problem form of the two-pass grouped kernel (one launch for
+// the final-state GEMMs of every final block of a round).  The problems (one
+// per final block: its vectors' digits x its H digits) have their own shapes
+// and K; their tiles form one work list, problem by problem, row tiles
+// fastest.  One CTA per SM takes items blockIdx.x, blockIdx.x + gridDim.x, ...
+// and runs each item's K in segments of at most kKSeg (the exactness bound of
+// the diagonal sums), each segment's FP64 result added to the previous ones'
+// by the same epilogue thread.  Tensor memory holds one segment at a time, so
+// the barriers that hand it between the MMA issuer and the epilogue count
+// segments: accf[p] completes once per segment and pass, tfree0 / tfree1 once
+// per segment after the epilogue has read pass 0 / pass 1.
+constexpr int kGpMaxProb = 44;  // 44 x 576 B of kernel parameters (limit 32,764 B)
+
+struct GpProb {
+  CUtensorMap aq, at, bq, bt;
+  const int32_t* ea;
+  const int32_t* eb;
+  double* C;
+  int ldc, M, Mpad, Nc, K, nM, nN, first;  // first: the problem's first work item
+};
+struct GpParams {
+  GpProb p[kGpMaxProb];
+  int nprob, nitems;
+};
+
+template <int S, int BN, int D1>
+__global__ void __launch_bounds__(kThreadsG, 1)
+    k_split_gemm_gp(const __grid_constant__ GpParams P, int w, int* err) {
+  constexpr int NQ = S / 4, NT = S % 4;
+  constexpr int HALF = BN / 2, NCH = HALF / kChunkG;
+  constexpr int MAXD = D1 > S - D1 ? D1 : S - D1;
+  static_assert(D1 < S && D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
+  static_assert((BN * 128) % 1024 == 0 && HALF % kChunkG == 0, "tile shape");
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  constexpr uint32_t kAq = kBM * 128, kAt = kBM * 32, kBq = BN * 128, kBt = BN * 32;
+  constexpr uint32_t kAbytes = NQ * kAq + NT * kAt;
+  constexpr uint32_t kStage = stage_bytes_g(S, BN);
+  constexpr int PK = (D1 <= 4 && 2 * (kAq + kBq) <= kStage) ? 2 : 1;
+  constexpr int ST = kStages2;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
+  uint64_t* empty = full + ST;
+  uint64_t* accf = empty + ST;    // [2]
+  uint64_t* tfree0 = accf + 2;
+  uint64_t* tfree1 = tfree0 + 1;
+  uint64_t* drain = tfree1 + 1;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < ST; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(&accf[0], 1);
+    mbar_init(&accf[1], 1);
+    mbar_init(tfree0, 256);
+    mbar_init(tfree1, 256);
+    mbar_init(drain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                     sptr(tmem_slot)));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  // item -> (problem, row tile, column tile); every role walks the same list
+  auto decode = [&](int item, int& pi, int& m0, int& n0) {
+    pi = 0;
+    while (pi + 1 < P.nprob && P.p[pi + 1].first <= item) ++pi;
+    const int local = item - P.p[pi].first;
+    m0 = (local % P.p[pi].nM) * kBM;
+    n0 = (local / P.p[pi].nM) * BN;
+  };
+
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer: one continuous slot ring over all segments
+      int it = 0;
+      bool ok = true;
+      for (int item = blockIdx.x; item < P.nitems && ok; item += gridDim.x) {
+        int pi, m0, n0;
+        decode(item, pi, m0, n0);
+        const GpProb& pr = P.p[pi];
+        for (int k0 = 0; k0 < pr.K && ok; k0 += kKSeg) {
+          const int nk = min(kKSeg, pr.K - k0) / kBK, nk0 = nk / PK;
+          for (int sl = 0; sl < nk0 + nk; ++sl, ++it) {
+            const int pass = sl >= nk0, st = it % ST;
+            if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 31)) {
+              ok = false;
+              break;
+            }
+            unsigned char* sa = smem + st * kStage;
+            if (pass == 0 && PK == 2) {
+              mbar_expect_tx(&full[st], 2 * (kAq + kBq));
+              for (int h = 0; h < 2; ++h) {
+                const int kb = k0 / kBK + 2 * sl + h;
+                unsigned char* sh = sa + h * (kAq + kBq);
+                tma_load_3d(sh, &pr.aq, &full[st], kb * 64, m0, 0);
+                tma_load_3d(sh + kAq, &pr.bq, &full[st], kb * 64, n0, 0);
+              }
+            } else {
+              const int kb = k0 / kBK + (pass ? sl - nk0 : sl);
+              const int np = pass ? S : D1;
+              const int gq = min(NQ, (np + 3) / 4), tq = max(0, np - 4 * NQ);
+              unsigned char* sb = sa + kAbytes;
+              mbar_expect_tx(&full[st], gq * (kAq + kBq) + tq * (kAt + kBt));
+              for (int g = 0; g < gq; ++g) {
+                tma_load_3d(sa + g * kAq, &pr.aq, &full[st], kb * 64, m0, g);
+                tma_load_3d(sb + g * kBq, &pr.bq, &full[st], kb * 64, n0, g);
+              }
+              for (int q = 0; q < tq; ++q) {
+                tma_load_3d(sa + NQ * kAq + q * kAt, &pr.at, &full[st], kb * kBK, m0, q);
+                tma_load_3d(sb + NQ * kBq + q * kBt, &pr.bt, &full[st], kb * kBK, n0, q);
+              }
+            }
+          }
+        }
+      }
+      if (*abort_flag) {  // copies in flight land before the shared memory goes away
+        for (int j = (it > ST ? it - ST : 0); j < it; ++j) {
+          const uint64_t t0 = gtimer();
+          while (!mbar_try(&full[j % ST], (j / ST) & 1) && gtimer() - t0 < 1000000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      const uint32_t idesc = idesc_bf16(kBM, BN);
+      int it = 0, seg = 0;  // ring slot and segment counters of this CTA
+      bool ok = true;
+      for (int item = blockIdx.x; item < P.nitems && ok; item += gridDim.x) {
+        int pi, m0, n0;
+        decode(item, pi, m0, n0);
+        const int K = P.p[pi].K;
+        for (int k0 = 0; k0 < K && ok; k0 += kKSeg, ++seg) {
+          const int nk = min(kKSeg, K - k0) / kBK, nk0 = nk / PK;
+          if (seg > 0) {  // the epilogue has read the previous segment's pass 1
+            ok = mbar_wait(tfree1, (seg - 1) & 1, abort_flag, err, 34);
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            if (!ok) break;
+          }
+          for (int sl = 0; sl < nk0 + nk; ++sl, ++it) {
+            const int pass = sl >= nk0, st = it % ST;
+            if (pass == 1 && sl == nk0) {  // pass 1 reuses pass 0's tensor memory
+              mma_commit(&accf[0]);
+              ok = mbar_wait(tfree0, seg & 1, abort_flag, err, 35);
+              asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+              if (!ok) break;
+            }
+            if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 32)) {
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+            const uint32_t sa = sptr(smem + st * kStage);
+            if (pass == 0 && PK == 2) {
+#pragma unroll
+              for (int h = 0; h < 2; ++h) {
+                const uint32_t a0 = sa + h * (kAq + kBq), b0 = a0 + kAq;
+                const bool first = sl == 0 && h == 0;
+#pragma unroll
+                for (int d = 0; d < D1; ++d)
+#pragma unroll
+                  for (int p = 0; p <= d; ++p)
+                    mma_bf16(tmem + d * BN, sdesc_sw128(a0 + p * 32),
+                             sdesc_sw128(b0 + (d - p) * 32), idesc, (!first || p > 0) ? 1u : 0u);
+              }
+            } else {
+              const uint32_t a0 = sa, b0 = sa + kAbytes;
+              auto adesc = [&](int p) {
+                return p < 4 * NQ ? sdesc_sw128(a0 + (p >> 2) * kAq + (p & 3) * 32)
+                                  : sdesc_sw32(a0 + NQ * kAq + (p - 4 * NQ) * kAt);
+              };
+              auto bdesc = [&](int p) {
+                return p < 4 * NQ ? sdesc_sw128(b0 + (p >> 2) * kBq + (p & 3) * 32)
+                                  : sdesc_sw32(b0 + NQ * kBq + (p - 4 * NQ) * kBt);
+              };
+              const int kb = pass ? sl - nk0 : sl;
+              if (pass == 0) {
+#pragma unroll
+                for (int d = 0; d < D1; ++d)
+#pragma unroll
+                  for (int p = 0; p <= d; ++p)
+                    mma_bf16(tmem + d * BN, adesc(p), bdesc(d - p), idesc,
+                             (kb > 0 || p > 0) ? 1u : 0u);
+              } else {
+#pragma unroll
+                for (int d = D1; d < S; ++d)
+#pragma unroll
+                  for (int p = 0; p <= d; ++p)
+                    mma_bf16(tmem + (d - D1) * BN, adesc(p), bdesc(d - p), idesc,
+                             (kb > 0 || p > 0) ? 1u : 0u);
+              }
+            }
+            mma_commit(&empty[st]);
+          }
+          if (ok) mma_commit(&accf[1]);
+        }
+      }
+      // every MMA issued has completed before the tensor memory is freed
+      mma_commit(drain);
+      const uint64_t t0 = gtimer();
+      while (!mbar_try(drain, 0) && gtimer() - t0 < 1000000000ull) {
+      }
+    }
+  } else {
+    // warps 2..9: TMEM lane quadrant (warp % 4), column half (warp - 2) / 4
+    const int q4 = warp & 3, half = (warp - 2) >> 2;
+    const uint32_t lanes = (uint32_t)(q4 * 32) << 16;
+    int seg = 0;
+    bool ok = true;
+    for (int item = blockIdx.x; item < P.nitems && ok; item += gridDim.x) {
+      int pi, m0, n0;
+      decode(item, pi, m0, n0);
+      const GpProb& pr = P.p[pi];
+      const int m = m0 + q4 * 32 + lane;
+      const int emr = (m < pr.M) ? pr.ea[m] : 0;
+      for (int k0 = 0; k0 < pr.K && ok; k0 += kKSeg, ++seg) {
+        long long v0[NCH][kChunkG];  // pass 0's exact sums of this thread's columns
+        for (int pass = 0; pass < 2 && ok; ++pass) {
+          ok = mbar_wait(&accf[pass], seg & 1, abort_flag, err, 33, 256);
+          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+          if (!ok) break;
+          const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
+#pragma unroll
+          for (int ch = 0; ch < NCH; ++ch) {
+            const int c0 = half * HALF + ch * kChunkG;
+            uint32_t f[MAXD][kChunkG];
+#pragma unroll
+            for (int d = 0; d < MAXD; ++d)
+              if (d < d1 - d0) tmem_ld8_nowait(tmem + lanes + d * BN + c0, f[d]);
+            tmem_wait_ld();
+            long long v[kChunkG];
+#pragma unroll
+            for (int j = 0; j < kChunkG; ++j) v[j] = 0;
+#pragma unroll
+            for (int d = 0; d < MAXD; ++d)
+              if (d < d1 - d0) {
+#pragma unroll
+                for (int j = 0; j < kChunkG; ++j)
+                  v[j] = (v[j] << w) + (long long)__float2int_rn(__uint_as_float(f[d][j]));
+              }
+            if (pass == 0) {
+#pragma unroll
+              for (int j = 0; j < kChunkG; ++j) v0[ch][j] = v[j];
+            } else if (m < pr.M) {
+#pragma unroll
+              for (int j = 0; j < kChunkG; ++j) {
+                const int n = n0 + c0 + j;
+                if (n < pr.Nc) {
+                  const int base = emr + pr.eb[n] - 2 * w;
+                  double out = scaled_int(v0[ch][j], base - w * (D1 - 1)) +
+                               scaled_int(v[j], base - w * (S - 1));
+                  double* dst = pr.C + (size_t)n * pr.ldc + m;
+                  if (k0 > 0) out += ld_acc(dst);  // the earlier segments' sum
+                  *dst = out;
+                }
+              }
+            }
+          }
+          // all reads of this pass are done: the MMA issuer may overwrite the columns
+          asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(
+                           sptr(pass ? tfree1 : tfree0))
+                       : "memory");
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+  }
+}
+
 // ------------------------------------------------------------------ slicing
 // FP64 arithmetic is scarce on this GPU, so the digits are cut with integer
 // operations on the bit pattern.  For a row with exponent e (max|x| < 2^(e-1)),
@@ -1289,6 +1576,11 @@ cudaError_t set_attributes() {
         status = set_smem(k_split_gemm_g<S, BN2, d1b_of(S), false>, smemg_bytes(S, BN2), k_split_gemm_g<S, BN2, d1b_of(S), true>);
       if (status == cudaSuccess)
         status = set_smem(k_split_gemm_g<S, BN1, S, false>, smemg_bytes(S, BN1), k_split_gemm_g<S, BN1, S, true>);
+      if constexpr (S == 9)
+        if (status == cudaSuccess)
+          status = cudaFuncSetAttribute(k_split_gemm_gp<S, BN2, D1>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)smemg_bytes(S, BN2));
       constexpr int DC = d1c_of(S);
       if (status == cudaSuccess)
         status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 1>,
@@ -1810,6 +2102,104 @@ gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol
     return cudaSuccess;
   });
   return r;
+}
+
+// The persistent grouped final GEMM: the default two-pass grouped geometry at
+// s = 9 (other digit counts, the plain layout and a pinned GI_SPLIT_FORCE
+// configuration take one launch per final block); GI_SPLIT_PERSIST=0 turns it
+// off.
+bool split_grouped_final(const Ctx* c) {
+  if (!c->split || !c->split->grouped || c->split->s != 9 || getenv("GI_SPLIT_FORCE"))
+    return false;
+  const char* e = getenv("GI_SPLIT_PERSIST");
+  return !(e && std::strcmp(e, "0") == 0);
+}
+int split_grouped_max_jobs() { return kGpMaxProb; }
+int split_grouped_items(int nvec, int ncol) {
+  return (round_up(nvec, kBM) / kBM) * ((ncol + bn2_of(9) - 1) / bn2_of(9));
+}
+
+gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
+  SplitState* S = state(c);
+  constexpr int SS = 9, BN = bn2_of(SS), D1 = d1_of(SS);
+  if (S->s != SS || !S->grouped || jobs.empty() || (int)jobs.size() > kGpMaxProb) {
+    c->err = "split precision: grouped final GEMM outside its configuration";
+    return GI_ERR_STATE;
+  }
+  gi_status g;
+  size_t elems = 0, cols = 0;
+  for (const FinalJob& j : jobs) {
+    elems += (size_t)j.ncol * j.ldh;
+    cols += j.ncol;
+  }
+  g = check(c, S->b_slices.reserve((size_t)SS * elems), "H slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->b_exp.reserve(std::max<size_t>(cols, 1)), "H exponents");
+  if (g != GI_OK) return g;
+  // problems in decreasing K, so that the longest items are dealt out first
+  std::vector<int> order(jobs.size());
+  for (size_t i = 0; i < jobs.size(); ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return jobs[a].ldh > jobs[b].ldh; });
+  GpParams* P = new GpParams();  // ~25 KB: not on the host stack
+  P->nprob = (int)jobs.size();
+  P->nitems = 0;
+  size_t eoff = 0, boff = 0;
+  double flops = 0.0;
+  for (int q = 0; q < (int)jobs.size() && g == GI_OK; ++q) {
+    const FinalJob& j = jobs[order[q]];
+    Block& fb = *j.fb;
+    const int K = j.ldh, vpad = round_up(fb.nvec, kBM);
+    g = block_digits(c, fb, K, /*wait=*/true);
+    if (g != GI_OK) break;
+    uint16_t* bs = S->b_slices.p + boff;
+    int32_t* be = S->b_exp.p + eoff;
+    g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                return slice(j.H, j.ldh, j.ncol, K, j.ncol, SS, S->w, true, bs, be, c->stream);
+              }),
+              "slice H");
+    if (g != GI_OK) break;
+    GpProb& pr = P->p[q];
+    const int nq = SS / 4, nt = SS % 4;
+    if (!make_map_groups(&pr.aq, fb.d_digits.p, K, vpad, nq, kBM, K) ||
+        !make_map(&pr.at, fb.d_digits.p + (size_t)4 * nq * vpad * K, K, vpad, nt, kBM, 1, K) ||
+        !make_map_groups(&pr.bq, bs, K, j.ncol, nq, BN, K) ||
+        !make_map(&pr.bt, bs + (size_t)4 * nq * j.ncol * K, K, j.ncol, nt, BN, 1, K)) {
+      g = check(c, cudaErrorInvalidValue, "grouped final GEMM tensor maps");
+      break;
+    }
+    pr.ea = fb.d_digit_exp.p;
+    pr.eb = be;
+    pr.C = j.T;
+    pr.ldc = j.ldt;
+    pr.M = fb.nvec;
+    pr.Mpad = vpad;
+    pr.Nc = j.ncol;
+    pr.K = K;
+    pr.nM = vpad / kBM;
+    pr.nN = (j.ncol + BN - 1) / BN;
+    pr.first = P->nitems;
+    P->nitems += pr.nM * pr.nN;
+    boff += (size_t)SS * j.ncol * K;
+    eoff += j.ncol;
+    flops += (double)SS * (SS + 1) / 2 * 2.0 * fb.nvec * (double)j.ncol * fb.nsize;
+  }
+  if (g == GI_OK && P->nitems > 0) {
+    c->stats.flops_tensor += flops;
+    g = check(c, kernel_attributes(SS), "kernel attributes");
+    if (g == GI_OK) {
+      const int grid = std::min(P->nitems, std::max(c->nsm, 1));
+      const size_t sm = smemg_bytes(SS, BN);
+      g = check(c, timed(c, GI_PHASE_FINAL_GEMM, [&] {
+                  k_split_gemm_gp<SS, BN, D1><<<grid, kThreadsG, sm, c->stream>>>(*P, S->w,
+                                                                                 S->err.p);
+                  return cudaGetLastError();
+                }),
+                "grouped final GEMM launch");
+    }
+  }
+  delete P;
+  return g;
 }
 
 int split_digits(const Ctx* c) { return shape_of(c).s; }

@@ -10,6 +10,22 @@ gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz
 // (f < nvec, n < ncol); the block's digit planes are cut on first use.
 gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol, double* T,
                            int ldt);
+// The final-state GEMMs of several final blocks in one persistent launch:
+// job j computes T_j[n*ldt_j + f] = sum_s V_Fj[f][s] * H_j[n*ldh_j + s].  The
+// H digits of all jobs go to one workspace (split_reserve sizes it), so the
+// jobs together may hold at most that many elements and columns, and at most
+// split_grouped_max_jobs() of them.
+struct FinalJob {
+  Block* fb;
+  const double* H;
+  int ldh, ncol;
+  double* T;
+  int ldt;
+};
+bool split_grouped_final(const Ctx* c);  // the persistent grouped launch applies
+int split_grouped_max_jobs();
+int split_grouped_items(int nvec, int ncol);  // work items of one job
+gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs);
 // Called once per run before the launch loop (sizes workspaces, slices the dipole).
 gi_status split_prepare(Ctx* c);
 // Before a launch sequence that must not allocate (graph capture): the B

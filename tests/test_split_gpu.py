@@ -44,9 +44,12 @@ def test_split_slice_counts(pkg, synth, oracle, slices):
     print(slices, res)
 
 
-def test_autotuner_table_and_results(pkg, synth, tmp_path):
+def test_autotuner_table_and_results(pkg, synth, tmp_path, monkeypatch):
     """gi_set_tuning(1, path): every GEMM shape class gets a timed choice in the
-    table file, and the tuned run's lines agree with the default ones."""
+    table file, and the tuned run's lines agree with the default ones.  The
+    final-state GEMMs go through the tuner when they run one launch per final
+    block (GI_SPLIT_PERSIST=0)."""
+    monkeypatch.setenv("GI_SPLIT_PERSIST", "0")
     prob = synth.make_c2v(51, 64, [0, 1, 2, 3], nvec_max=24)
     path = str(tmp_path / "tune.txt")
     with pkg.Engine(0) as eng:
@@ -100,3 +103,28 @@ def test_every_split_kernel_large_k(pkg, synth, monkeypatch, config):
     got, _ = run(pkg, prob)
     res = compare(got, want, rtol_S=1e-10, norm_tol=1e-12)
     print(config, res)
+
+
+@pytest.mark.parametrize("case,budget", [("c3v", 0), ("c3v", 24 << 20), ("c2v_large_k", 0)])
+def test_persistent_grouped_final_gemm(pkg, synth, monkeypatch, case, budget):
+    """The final-state GEMMs of all final blocks of a round in one persistent
+    launch (a work list of uneven tiles, K segments inside the kernel) give the
+    same lines, bit for bit, as one launch per block: in one round or many
+    (small HBM budget), and with final blocks of ~2100 functions (two K
+    segments per tile)."""
+    prob = (synth.make_c3v(71, 40, [0, 1, 2, 3, 4], nvec_max=30) if case == "c3v"
+            else synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12))
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("GI_SPLIT_PERSIST", mode)
+        with pkg.Engine(0, hbm_budget=budget) as eng:
+            eng.load(prob, precision=1)
+            eng.run(phase_timing=True)
+            st = eng.stats()
+            out[mode] = (pkg.keyed(eng.lines(), eng.levels()), st["launches_phase"]["final_gemm"])
+    (a, la), (b, lb) = out["0"], out["1"]
+    order = ["jI", "gammaI", "recI", "jF", "gammaF", "recF"]
+    a, b = np.sort(a, order=order), np.sort(b, order=order)
+    assert len(a) > 1000 and lb < la
+    for f in a.dtype.names:
+        assert np.array_equal(a[f], b[f]), f
