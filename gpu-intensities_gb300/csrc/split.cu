@@ -1437,6 +1437,71 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, size_t xstri
   }
 }
 
+// The same cut with one 256-thread block per row and the digit count fixed at
+// compile time (the planes' row bases in registers, the digit loop unrolled):
+// rows as long as a final block's basis (~11k elements) keep enough loads in
+// flight, where one warp per row leaves the kernel latency-bound.
+template <int S>
+__global__ void __launch_bounds__(256) k_slice_rows_b(const double* __restrict__ X, int ldx,
+                                                      size_t xstride, int rows, int K,
+                                                      int rows_pad, int w,
+                                                      uint32_t* __restrict__ out, int grouped,
+                                                      int32_t* __restrict__ e_out) {
+  __shared__ unsigned long long wmax[8];
+  const int r = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const size_t rset = (size_t)gridDim.y * rows_pad;     // rows of the plane set
+  const size_t ro = (size_t)blockIdx.y * rows_pad + r;  // this row in the set
+  const double2* x2 =
+      reinterpret_cast<const double2*>(X + blockIdx.y * xstride + (size_t)r * ldx);
+  const int K2 = K >> 1;
+  unsigned long long mx = 0;
+  if (r < rows)
+    for (int k = threadIdx.x; k < K2; k += 256) {
+      const double2 v = x2[k];
+      mx = max(mx, (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull);
+      mx = max(mx, (unsigned long long)__double_as_longlong(v.y) & 0x7FFFFFFFFFFFFFFFull);
+    }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) wmax[warp] = mx;
+  __syncthreads();
+  mx = wmax[0];
+#pragma unroll
+  for (int i = 1; i < 8; ++i) mx = max(mx, wmax[i]);
+  const int e = row_exponent(mx) + 1;  // |x| < 2^(e-1): every digit within 2^(w-1)
+  if (threadIdx.x == 0) e_out[ro] = e;
+  // 32-bit word offsets: plane p of this row starts at base[p]; the pair of
+  // elements (2k, 2k+1) lies koff words further (digit_offset's layouts)
+  const int nq = grouped ? S / 4 : 0;
+  size_t base[S];
+#pragma unroll
+  for (int p = 0; p < S; ++p)
+    base[p] = p < 4 * nq ? (((size_t)(p >> 2) * rset + ro) * 4 * (size_t)K + (p & 3) * 16) >> 1
+                         : ((size_t)4 * nq * rset * K + ((size_t)(p - 4 * nq) * rset + ro) * K) >> 1;
+  const int ws = w * S;
+  const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
+  for (int k = threadIdx.x; k < K2; k += 256) {
+    long long X0 = 0, X1 = 0;
+    if (r < rows) {
+      const double2 v = x2[k];
+      X0 = fixed_point(v.x, e, ws);
+      X1 = fixed_point(v.y, e, ws);
+    }
+    const size_t kg = (size_t)(k >> 3) * 32 + (k & 7);
+#pragma unroll
+    for (int p = S - 1; p >= 1; --p) {
+      const long long a0 = ((X0 + half) & mask) - half;
+      const long long a1 = ((X1 + half) & mask) - half;
+      X0 = (X0 - a0) >> w;
+      X1 = (X1 - a1) >> w;
+      out[base[p] + (p < 4 * nq ? kg : (size_t)k)] =
+          (uint32_t)bf16_of_int((int)a0) | ((uint32_t)bf16_of_int((int)a1) << 16);
+    }
+    out[base[0] + (4 * nq > 0 ? kg : (size_t)k)] =
+        (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
+  }
+}
+
 // ------------------------------------------------------------------ host
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
@@ -1705,6 +1770,12 @@ cudaError_t slice(const double* X, int ldx, int rows, int K, int rows_pad, int s
   const int wpb = 8;
   if ((K & 1) || (grouped && (K & 15)) || nstack < 1 || nstack > 65535)
     return cudaErrorInvalidValue;
+  if (s == 9) {
+    k_slice_rows_b<9><<<dim3(rows_pad, nstack), 256, 0, st>>>(
+        X, ldx, xstride, rows, K, rows_pad, w, reinterpret_cast<uint32_t*>(out), grouped ? 1 : 0,
+        e);
+    return cudaGetLastError();
+  }
   const dim3 grid((rows_pad + wpb - 1) / wpb, nstack);
   k_slice_rows<<<grid, wpb * 32, 0, st>>>(X, ldx, xstride, rows, K, rows_pad, s, w,
                                           reinterpret_cast<uint32_t*>(out), grouped ? 1 : 0, e);
