@@ -158,6 +158,10 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
                            long long cap) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y;
+  // the initial level's Boltzmann factor, once per block (FP64 exp is scarce)
+  __shared__ double boltz_i;
+  if (threadIdx.x == 0) boltz_i = exp(-(EI[i] - p.zpe) * p.beta);
+  __syncthreads();
   bool keep = false, pass = false;
   gi_line L;
   if (f < nF && upper_ok[f]) {
@@ -176,8 +180,7 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
       ls /= (double)p.ndegI;
       if (p.reduced && p.ndegF != 1 && p.ndegI != 1) ls *= (double)p.ndegI;
       const double anu = fabs(nu);
-      const double boltz_fc =
-          anu * exp(-(ei - p.zpe) * p.beta) * (1.0 - exp(-anu * p.beta)) / p.q_stat;
+      const double boltz_fc = anu * boltz_i * (1.0 - exp(-anu * p.beta)) / p.q_stat;
       const double A = p.A_coef * (double)(2 * p.jI + 1) * ls * (anu * anu * anu);
       const double S = ls * p.gns * (double)((2 * p.jI + 1) * (2 * p.jF + 1));
       const double In = S * p.intens_cm_mol * boltz_fc;
