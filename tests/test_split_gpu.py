@@ -105,15 +105,20 @@ def test_every_split_kernel_large_k(pkg, synth, monkeypatch, config):
     print(config, res)
 
 
-@pytest.mark.parametrize("case,budget", [("c3v", 0), ("c3v", 24 << 20), ("c2v_large_k", 0)])
+@pytest.mark.parametrize("case,budget", [("c3v", 0), ("c3v", 24 << 20), ("c2v_large_k", 0),
+                                         ("c3v_many_blocks", 0)])
 def test_persistent_grouped_final_gemm(pkg, synth, monkeypatch, case, budget):
     """The final-state GEMMs of all final blocks of a round in one persistent
     launch (a work list of uneven tiles, K segments inside the kernel) give the
     same lines, bit for bit, as one launch per block: in one round or many
     (small HBM budget), and with final blocks of ~2100 functions (two K
     segments per tile)."""
-    prob = (synth.make_c3v(71, 40, [0, 1, 2, 3, 4], nvec_max=30) if case == "c3v"
-            else synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12))
+    if case == "c3v":
+        prob = synth.make_c3v(71, 40, [0, 1, 2, 3, 4], nvec_max=30)
+    elif case == "c2v_large_k":
+        prob = synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12)
+    else:  # 63 final blocks in one round: groups split at the launch's 44 problems
+        prob = synth.make_c3v(72, 24, list(range(21)), nvec_max=6)
     out = {}
     for mode in ("0", "1"):
         monkeypatch.setenv("GI_SPLIT_PERSIST", mode)
