@@ -609,11 +609,12 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   c->phase_recs.clear();
   // a streamed dipole's copy stream is not part of a capture: eager runs
   const bool use_graph = (flags & GI_RUN_GRAPH) && !c->timing && !c->parent && !c->streamed();
-  bool grouped_final = false;
+  bool grouped_final = false, fused_y = false;
   if (P.precision == GI_PREC_SPLIT) {
     gi_status s = split_prepare(c);
     if (s != GI_OK) return s;
     grouped_final = split_grouped_final(c);
+    fused_y = split_fused_y(c);
   }
   // Final blocks go through the final-state GEMM in groups: with the persistent
   // grouped launch, consecutive blocks of a round until the group has work for
@@ -712,6 +713,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     mixv(c->d_lines.n);
     mixv(c->ck_count);
     mixv(grouped_final);
+    mixv(fused_y);
     if (P.precision == GI_PREC_SPLIT) mixv(split_identity(c));
     for (size_t r = 0; r < rounds.size(); r++) {
       mixv(rounds[r].ncolY);
@@ -749,15 +751,24 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     for (const Unit& u : R.units) {
       const Basis& bI = *c->bases[u.I->blk->J];
       const int ndegI = c->degen[u.I->blk->gamma];
-      GI_CUDA(c, timed(c, GI_PHASE_CORRELATE, [&] {
-                return launch_build_y(u.I->blk->d_vecs.p, u.I->blk->ld, c->w_ivec.p + 2 * u.off,
-                                      u.nI, ndegI, bI, u.I->blk->gamma, ndegI, N, Kp,
-                                      c->w_y.p + u.ycol * Kp, c->stream);
-              }));
+      if (fused_y) {  // straight into the digit planes of the half-ls GEMM's B operand
+        gi_status s = split_build_y_digits(c, u.I->blk->d_vecs.p, u.I->blk->ld,
+                                           c->w_ivec.p + 2 * u.off, u.nI, ndegI, bI,
+                                           u.I->blk->gamma, u.ycol, R.ncolY);
+        if (s != GI_OK) return s;
+      } else {
+        GI_CUDA(c, timed(c, GI_PHASE_CORRELATE, [&] {
+                  return launch_build_y(u.I->blk->d_vecs.p, u.I->blk->ld,
+                                        c->w_ivec.p + 2 * u.off, u.nI, ndegI, bI,
+                                        u.I->blk->gamma, ndegI, N, Kp, c->w_y.p + u.ycol * Kp,
+                                        c->stream);
+                }));
+      }
       by_corr += 8.0 * ((double)u.nI * u.I->blk->nsize + (double)u.ncolY * Kp);
     }
     if (P.precision == GI_PREC_SPLIT) {
-      gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY);
+      gi_status s =
+          split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY, fused_y);
       if (s != GI_OK) return s;
     } else {
       gi_status s = dipole_gemm_fp64(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY, c->stream);

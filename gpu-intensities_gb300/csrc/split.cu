@@ -1502,6 +1502,83 @@ __global__ void __launch_bounds__(256) k_slice_rows_b(const double* __restrict__
   }
 }
 
+// Y built straight into its digit planes (split path): one 256-thread block per
+// row (i, d, slot) of the B operand computes the row's Kp values of Y with
+// k_build_y's arithmetic (the same order of operations, so the same doubles)
+// into shared memory, takes the row exponent and cuts the digits as
+// k_slice_rows_b does.  The FP64 Y never goes to HBM.
+template <int S>
+__global__ void __launch_bounds__(256)
+    k_build_y_digits(const double* __restrict__ vecs, int ld, const int32_t* __restrict__ ivec,
+                     int ndeg, const int32_t* __restrict__ yptr, const int32_t* __restrict__ yroot,
+                     const int32_t* __restrict__ root_case, const int32_t* __restrict__ root_lam,
+                     const int32_t* __restrict__ case_iterm,
+                     const int32_t* __restrict__ case_nelem, const double* __restrict__ rep,
+                     int Ntot, int degen, int nslot, int N, int Kp, int w,
+                     uint32_t* __restrict__ out, int grouped, int32_t* __restrict__ e_out,
+                     size_t row0, size_t rset) {
+  extern __shared__ __align__(16) double ys[];  // the row's Kp values
+  __shared__ unsigned long long wmax[8];
+  const int row = blockIdx.x;  // (i * ndeg + d) * nslot + slot within the unit
+  const int col = row / nslot, slot = row - col * nslot;
+  const int i = col / ndeg, d = col - i * ndeg;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double* vs = vecs + (size_t)ivec[i] * ld;
+  const double* rd = rep + (size_t)d * Ntot;
+  unsigned long long mx = 0;
+  for (int v = threadIdx.x; v < Kp; v += 256) {
+    double acc = 0.0;
+    if (v < N) {
+      const int q = slot * N + v;
+      for (int p = yptr[q]; p < yptr[q + 1]; ++p) {
+        const int r = yroot[p];
+        const int c = root_case[r], lam = root_lam[r];
+        const int it = case_iterm[c], ne = case_nelem[c];
+        const double* rr = rd + (size_t)lam * degen * Ntot;
+        for (int j = 0; j < ne; ++j) acc = fma(vs[it + j], rr[it + j], acc);
+      }
+    }
+    ys[v] = acc;
+    mx = max(mx, (unsigned long long)__double_as_longlong(acc) & 0x7FFFFFFFFFFFFFFFull);
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) wmax[warp] = mx;
+  __syncthreads();  // also: every value of the row is in shared memory
+  mx = wmax[0];
+#pragma unroll
+  for (int q = 1; q < 8; ++q) mx = max(mx, wmax[q]);
+  const int e = row_exponent(mx) + 1;
+  const size_t ro = row0 + row;
+  if (threadIdx.x == 0) e_out[ro] = e;
+  const int nq = grouped ? S / 4 : 0;
+  size_t base[S];
+#pragma unroll
+  for (int p = 0; p < S; ++p)
+    base[p] = p < 4 * nq ? (((size_t)(p >> 2) * rset + ro) * 4 * (size_t)Kp + (p & 3) * 16) >> 1
+                         : ((size_t)4 * nq * rset * Kp + ((size_t)(p - 4 * nq) * rset + ro) * Kp) >> 1;
+  const int ws = w * S;
+  const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
+  const double2* y2 = reinterpret_cast<const double2*>(ys);
+  for (int k = threadIdx.x; k < (Kp >> 1); k += 256) {
+    const double2 v = y2[k];
+    long long X0 = fixed_point(v.x, e, ws), X1 = fixed_point(v.y, e, ws);
+    const size_t kg = (size_t)(k >> 3) * 32 + (k & 7);
+#pragma unroll
+    for (int p = S - 1; p >= 1; --p) {
+      const long long a0 = ((X0 + half) & mask) - half;
+      const long long a1 = ((X1 + half) & mask) - half;
+      X0 = (X0 - a0) >> w;
+      X1 = (X1 - a1) >> w;
+      out[base[p] + (p < 4 * nq ? kg : (size_t)k)] =
+          (uint32_t)bf16_of_int((int)a0) | ((uint32_t)bf16_of_int((int)a1) << 16);
+    }
+    out[base[0] + (4 * nq > 0 ? kg : (size_t)k)] =
+        (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
+  }
+}
+constexpr int kFusedYMaxKp = 8192;  // 64 KB of shared memory per row
+
 // ------------------------------------------------------------------ host
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
@@ -1641,11 +1718,16 @@ cudaError_t set_attributes() {
         status = set_smem(k_split_gemm_g<S, BN2, d1b_of(S), false>, smemg_bytes(S, BN2), k_split_gemm_g<S, BN2, d1b_of(S), true>);
       if (status == cudaSuccess)
         status = set_smem(k_split_gemm_g<S, BN1, S, false>, smemg_bytes(S, BN1), k_split_gemm_g<S, BN1, S, true>);
-      if constexpr (S == 9)
+      if constexpr (S == 9) {
         if (status == cudaSuccess)
           status = cudaFuncSetAttribute(k_split_gemm_gp<S, BN2, D1>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smemg_bytes(S, BN2));
+        if (status == cudaSuccess)
+          status = cudaFuncSetAttribute(k_build_y_digits<S>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(kFusedYMaxKp * sizeof(double)));
+      }
       constexpr int DC = d1c_of(S);
       if (status == cudaSuccess)
         status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 1>,
@@ -2040,19 +2122,21 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
 }
 
 gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zstride,
-                            int ncol) {
+                            int ncol, bool y_digits_ready) {
   SplitState* S = state(c);
   const int K = c->Kp;
   gi_status g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "Y slices");
   if (g != GI_OK) return g;
   g = check(c, S->b_exp.reserve(ncol), "Y exponents");
   if (g != GI_OK) return g;
-  g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-              return slice(Y, ldy, ncol, K, ncol, S->s, S->w, S->grouped, S->b_slices.p, S->b_exp.p,
-                           c->stream);
-            }),
-            "slice Y");
-  if (g != GI_OK) return g;
+  if (!y_digits_ready) {
+    g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                return slice(Y, ldy, ncol, K, ncol, S->s, S->w, S->grouped, S->b_slices.p,
+                             S->b_exp.p, c->stream);
+              }),
+              "slice Y");
+    if (g != GI_OK) return g;
+  }
   // algorithmic count: the true contraction length N, not the padded K
   c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * c->N * 3;
   if (S->panel) {
@@ -2271,6 +2355,30 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
   }
   delete P;
   return g;
+}
+
+bool split_fused_y(const Ctx* c) { return split_grouped_final(c) && c->Kp <= kFusedYMaxKp; }
+
+gi_status split_build_y_digits(Ctx* c, const double* vecs, int ld, const int32_t* ivec, int nI,
+                               int ndeg, const Basis& b, int gamma, size_t row0,
+                               size_t rows_total) {
+  SplitState* S = state(c);
+  const int rows = nI * ndeg * b.nslot;
+  if (rows == 0) return GI_OK;
+  if (S->s != 9 || S->b_slices.n < (size_t)9 * rows_total * c->Kp || S->b_exp.n < rows_total) {
+    c->err = "split precision: Y digit workspace not prepared";
+    return GI_ERR_STATE;
+  }
+  return check(c, timed(c, GI_PHASE_CORRELATE, [&] {
+                 k_build_y_digits<9><<<rows, 256, (size_t)c->Kp * sizeof(double), c->stream>>>(
+                     vecs, ld, ivec, ndeg, b.d_yptr.p, b.d_yroot.p, b.d_root_case.p,
+                     b.d_root_lam.p, b.d_case_iterm[gamma].p, b.d_case_nelem[gamma].p,
+                     b.d_rep[gamma].p, b.Ntotal[gamma], ndeg, b.nslot, c->N, c->Kp, S->w,
+                     reinterpret_cast<uint32_t*>(S->b_slices.p), S->grouped ? 1 : 0, S->b_exp.p,
+                     row0, rows_total);
+                 return cudaGetLastError();
+               }),
+               "Y digits");
 }
 
 int split_digits(const Ctx* c) { return shape_of(c).s; }

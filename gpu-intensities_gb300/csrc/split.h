@@ -4,8 +4,16 @@
 
 namespace gi {
 // Z[c][n*ldz + f] = sum_v mu_c(v, f) * Y[n*ldy + v] for c = 0..2, n < ncol.
+// y_digits_ready: split_build_y_digits already wrote Y's digits (Y unused).
 gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zstride,
-                            int ncol);
+                            int ncol, bool y_digits_ready = false);
+// Y of one unit (nI vectors of block `vecs`, ndeg components) built directly
+// into rows [row0, row0 + nI * ndeg * nslot) of the Y digit set of a round of
+// rows_total rows; split_fused_y() says when this path applies.
+bool split_fused_y(const Ctx* c);
+gi_status split_build_y_digits(Ctx* c, const double* vecs, int ld, const int32_t* ivec, int nI,
+                               int ndeg, const Basis& b, int gamma, size_t row0,
+                               size_t rows_total);
 // T[n*ldt + f] = sum_s V_F[f][s] * H[n*ldh + s] for the vectors of block fb
 // (f < nvec, n < ncol); the block's digit planes are cut on first use.
 gi_status split_gemm_final(Ctx* c, Block& fb, const double* H, int ldh, int ncol, double* T,
