@@ -14,16 +14,25 @@
 //     product is at most 2^(2w-2) and diagonal d has d+1 of them per k, so
 //     for w = 6 and K <= 2048 the sum is at most (d+1) 2^21, exact in the
 //     worst case for d <= 7 (the last diagonal of s = 9 carries the weight
-//     2^-48, where fp32 rounding is negligible).  Longer K runs as launches
-//     over segments of 2048, each adding its FP64 result to the previous ones';
-//   * the epilogue combines the diagonals in FP64 (Horner in 2^-w) and
-//     rescales by 2^(e_m + e_n - 2w).
+//     2^-48, where fp32 rounding is negligible).  Longer K runs in segments
+//     of 2048, each adding its FP64 result to the previous ones';
+//   * the epilogue combines the diagonals exactly in int64 (Horner in 2^w)
+//     and builds the FP64 result scaled by 2^(e_m + e_n - 2w).
 //
-// Kernel: one 128 x BN output tile per CTA; warp 0 issues TMA loads (one 3-D
-// box brings all s digit planes of a 32-wide K block), warp 1 (one thread)
-// issues tcgen05.mma for every digit pair of the block, warps 2-5 read the s
-// accumulators from TMEM and write FP64.  Every mbarrier wait is bounded by
-// %globaltimer; a timeout sets a device error word and the CTA unwinds.
+// Kernels (warp 0 issues TMA loads, one thread of warp 1 issues tcgen05.mma
+// for every digit pair of a K slice, the remaining warps read the
+// accumulators from TMEM and write FP64):
+//   k_split_gemm, k_split_gemm2, k_split_gemm3  plain digit layout: one pass,
+//       two passes, two passes with TMA-multicast clusters;
+//   k_split_gemm_g   grouped digit layout (four planes per 128-byte TMA row),
+//       one or two passes, one 128 x BN tile per CTA;
+//   k_split_gemm_gp  the grouped two-pass kernel made persistent over a work
+//       list of tiles of several GEMMs (the final-state GEMMs of a group of
+//       final blocks), K segments inside;
+//   k_slice_rows(_b), k_build_y_digits  FP64 rows -> digit planes (the latter
+//       builds the half-ls GEMM's Y rows and cuts them in one pass).
+// Every mbarrier wait is bounded by %globaltimer; a timeout sets a device
+// error word and the CTA unwinds.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
