@@ -26,6 +26,11 @@ def test_null_arguments_rejected(pkg):
     assert lib.gi_create(None, 0, 0) == pkg.GI_ERR_ARG
     assert lib.gi_destroy(None) == pkg.GI_OK
     assert lib.gi_set_symmetry(None, 1) == pkg.GI_ERR_ARG
+    # streamed dipole and the split GEMM probe check their arguments before any CUDA call
+    assert lib.gi_set_dipole_streamed(None, 10, None, 0, 0) == pkg.GI_ERR_ARG
+    assert lib.gi_dipole_panel_rows(None) == 0
+    assert lib.gi_probe_split_gemm(0, 0, 0, 4, 64, None, None, None) == pkg.GI_ERR_ARG
+    assert lib.gi_probe_split_gemm(0, 0, 4, 4, -1, None, None, None) == pkg.GI_ERR_ARG
 
 
 def test_struct_layouts_match_header(pkg, tmp_path):
