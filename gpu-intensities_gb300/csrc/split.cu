@@ -1573,6 +1573,11 @@ __global__ void __launch_bounds__(256)
     const double2 v = y2[k];
     long long X0 = fixed_point(v.x, e, ws), X1 = fixed_point(v.y, e, ws);
     const size_t kg = (size_t)(k >> 3) * 32 + (k & 7);
+    if ((X0 | X1) == 0) {  // most of Y is zero: every digit of the pair is zero
+#pragma unroll
+      for (int p = 0; p < S; ++p) out[base[p] + (p < 4 * nq ? kg : (size_t)k)] = 0u;
+      continue;
+    }
 #pragma unroll
     for (int p = S - 1; p >= 1; --p) {
       const long long a0 = ((X0 + half) & mask) - half;
