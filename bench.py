@@ -11,14 +11,22 @@ Metric: linestrengths/s, counting lines that pass every filter before the
 intensity threshold (1e-30 cm/molecule; the post-threshold count is reported
 beside it).
 
-  value   inputs resident in HBM, lines kept on the device, wall time of K
-          steps bracketed by synchronize (and a barrier across ranks)
+  value   inputs resident in HBM, lines kept on the device, CUDA-event time
+          of K steps on the engine's stream, bracketed by synchronize (and a
+          barrier across ranks); each step is one CUDA-graph launch
   e2e     the same job through the C ABI from pinned host buffers: every step
           uploads the dipole and every eigenvector block and reads all lines
           back to host memory
-  --impl reference   the reference's algorithm on the host cores (the CPU
-          oracle port; the reference has no CPU implementation of the path)
-          on a bounded sample of the same workload
+  roofline    the half-ls split GEMM's algorithmic TFLOP/s against the
+          measured bf16 peak, with its DRAM traffic
+  fp64_path / accuracy   the FP64 GPU path on the same job; split vs FP64
+          error per line on its J <= 3 part
+  serving     pair jobs arriving as a Poisson stream through gi_serve_*
+  dipole_streamed   the job with its dipole kept in host memory and streamed
+          in four panels
+  cpu_baseline / --impl reference   the reference's algorithm on the host
+          cores (the CPU oracle port; the reference has no CPU implementation
+          of the path) on a bounded sample of the same workload
 
 Multi-GPU (torchrun): every rank runs an independent replica of the job with
 its own seed (no collective on the data path), value = all ranks' lines /
