@@ -377,8 +377,7 @@ def main_ours(args):
     autotune = []
     if os.path.exists(tune_path):
         names = {"0": "one-pass", "1": "two-pass (split at s/2)", "2": "two-pass (split at s - s/2)",
-                 "3": "two-pass, 2x1 multicast cluster", "4": "two-pass, 1x2 multicast cluster",
-                 "5": "two-pass, 2x2 multicast cluster", "6": "grouped layout, two-pass (s/2)",
+                 "6": "grouped layout, two-pass (s/2)",
                  "7": "grouped layout, two-pass (s - s/2)", "8": "grouped layout, one-pass"}
         for line in open(tune_path).read().splitlines():
             s_, nA, nb, K, layout, kind, ga, ms = line.split()

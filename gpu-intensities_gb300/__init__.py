@@ -194,7 +194,6 @@ def lib():
         L.gi_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_stats)]
         L.gi_half_ls.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p]
         L.gi_measure_fp64_peak.argtypes = [C.c_int, f64p]
-        L.gi_measure_mma_cycles.argtypes = [C.c_int, C.c_int, f64p]
         L.gi_probe_split_gemm.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, f64p, f64p,
                                           f64p]
         L.gi_half_ls_noalloc.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
@@ -212,15 +211,6 @@ def measure_fp64_peak(device: int = 0) -> float:
     st = lib().gi_measure_fp64_peak(device, C.byref(v))
     if st != GI_OK:
         raise GiError(st, "gi_measure_fp64_peak failed")
-    return v.value
-
-
-def measure_mma_cycles(device: int = 0, n: int = 128) -> float:
-    """Cycles of one bf16 tcgen05 MMA (M=128, K=16) of width n (gi_measure_mma_cycles)."""
-    v = C.c_double(0.0)
-    st = lib().gi_measure_mma_cycles(device, n, C.byref(v))
-    if st != GI_OK:
-        raise GiError(st, "gi_measure_mma_cycles failed")
     return v.value
 
 

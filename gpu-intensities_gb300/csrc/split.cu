@@ -22,8 +22,7 @@
 // Kernels (warp 0 issues TMA loads, one thread of warp 1 issues tcgen05.mma
 // for every digit pair of a K slice, the remaining warps read the
 // accumulators from TMEM and write FP64):
-//   k_split_gemm, k_split_gemm2, k_split_gemm3  plain digit layout: one pass,
-//       two passes, two passes with TMA-multicast clusters;
+//   k_split_gemm, k_split_gemm2  plain digit layout: one pass, two passes;
 //   k_split_gemm_g   grouped digit layout (four planes per 128-byte TMA row),
 //       one or two passes, one 128 x BN tile per CTA;
 //   k_split_gemm_gp  the grouped two-pass kernel made persistent over a work
@@ -136,24 +135,6 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
       "l"(reinterpret_cast<uint64_t>(map)), "r"(sptr(bar)), "r"(c0), "r"(c1), "r"(c2)
       : "memory");
 }
-// The same load delivered to every CTA of `mask` in the cluster (same smem
-// offset, complete_tx on the mbarrier at the same offset in each of them).
-__device__ __forceinline__ void tma_load_3d_mc(void* dst, const CUtensorMap* map, uint64_t* bar,
-                                               int c0, int c1, int c2, uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
-      ".multicast::cluster [%0], [%1, {%3, %4, %5}], [%2], %6;\n" ::"r"(sptr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(sptr(bar)), "r"(c0), "r"(c1), "r"(c2), "h"(mask)
-      : "memory");
-}
-__device__ __forceinline__ uint32_t cluster_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cluster_sync_all() {
-  asm volatile("barrier.cluster.arrive.release;\nbarrier.cluster.wait.acquire;\n" ::: "memory");
-}
 // The earlier K segments' sum at an output element (K-segmented launches).
 // A volatile load: it stays inside its branch, so launches that do not
 // accumulate never read C.
@@ -220,15 +201,6 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
           sptr(bar))
-      : "memory");
-}
-// Arrives on the mbarrier at this offset in every CTA of `mask` once the
-// MMAs issued so far have completed.
-__device__ __forceinline__ void mma_commit_mc(uint64_t* bar, uint16_t mask) {
-  asm volatile(
-      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64"
-      " [%0], %1;\n" ::"r"(sptr(bar)),
-      "h"(mask)
       : "memory");
 }
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
@@ -582,199 +554,6 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
-  if (warp == 1) {
-    asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
-  }
-}
-
-
-// Cluster variant of the two-pass kernel.  A cluster of CM x CN CTAs computes
-// CM row tiles x CN column tiles; the CN CTAs of one row tile share its A digit
-// planes and the CM CTAs of one column tile share its B planes.  Each plane is
-// fetched from L2 once per cluster by one of its sharers and multicast into
-// every sharer's shared memory, which divides the L2-to-SM traffic per tile by
-// up to CN (A) and CM (B).  A CTA may refill a stage only when every CTA it
-// sends to has released it, so each CTA's MMA commit arrives on the "empty"
-// barrier of all CTAs that share its row or its column tile.  Tiles past the
-// edge still take part in the loads and releases (their TMA boxes read zeros)
-// and skip the stores.
-template <int S, int BN, int D1, int CM, int CN>
-__global__ void __launch_bounds__(kThreads, 1)
-    k_split_gemm3(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
-                  int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
-                  int nN, int GAc, int accum, int* err) {
-  static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
-  static_assert(CM * CN >= 2 && CM * CN <= 8, "portable cluster size");
-  constexpr int CS = CM * CN;
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  unsigned char* smem = reinterpret_cast<unsigned char*>(
-      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  constexpr uint32_t kAplane = kBM * kBK * 2, kBplane = BN * kBK * 2;
-  constexpr uint32_t kStage = S * (kAplane + kBplane);
-  constexpr int ST = kStages2;
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
-  uint64_t* empty = full + ST;
-  uint64_t* accf = empty + ST;
-  uint64_t* tfree = accf + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(tfree + 1);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
-
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int rank = (int)cluster_rank();
-  const int rm = rank % CM, rn = rank / CM;
-  const int q = blockIdx.x / CS;
-  const int nAc = (nA + CM - 1) / CM, nNc = (nN + CN - 1) / CN;
-  const int grp = q / (GAc * nNc);
-  const int r = q - grp * GAc * nNc;
-  const int gsz = min(GAc, nAc - grp * GAc);
-  const int ai = (grp * GAc + r % gsz) * CM + rm;
-  const int nt = (r / gsz) * CN + rn;
-  const bool valid = ai < nA && nt < nN;
-  const int n0 = nt * BN, m0 = (ai % nM) * kBM, z = ai / nM;
-  const int arow = z * Mpad + m0;  // past the last row tile: rows beyond the map read zeros
-  const int nk = K / kBK;
-  uint16_t maskA = 0, maskB = 0;  // CTAs sharing my row tile / my column tile
-  for (int j = 0; j < CN; ++j) maskA |= (uint16_t)(1u << (rm + CM * j));
-  for (int i = 0; i < CM; ++i) maskB |= (uint16_t)(1u << (i + CM * rn));
-  const uint16_t mask_rel = maskA | maskB;
-
-  if (threadIdx.x == 0) {
-    for (int i = 0; i < ST; ++i) {
-      mbar_init(&full[i], 1);
-      mbar_init(&empty[i], CM + CN - 1);
-    }
-    mbar_init(&accf[0], 1);
-    mbar_init(&accf[1], 1);
-    mbar_init(tfree, 128);
-    *abort_flag = 0;
-    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-  }
-  if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
-                     sptr(tmem_slot)));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  cluster_sync_all();  // every CTA's barriers exist before any peer signals them
-  asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-  const uint32_t tmem = *tmem_slot;
-
-  if (warp == 0) {
-    if (lane == 0) {  // TMA producer: this CTA's share of the planes, multicast
-      for (int it = 0; it < 2 * nk; ++it) {
-        const int pass = it >= nk, kb = it - pass * nk, st = it % ST;
-        const int np = pass ? S : D1;
-        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 11, 64))
-          break;
-        unsigned char* sa = smem + st * kStage;
-        mbar_expect_tx(&full[st], np * (kAplane + kBplane));  // everything landing here
-        for (int p = 0; p < np; ++p) {
-          if (p % CN == rn)
-            tma_load_3d_mc(sa + p * kAplane, &tmA, &full[st], kb * kBK, arow, p, maskA);
-          if (p % CM == rm)
-            tma_load_3d_mc(sa + S * kAplane + p * kBplane, &tmB, &full[st], kb * kBK, n0, p,
-                           maskB);
-        }
-      }
-    }
-  } else if (warp == 1) {
-    if (lane == 0) {  // MMA issuer
-      const uint32_t idesc = idesc_bf16(kBM, BN);
-      bool ok = true;
-      int last = 0;
-      for (int pass = 0; pass < 2 && ok; ++pass) {
-        last = pass;
-        if (pass == 1) {
-          ok = mbar_wait(tfree, 0, abort_flag, err, 14);
-          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-          if (!ok) break;
-        }
-        for (int kb = 0; kb < nk; ++kb) {
-          const int it = pass * nk + kb, st = it % ST;
-          if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 12)) {
-            ok = false;
-            break;
-          }
-          asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-          const uint32_t a0 = sptr(smem + st * kStage);
-          const uint32_t b0 = a0 + S * kAplane;
-          if (pass == 0) {
-#pragma unroll
-            for (int d = 0; d < D1; ++d)
-#pragma unroll
-              for (int p = 0; p <= d; ++p)
-                mma_bf16(tmem + d * BN, sdesc_sw32(a0 + p * kAplane),
-                         sdesc_sw32(b0 + (d - p) * kBplane), idesc, (kb > 0 || p > 0) ? 1u : 0u);
-          } else {
-#pragma unroll
-            for (int d = D1; d < S; ++d)
-#pragma unroll
-              for (int p = 0; p <= d; ++p)
-                mma_bf16(tmem + (d - D1) * BN, sdesc_sw32(a0 + p * kAplane),
-                         sdesc_sw32(b0 + (d - p) * kBplane), idesc, (kb > 0 || p > 0) ? 1u : 0u);
-          }
-          mma_commit_mc(&empty[st], mask_rel);  // the stage is free here and at every sender
-        }
-        mma_commit(&accf[pass]);
-      }
-      if (*abort_flag) {
-        uint64_t t0 = gtimer();
-        while (!mbar_try(&accf[last], 0) && gtimer() - t0 < 1000000000ull) {
-        }
-      }
-    }
-  } else {
-    const int q4 = warp & 3;
-    const int m = m0 + q4 * 32 + lane;
-    const bool row_ok = valid && m < M;
-    const int emr = row_ok ? ea[z * Mpad + m] : 0;
-    double* Cz = C + (size_t)(valid ? z : 0) * strideC;
-    for (int pass = 0; pass < 2; ++pass) {
-      const bool ok = mbar_wait(&accf[pass], 0, abort_flag, err, 13, 1000);
-      asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-      if (!ok) break;
-      const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
-      for (int c0 = 0; c0 < BN; c0 += 16) {
-        long long v[16];
-#pragma unroll
-        for (int j = 0; j < 16; ++j) v[j] = 0;
-        for (int d = d0; d < d1; ++d) {
-          float f[16];
-          tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (d - d0) * BN + c0, f);
-#pragma unroll
-          for (int j = 0; j < 16; ++j) v[j] = (v[j] << w) + (long long)__float2int_rn(f[j]);
-        }
-        if (row_ok) {
-#pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const int n = n0 + c0 + j;
-            if (n < Nc) {
-              const int E = emr + eb[n] - 2 * w - w * (d1 - 1);
-              double* dst = Cz + (size_t)n * ldc + m;
-              const double part = scaled_int(v[j], E);
-              *dst = (pass || accum) ? *dst + part : part;
-            }
-          }
-        }
-      }
-      if (pass == 0) {
-        asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
-      }
-    }
-  }
-  asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-  __syncthreads();
-  if (*abort_flag) {
-    // copies a peer issued into this CTA before the abort land within
-    // microseconds; give them 20 ms before the shared memory goes away
-    const uint64_t t0 = gtimer();
-    while (gtimer() - t0 < 20000000ull) {
-    }
-  }
-  cluster_sync_all();  // no peer signals or writes this CTA after it exits
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
@@ -1649,10 +1428,9 @@ bool make_map_groups(CUtensorMap* map, const void* base, int K, int rows, int nq
 // raster group (row tiles whose digit planes share about ga_mb MB of L2).
 struct GemmConfig {
   int kind = 1;  // 0: k_split_gemm (one pass); 1, 2: k_split_gemm2 (two passes,
-                 // diagonals split at s/2 or s - s/2); 3, 4, 5: k_split_gemm3 with
-                 // 2 x 1, 1 x 2, 2 x 2 clusters (row x column tiles); these read
-                 // the plain layout.  6, 7, 8: k_split_gemm_g on the grouped
-                 // layout (two passes split at s/2 or s - s/2, or one pass)
+                 // diagonals split at s/2 or s - s/2); these read the plain
+                 // layout.  6, 7, 8: k_split_gemm_g on the grouped layout (two
+                 // passes split at s/2 or s - s/2, or one pass).  3-5 are unused.
   int ga_mb = 64;
 };
 
@@ -1678,7 +1456,7 @@ int tile_n(int s, int kind) { return (kind == 0 || kind == 8) ? bn_for(s) : bn2_
 // that the grouped layout is the plain one).
 bool kind_valid(int s, int kind, bool grouped) {
   if (grouped && s >= 4) return kind == 6 || kind == 8 || (kind == 7 && (s & 1));
-  return kind == 0 || kind == 1 || (kind == 2 && (s & 1)) || (kind >= 3 && kind <= 5 && s >= 4);
+  return kind == 0 || kind == 1 || (kind == 2 && (s & 1));
 }
 GemmConfig default_config(int s, bool grouped) {
   GemmConfig g;
@@ -1689,8 +1467,6 @@ struct Maps {
   CUtensorMap a, b;    // plain planes, or the grouped layout's four-plane groups
   CUtensorMap at, bt;  // grouped layout: the s % 4 plain planes after the groups
 };
-// the two-pass split point the cluster kernels use
-__host__ __device__ constexpr int d1c_of(int s) { return s - s / 2; }
 
 SplitShape shape_of(const Ctx* c) {
   int s = c->params.split_slices > 0 ? c->params.split_slices : kDefaultSlices;
@@ -1742,19 +1518,6 @@ cudaError_t set_attributes() {
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(kFusedYMaxKp * sizeof(double)));
       }
-      constexpr int DC = d1c_of(S);
-      if (status == cudaSuccess)
-        status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 1>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem2_bytes(S, BN2));
-      if (status == cudaSuccess)
-        status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 1, 2>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem2_bytes(S, BN2));
-      if (status == cudaSuccess)
-        status = cudaFuncSetAttribute(k_split_gemm3<S, BN2, DC, 2, 2>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)smem2_bytes(S, BN2));
     }
   });
   return status;
@@ -1804,32 +1567,6 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
             err);
       return cudaGetLastError();
-    }
-    if (cfg.kind >= 3 && cfg.kind <= 5) {
-      const int CM = cfg.kind == 4 ? 1 : 2, CN = cfg.kind == 3 ? 1 : 2;
-      const int nAc = (nA + CM - 1) / CM, nNc = (nN + CN - 1) / CN;
-      const int GAc = std::max(1, std::min(nAc, (int)(((size_t)cfg.ga_mb << 20) / (a_tile * CM))));
-      cudaLaunchConfig_t lc = {};
-      lc.gridDim = dim3((unsigned)(nAc * nNc * CM * CN));
-      lc.blockDim = dim3(kThreads);
-      lc.dynamicSmemBytes = smem2_bytes(S, BN2);
-      lc.stream = st;
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = CM * CN;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      lc.attrs = at;
-      lc.numAttrs = 1;
-      constexpr int DC = d1c_of(S);
-      if (cfg.kind == 3)
-        return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 2, 1>, tA, tB, ea, eb, C, ldc,
-                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, accum, err);
-      if (cfg.kind == 4)
-        return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 1, 2>, tA, tB, ea, eb, C, ldc,
-                                  strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, accum, err);
-      return cudaLaunchKernelEx(&lc, k_split_gemm3<S, BN2, DC, 2, 2>, tA, tB, ea, eb, C, ldc,
-                                strideC, M, Mpad, Nc, K, w, nM, nA, nN, GAc, accum, err);
     }
   }
   if (one)
@@ -2002,9 +1739,8 @@ static Tuner& tuner() {
   return t;
 }
 static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16}, {2, 64},
-                                         {2, 32}, {0, 64}, {0, 32}, {3, 32}, {4, 32},
-                                         {5, 32}, {6, 64}, {6, 32}, {6, 128}, {7, 64},
-                                         {7, 32}, {8, 64}, {8, 32}};
+                                         {2, 32}, {0, 64}, {0, 32}, {6, 64}, {6, 32},
+                                         {6, 128}, {7, 64}, {7, 32}, {8, 64}, {8, 32}};
 
 static void tune_load(Tuner& t, const std::string& path) {
   t.loaded = path;

@@ -4,9 +4,9 @@
  * The FP64 path's roofline denominator is not in the measured peak table
  * (that holds HBM copy bandwidth and bf16 GEMM throughput), so the engine
  * measures the FP64 tensor-pipe peak itself: a kernel that issues only
- * independent mma.sync m8n8k4 .f64 instructions on every SM.  It also measures
- * the tcgen05 MMA issue rate by width.  No counterpart in the reference (it has
- * no performance instrumentation beyond wall time, main.cu:91-93).
+ * independent mma.sync m8n8k4 .f64 instructions on every SM.  No counterpart
+ * in the reference (it has no performance instrumentation beyond wall time,
+ * main.cu:91-93).
  */
 #ifndef GI_PROBE_H
 #define GI_PROBE_H
@@ -16,10 +16,6 @@ extern "C" {
 #endif
 /* Measured FP64 DMMA throughput of `device` in TFLOP/s (best of 3). */
 gi_status gi_measure_fp64_peak(int device, double* tflops);
-/* Cycles one tcgen05.mma kind::f16 (bf16, M = 128, K = 16) takes at width
-   n in {32, 48, 64, 96, 128, 256}, issued back to back on every SM; the
-   split-precision tile shapes follow from this rate. */
-gi_status gi_measure_mma_cycles(int device, int n, double* cycles);
 /* The split-precision GEMM alone on host arrays, for tests on arbitrary
    operands: C[n*M + m] = sum_k A[m*K + k] * B[n*K + k] with `slices` bf16
    digits per operand (0: the engine's default), on the kernel that the
