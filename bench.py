@@ -1,36 +1,42 @@
 #!/usr/bin/env python
 """Throughput benchmark of the GB300 line-intensity engine.
 
-Workload (default ``c2v_plain``): triatomic C2v, J = 0..10, Nvib = 2000,
-the lowest 1000 eigenvectors per (J, Gamma) under 15000 cm^-1, every
-dJ = 0, +-1 block pair; seeded synthetic inputs of those shapes (no TROVE
-checkpoints exist here).  One step = one whole intensity job over that
-input: every line S, A_if, I(T) after the reference's filters.
+Headline workload ``c3v_batched`` (the batched form): tetratomic C3v (A1, A2,
+E), J = 0..40, Nvib = 3000, up to 1500 eigenvectors per (J, Gamma) under
+12000 cm^-1 (blocks of ~1000 to 81000 functions, ~40 GB of vectors), every
+dJ = 0, +-1 block pair, T = 500 K; seeded synthetic inputs of those shapes (no
+TROVE checkpoints exist here).  All blocks stay resident in HBM.
 
-Metric: linestrengths/s, counting lines that pass every filter before the
-intensity threshold (1e-30 cm/molecule; the post-threshold count is reported
-beside it).
+A step is one batch of that job: the initial levels at positions
+l % 10 == shard of the energy-sorted level table against every final level,
+the split of initial levels the reference makes across devices
+(cuda_host.cu:1174).  Steps cycle through the ten shards, so ten steps are one
+whole job.  Metric: linestrengths/s, lines passing every filter before the
+intensity threshold (1e-30 cm/molecule; the post-threshold rate beside it).
 
-  value   inputs resident in HBM, lines kept on the device, CUDA-event time
-          of K steps on the engine's stream, bracketed by synchronize (and a
+  value   inputs resident in HBM, lines kept on the device, CUDA-event time of
+          K steps on the engine's stream, bracketed by synchronize (and a
           barrier across ranks); each step is one CUDA-graph launch
-  e2e     the same job through the C ABI from pinned host buffers: every step
-          uploads the dipole and every eigenvector block and reads all lines
-          back to host memory
-  roofline    the half-ls split GEMM's algorithmic TFLOP/s against the
-          measured bf16 peak, with its DRAM traffic
-  fp64_path / accuracy   the FP64 GPU path on the same job; split vs FP64
-          error per line on its J <= 3 part
-  serving     pair jobs arriving as a Poisson stream through gi_serve_*
-  dipole_streamed   the job with its dipole kept in host memory and streamed
-          in four panels
-  cpu_baseline / --impl reference   the reference's algorithm on the host
-          cores (the CPU oracle port; the reference has no CPU implementation
-          of the path) on a bounded sample of the same workload
+  e2e     the same steps through the C ABI from pinned host buffers: every step
+          uploads the dipole and every eigenvector block and reads the step's
+          lines back to host memory
+  roofline    the half-ls split GEMM (the dominant kernel): tensor-pipe rate of
+          its bf16 digit products against the measured bf16 peak, its FP64-
+          equivalent rate, and its DRAM traffic
+  fp64_path   the plain FP64 GPU path and the split path on the same batch (one
+          fortieth of the job)
+  accuracy    per-line error of both paths against the CPU oracle (double-double
+          checker) on a (J, J+1) sample of the workload
+  legs    the other workloads: c2v_plain (config 2: split and FP64 jobs),
+          c2v_precision (config 3: split and FP64 on one batch), serving (pair
+          jobs through gi_serve_*), the dipole streamed from host memory
+  cpu_baseline / --impl reference   the reference's algorithm restated in C
+          (plain FP64, the oracle port; the reference has no CPU path) on all
+          host cores, on the same bounded sample of the workload in both arms
 
-Multi-GPU (torchrun): every rank runs an independent replica of the job with
-its own seed (no collective on the data path), value = all ranks' lines /
-max time ("weak" scaling).
+Multi-GPU (torchrun): every rank runs an independent replica of the job with its
+own seed (no collective on the data path), value = all ranks' lines / max time
+("weak" scaling).
 """
 from __future__ import annotations
 
@@ -39,6 +45,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import threading
 import time
 
@@ -50,37 +57,44 @@ import __graft_entry__ as G  # noqa: E402
 
 METRIC = "linestrengths/s"
 THRESH_I = 1e-30  # cm/molecule
-# DRAM bytes (read + write) of one half-line-strength k_split_gemm_g launch per Y
-# column: ncu on the J <= 4 part of c2v_plain measured 62.14 GB + 6.54 GB for a
-# launch of 1000 x 96-column tiles.
-SPLIT_HALFLS_DRAM_BYTES_PER_COL = (62.136866e9 + 6.543222e9) / 96000
+SHARDS = {"c3v_batched": 10}
+# the CPU sample (both arms): one reference run (J, J+1) restricted to the
+# lowest initial levels
+CPU_SAMPLE = {"c3v_batched": ((20, 21), 2), "c2v_plain": ((9, 10), 8),
+              "c2v_small": ((0, 1), 4), "c3v_small": ((1, 2), 4)}
+# DRAM bytes (read + write) per Y column of one half-line-strength split GEMM
+# launch, from ncu captures (profiles/): N = 3000 (c3v) and N = 2000 (c2v)
+SPLIT_HALFLS_DRAM_BYTES_PER_COL = {3000: None, 2000: (62.136866e9 + 6.543222e9) / 96000}
 
 
-def parse():
+def parse(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2v_plain")
+    ap.add_argument("--workload", default="c3v_batched")
     ap.add_argument("--jmax", type=int, default=None, help="restrict J to 0..jmax")
+    ap.add_argument("--shards", type=int, default=None,
+                    help="batches per job (a step is one batch); default 10 for c3v_batched")
     ap.add_argument("--precision", default="split", choices=["fp64", "split"])
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--slices", type=int, default=0, help="bf16 digits per operand (split)")
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64-path comparison")
-    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
-    ap.add_argument("--no-stream", action="store_true",
-                    help="skip the streamed-dipole measurement")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--no-legs", action="store_true",
+                    help="skip the other workloads (c2v_plain, c2v_precision, serving, streamed)")
+    ap.add_argument("--legs", default="plain,precision,serving,streamed")
     ap.add_argument("--serve-jmax", type=int, default=4,
-                    help="serving: pair jobs of the J <= jmax part of the workload")
+                    help="serving: pair jobs of the J <= jmax part of c2v_plain")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: Poisson jobs/s")
     ap.add_argument("--serve-slots", type=int, default=3)
     ap.add_argument("--tune-table", default=None,
                     help="autotuner table file: read if present, extended and written")
-    return ap.parse_args()
+    return ap.parse_args(argv)
 
 
 def dist_env():
@@ -102,24 +116,36 @@ def across_ranks(dt, lines_pre, lines_post, device):
     return float(t.item()), int(n[0].item()), int(n[1].item())
 
 
-def make_problem(args, rank=0):
+def make_problem(args, rank=0, workload=None, jlist=None):
     G.load_package()
     from gpu_intensities_gb300 import synth
     kw = {}
-    if args.jmax is not None:
+    if jlist is not None:
+        kw["jlist"] = list(jlist)
+    elif args.jmax is not None:
         kw["jlist"] = list(range(args.jmax + 1))
-    prob = synth.workload(args.workload, seed=args.seed + rank, **kw)
+    prob = synth.workload(workload or args.workload, seed=args.seed + rank, **kw)
     prob.params.thresh_intensity = THRESH_I
     return prob
 
 
+def nshards_of(args):
+    return args.shards if args.shards else SHARDS.get(args.workload, 1)
+
+
 def config_of(args, prob):
+    vec_bytes = sum(b.vecs.nbytes for b in prob.blocks.values())
     return {"workload": args.workload, "sym": "C2v" if prob.sym_type == 1 else "C3v",
             "J": [min(prob.jlist), max(prob.jlist)], "Nvib": prob.N,
             "nvec_max_per_block": max(b.nvec for b in prob.blocks.values()),
+            "nsize_max": max(b.nsize for b in prob.blocks.values()),
             "levels": int(sum(b.nvec for b in prob.blocks.values())),
+            "eigenvector_bytes": int(vec_bytes), "T_K": prob.params.temperature,
+            "shards_per_job": nshards_of(args),
+            "step": "one shard: initial levels l % shards == step % shards of the level table, "
+                    "every final level",
             "precision": args.precision, "thresh_intensity_cm_per_molecule": THRESH_I,
-            "l2": "inputs (eigenvector blocks, 1.9 GB) larger than L2",
+            "l2": f"inputs ({vec_bytes / 1e9:.1f} GB of eigenvectors) larger than L2",
             "seed": args.seed}
 
 
@@ -185,74 +211,70 @@ class ClockSampler:
                 "samples": len(rows)}
 
 
-# ---------------------------------------------------------------- CPU baseline
-def cpu_sample(prob, nlow: int):
-    """Bounded sample of the workload for the oracle: the reference run over the
-    two highest J with only the nlow lowest initial levels kept (lower energy
-    window), every final level kept."""
+# ---------------------------------------------------------------- samples
+def sample_problem(args, workload):
+    """The bounded sample of a workload: the two J of one reference run, with
+    the initial levels restricted to the lowest few (lower energy window)."""
+    (j0, j1), nlow = CPU_SAMPLE[workload]
+    prob = make_problem(args, workload=workload, jlist=[j0, j1])
+    e = np.sort(np.concatenate([b.energies for b in prob.blocks.values()]))
+    cut = float(e[min(nlow, len(e)) - 1])
+    prob.params.erange_lower = (prob.params.erange_lower[0], cut)
+    return prob, (j0, j1), nlow
+
+
+def run_cpu(prob, pair, threads, precise):
     O = G.load_oracle()
-    js = prob.jlist
-    pair = (js[-2], js[-1])
-    zpe = O.resolve_zpe(prob)
-    e = np.sort(np.concatenate([prob.blocks[(J, g)].energies for J in pair
-                                for g in range(prob.nrep) if (J, g) in prob.blocks]))
-    cut = float(e[min(nlow, len(e)) - 1]) - (zpe if zpe > 0 else 0.0)
-    saved = prob.params.erange_lower
-    prob.params.erange_lower = (saved[0], cut)
-    return O, pair, zpe, saved
+    t = time.perf_counter()
+    lines = O.run_pair(prob, pair, None, nthreads=threads, precise=precise)
+    return lines, time.perf_counter() - t
 
 
-def run_cpu(prob, nlow: int, threads: int):
-    O, pair, zpe, saved = cpu_sample(prob, nlow)
-    try:
-        t = time.perf_counter()
-        lines = O.run_pair(prob, pair, zpe, nthreads=threads)
-        dt = time.perf_counter() - t
-    finally:
-        prob.params.erange_lower = saved
-    return len(lines), dt, pair
-
-
-def cpu_baseline(prob, nlow=8):
+def cpu_baseline(args):
+    prob, pair, nlow = sample_problem(args, args.workload)
     threads = os.cpu_count() or 1
-    n, dt, pair = run_cpu(prob, nlow, threads)
-    return {"value": n / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"oracle run over J={pair[0]},{pair[1]} restricted to the {nlow} lowest "
-                      f"initial levels ({n} lines in {dt:.1f} s)"}
+    lines, dt = run_cpu(prob, pair, threads, precise=False)
+    return {"value": len(lines) / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{args.workload}: the reference run over J={pair[0]},{pair[1]} with the "
+                      f"{nlow} lowest initial levels ({len(lines)} lines in {dt:.1f} s), the "
+                      f"reference's algorithm restated in C, plain FP64, OpenMP"}
 
 
 # ---------------------------------------------------------------- accuracy
-def split_accuracy(pkg, prob, slices, device):
-    """Split path against the FP64 GPU path (itself parity-tested against the
-    CPU oracle) on the J <= 3 part of the workload: identical line selection
-    and the per-line relative error of S."""
-    from gpu_intensities_gb300 import synth
-    sub = synth.Problem(prob.sym_type, prob.N, prob.mu,
-                        {J: b for J, b in prob.bases.items() if J <= 3},
-                        {k: b for k, b in prob.blocks.items() if k[0] <= 3}, prob.params,
-                        name=prob.name + "_J0-3")
-    out = {}
-    for name, prec in (("fp64", pkg.GI_PREC_FP64), ("split", pkg.GI_PREC_SPLIT)):
-        with pkg.Engine(device) as e:
-            e.load(sub, precision=prec, split_slices=slices)
-            e.run()
-            out[name] = pkg.keyed(e.lines(), e.levels())
-    a, b = out["fp64"], out["split"]
+def _sorted_keyed(lines):
     keys = ("jI", "gammaI", "recI", "jF", "gammaF", "recF")
-    a = a[np.lexsort(tuple(a[k] for k in reversed(keys)))]
-    b = b[np.lexsort(tuple(b[k] for k in reversed(keys)))]
-    same = len(a) == len(b) and all(np.array_equal(a[k], b[k]) for k in keys)
-    res = {"sample": "J<=3 part of the workload, split vs FP64 GPU path",
-           "lines": int(len(a)), "identical_selection": bool(same)}
-    if same and len(a):
-        rel = np.abs(b["S"] - a["S"]) / np.where(a["S"] > 0, a["S"], 1.0)
-        tmax = np.abs(a["t"]).max()
-        well = np.abs(a["t"]).max(axis=1) >= 1e-4 * tmax
-        res.update({"rel_err_S_max": float(rel.max()), "rel_err_S_p99": float(np.quantile(rel, 0.99)),
-                    "rel_err_S_max_well_conditioned": float(rel[well].max()),
-                    "well_conditioned_fraction": float(well.mean()),
-                    "note": "well conditioned: |t| >= 1e-4 max|t| (no cancellation beyond 1e4)"})
-    return res
+    return lines[np.lexsort(tuple(lines[k] for k in reversed(keys)))], keys
+
+
+def compare_lines(got, ref):
+    """Identical selection and the per-line relative error of S against the
+    oracle, on every line (all lines here are above the intensity threshold)."""
+    g, keys = _sorted_keyed(got)
+    r, _ = _sorted_keyed(ref)
+    same = len(g) == len(r) and all(np.array_equal(g[k], r[k]) for k in keys)
+    out = {"lines": int(len(r)), "identical_selection": bool(same)}
+    if same and len(r):
+        rel = np.abs(g["S"] - r["S"]) / np.abs(r["S"])
+        out.update({"rel_err_S_max": float(rel.max()), "rel_err_S_p99": float(np.quantile(rel, 0.99)),
+                    "rel_err_I_max": float((np.abs(g["I"] - r["I"]) / np.abs(r["I"])).max())})
+    return out
+
+
+def accuracy_vs_oracle(pkg, args, device, workload):
+    """Both GPU paths against the CPU oracle (double-double checker) on the
+    bounded sample of the workload."""
+    prob, pair, nlow = sample_problem(args, workload)
+    ref, dt = run_cpu(prob, pair, os.cpu_count() or 1, precise=True)
+    out = {"sample": f"{workload}: reference run J={pair[0]},{pair[1]}, the {nlow} lowest initial "
+                     f"levels, every line above the intensity threshold",
+           "oracle_seconds": dt}
+    for name, prec in (("split", pkg.GI_PREC_SPLIT), ("fp64", pkg.GI_PREC_FP64)):
+        with pkg.Engine(device) as e:
+            e.load(prob, precision=prec, split_slices=args.slices)
+            e.run()
+            got = pkg.keyed(e.lines(), e.levels())
+        out[name] = compare_lines(got, ref)
+    return out
 
 
 # ---------------------------------------------------------------- reference arm
@@ -260,26 +282,29 @@ def main_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    prob = make_problem(args)
+    prob, pair, nlow = sample_problem(args, args.workload)
     threads = os.cpu_count() or 1
-    nlow = 4
     for _ in range(args.warmup):
-        run_cpu(prob, nlow, threads)
+        run_cpu(prob, pair, threads, precise=False)
     tot_n, tot_t = 0, 0.0
     for _ in range(args.steps):
-        n, dt, pair = run_cpu(prob, nlow, threads)
-        tot_n += n
+        lines, dt = run_cpu(prob, pair, threads, precise=False)
+        tot_n += len(lines)
         tot_t += dt
     v = tot_n / tot_t
+    cfg = {"workload": args.workload, "sample_of": args.workload, "J": list(pair),
+           "initial_levels": nlow, "precision": "fp64",
+           "thresh_intensity_cm_per_molecule": THRESH_I, "seed": args.seed}
     out = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC,
            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * tot_t / args.steps, "higher_is_better": True,
            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-           "config": config_of(args, prob),
+           "config": cfg,
            "cpu_baseline": {"value": v, "unit": METRIC, "cores": threads, "kind": "port",
-                            "sample": f"oracle (the reference's algorithm restated in C; the "
-                                      f"reference has no CPU path) over J={pair[0]},{pair[1]} "
-                                      f"with the {nlow} lowest initial levels per step"},
+                            "sample": f"the reference's algorithm restated in C (plain FP64, "
+                                      f"OpenMP; the reference has no CPU path) over "
+                                      f"J={pair[0]},{pair[1]} with the {nlow} lowest initial "
+                                      f"levels per step"},
            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0,
                    "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
@@ -288,13 +313,10 @@ def main_reference(args):
 
 # ---------------------------------------------------------------- serving
 def serve_bench(pkg, args, device, precision):
-    """Pair jobs (J, Gamma) -> (J', Gamma') of the J <= serve_jmax part of the
-    workload, submitted in random order with Poisson arrivals at serve_rate
+    """Pair jobs (J, Gamma) -> (J', Gamma') of the J <= serve_jmax part of
+    c2v_plain, submitted in random order with Poisson arrivals at serve_rate
     jobs/s to a serving context; latency is submit -> lines on the host."""
-    import argparse as _a
-    sub = _a.Namespace(**vars(args))
-    sub.jmax = args.serve_jmax
-    prob = make_problem(sub)
+    prob = make_problem(args, workload="c2v_plain", jlist=range(args.serve_jmax + 1))
     jobs = prob.pair_jobs()
     rng = np.random.default_rng(args.seed + 17)
     order = [jobs[i] for i in rng.permutation(len(jobs))]
@@ -318,7 +340,7 @@ def serve_bench(pkg, args, device, precision):
         makespan = time.perf_counter() - t0
         st = eng.serve_stats()
         eng.serve_stop()
-    return {"workload": f"{args.workload} J<={args.serve_jmax} pair jobs", "jobs": len(order),
+    return {"workload": f"c2v_plain J<={args.serve_jmax} pair jobs", "jobs": len(order),
             "arrival": f"Poisson {args.serve_rate:g} jobs/s, random order",
             "slots": st["slots"], "precision": "split" if precision else "fp64",
             "latency_p50_s": st["latency_p50"], "latency_p99_s": st["latency_p99"],
@@ -330,6 +352,148 @@ def serve_bench(pkg, args, device, precision):
             "budget_bytes": st["budget_bytes"], "peak_resident_bytes": st["peak_resident_bytes"]}
 
 
+# ---------------------------------------------------------------- helpers
+class Timer:
+    """Device seconds of a callable's launches: CUDA events on the engine's
+    stream, bracketed by synchronize and a barrier across ranks."""
+
+    def __init__(self, torch, stream, barrier):
+        self.torch, self.stream, self.barrier = torch, stream, barrier
+
+    def __call__(self, k, fn):
+        torch = self.torch
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        self.barrier()
+        a.record(self.stream)
+        out = [fn(i) for i in range(k)]
+        b.record(self.stream)
+        torch.cuda.synchronize()
+        self.barrier()
+        return a.elapsed_time(b) * 1e-3, out
+
+
+def register_host(torch, arrays):
+    """Page-lock numpy arrays in place (cudaHostRegister), so that copies from
+    them run at pinned-memory speed without a second host copy."""
+    rt = torch.cuda.cudart()
+    done = []
+    for a in arrays:
+        if a.nbytes and int(rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0:
+            done.append(a)
+    return done
+
+
+def unregister_host(torch, arrays):
+    rt = torch.cuda.cudart()
+    for a in arrays:
+        rt.cudaHostUnregister(a.ctypes.data)
+
+
+def split_roofline(prob, ps, peaks):
+    """The dominant kernel of the split path: the half-line-strength digit GEMM
+    (k_split_gemm_g, one launch per round)."""
+    sp, lp = ps["seconds_phase"], ps["launches_phase"]
+    dom = "halfls_gemm"
+    pairs = ps["flops_tensor"] / max(ps["flops_halfls"] + ps["flops_final"], 1.0)
+    flops = pairs * ps["flops_halfls"]
+    ncol = ps["flops_halfls"] / (6.0 * prob.N * prob.N)
+    peak = peaks.get("bf16_tflops", 1900.0)
+    achieved = flops / sp[dom] / 1e12 if sp[dom] else 0.0
+    per_col = SPLIT_HALFLS_DRAM_BYTES_PER_COL.get(prob.N)
+    return {"bound": "tensor", "kernel": "k_split_gemm_g (tcgen05 bf16 digit GEMM, grouped digit "
+                                         "layout, half line strength)",
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+            "traffic": per_col * ncol / max(lp[dom], 1) if per_col else None,
+            "traffic_source": "ncu dram__bytes_read+write of this kernel per Y column on a small "
+                              "case of the same Nvib, scaled by Y columns" if per_col else
+                              "not captured for this Nvib",
+            "achieved_meaning": "bf16 tensor-pipe rate: digit-pair products x 2 x M x N x K",
+            "tensor_tflop_per_launch": flops / max(lp[dom], 1) / 1e12,
+            "digit_pair_products": pairs,
+            "fp64_equivalent_tflops": ps["flops_halfls"] / sp[dom] / 1e12 if sp[dom] else 0.0,
+            "fp64_algorithmic_tflop_per_launch": ps["flops_halfls"] / max(lp[dom], 1) / 1e12,
+            "both_gemms_tflops": ps["flops_tensor"] / (sp["halfls_gemm"] + sp["final_gemm"]) / 1e12,
+            "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"
+            if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s",
+            "phase_seconds": {k: round(v, 6) for k, v in sp.items()},
+            "phase_launches": lp, "launch_avg_ms": 1e3 * sp[dom] / max(lp[dom], 1)}
+
+
+# ---------------------------------------------------------------- legs
+def leg_c2v_plain(pkg, args, device, timer_of):
+    """Config 2: the whole C2v J = 0..10 job per step, split and FP64."""
+    import torch
+    prob = make_problem(args, workload="c2v_plain")
+    out = {"workload": "c2v_plain: C2v, J=0..10, Nvib=2000, <=1000 vectors per (J, Gamma); one "
+                       "step = the whole job"}
+    with pkg.Engine(device) as eng:
+        stream = torch.cuda.Stream(device=device)
+        eng.set_stream(stream.cuda_stream)
+        timer = timer_of(stream)
+        eng.load(prob, precision=pkg.GI_PREC_SPLIT, split_slices=args.slices)
+        for _ in range(3):
+            eng.run(lines_on_device=True, graph=True)
+        dt, n = timer(3, lambda i: (eng.run(lines_on_device=True, graph=True),
+                                    eng.stats()["nlines_filtered"])[1])
+        out["split"] = {"value": sum(n) / dt, "unit": METRIC, "ms_per_step": 1e3 * dt / 3,
+                        "steps": 3, "lines_per_step": n[-1]}
+        eng.set_params(prob.params, precision=pkg.GI_PREC_FP64)
+        eng.run(lines_on_device=True, graph=True)
+        dt, n = timer(1, lambda i: (eng.run(lines_on_device=True, graph=True),
+                                    eng.stats()["nlines_filtered"])[1])
+        out["fp64"] = {"value": sum(n) / dt, "unit": METRIC, "ms_per_step": 1e3 * dt, "steps": 1}
+    out["speedup_split_over_fp64"] = out["split"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def leg_c2v_precision(pkg, args, device, timer_of):
+    """Config 3: C2v J = 20 -> 21, Nvib = 5000, 2000 vectors per block of ~26k,
+    log-uniform dipole; split and FP64 on the same batch (one tenth of the
+    initial levels)."""
+    import torch
+    prob = make_problem(args, workload="c2v_precision")
+    S = 10
+    out = {"workload": "c2v_precision: C2v, J=20,21, Nvib=5000, 2000 vectors per block, nsize "
+                       f"~26k, dipole log-uniform 1e-8..1; one step = shard 0 of {S}"}
+    with pkg.Engine(device) as eng:
+        stream = torch.cuda.Stream(device=device)
+        eng.set_stream(stream.cuda_stream)
+        timer = timer_of(stream)
+        for name, prec, k in (("split", pkg.GI_PREC_SPLIT, 3), ("fp64", pkg.GI_PREC_FP64, 1)):
+            if name == "split":
+                eng.load(prob, precision=prec, split_slices=args.slices)
+            else:
+                eng.set_params(prob.params, precision=prec)
+            eng.run(lines_on_device=True, graph=True, shard=0, nshards=S)
+            dt, n = timer(k, lambda i: (eng.run(lines_on_device=True, graph=True, shard=0,
+                                                nshards=S), eng.stats()["nlines_filtered"])[1])
+            out[name] = {"value": sum(n) / dt, "unit": METRIC, "ms_per_step": 1e3 * dt / k,
+                         "steps": k, "lines_per_step": n[-1]}
+    out["speedup_split_over_fp64"] = out["split"]["value"] / out["fp64"]["value"]
+    return out
+
+
+def leg_streamed(pkg, eng, prob, timer, S, value_rate):
+    """The headline batch with the dipole kept in host memory and streamed
+    through the device in four panels per half-ls GEMM (copies overlap)."""
+    rows = -(-prob.N // 4)
+    rows = -(-rows // 128) * 128
+    eng.set_dipole_streamed(prob.N, prob.mu, panel_rows=rows)
+    eng.run(lines_on_device=True, shard=0, nshards=S)
+    ts, n = timer(1, lambda i: (eng.run(lines_on_device=True, shard=0, nshards=S),
+                                eng.stats())[1])
+    ss = n[-1]
+    nr = ss["launches_phase"]["halfls_gemm"] // -(-prob.N // rows)
+    eng.set_dipole(prob.N, prob.mu)
+    return {"value": ss["nlines_filtered"] / ts, "unit": METRIC, "ms_per_step": 1e3 * ts,
+            "steps": 1, "panel_rows": rows, "panels": -(-prob.N // rows), "rounds": int(nr),
+            "h2d_bytes_per_step": int(nr * 3 * prob.N * prob.N * 8),
+            "vs_resident": (ss["nlines_filtered"] / ts) / value_rate,
+            "graph": "eager launches (a streamed dipole is not captured)"}
+
+
 # ---------------------------------------------------------------- our arm
 def main_ours(args):
     import torch
@@ -339,203 +503,172 @@ def main_ours(args):
         dist.init_process_group("nccl")
         torch.cuda.set_device(local)
     pkg = G.load_package()
-    prob = make_problem(args, rank)
     prec = pkg.GI_PREC_SPLIT if args.precision == "split" else pkg.GI_PREC_FP64
+    S = nshards_of(args)
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
+    def timer_of(stream):
+        return Timer(torch, stream, barrier)
+
+    t_setup = time.perf_counter()
+    prob = make_problem(args, rank)
+    cfg = config_of(args, prob)
     eng = pkg.Engine(local)
     eng.load(prob, precision=prec, split_slices=args.slices)
+    setup_s = time.perf_counter() - t_setup
     # the warm-up steps also tune the split GEMM launch configurations
-    import tempfile
     tune_path = args.tune_table or os.path.join(tempfile.gettempdir(),
                                                 f"gi_tune_{os.getpid()}.txt")
     eng.set_tuning(1, tune_path)
     # the engine's launches go to this stream, so its CUDA events bracket them
     stream = torch.cuda.Stream(device=local)
     eng.set_stream(stream.cuda_stream)
+    timer = timer_of(stream)
 
-    def timed_steps(k, fn):
-        """Device seconds per step of k calls of fn, CUDA events on the stream."""
-        a = torch.cuda.Event(enable_timing=True)
-        b = torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        barrier()
-        a.record(stream)
-        out = None
-        for _ in range(k):
-            out = fn()
-        b.record(stream)
-        torch.cuda.synchronize()
-        barrier()
-        return a.elapsed_time(b) * 1e-3 / k, out
+    def step(i):
+        eng.run(lines_on_device=True, graph=True, shard=i % S, nshards=S)
+        return eng.stats()
 
-    for _ in range(args.warmup):
-        eng.run(lines_on_device=True, graph=True)
+    for w in range(args.warmup):
+        step(w)
+    eng.set_tuning(0, tune_path)  # tuned: later shards are captured on their first run
     autotune = []
     if os.path.exists(tune_path):
         names = {"0": "one-pass", "1": "two-pass (split at s/2)", "2": "two-pass (split at s - s/2)",
-                 "6": "grouped layout, two-pass (s/2)",
-                 "7": "grouped layout, two-pass (s - s/2)", "8": "grouped layout, one-pass"}
+                 "6": "grouped layout, two-pass (s/2)", "7": "grouped layout, two-pass (s - s/2)",
+                 "8": "grouped layout, one-pass"}
         for line in open(tune_path).read().splitlines():
             s_, nA, nb, K, layout, kind, ga, ms = line.split()
             autotune.append({"digits": int(s_), "row_tiles": int(nA), "cols_bucket": 2 ** int(nb),
-                             "K": int(K), "kernel": names[kind], "l2_group_mb": int(ga),
+                             "K": int(K), "kernel": names.get(kind, kind), "l2_group_mb": int(ga),
                              "ms": float(ms)})
-    stats = []
-
-    def one():
-        eng.run(lines_on_device=True, graph=True)
-        stats.append(eng.stats())
 
     with ClockSampler(local) as clk:
         t0 = time.perf_counter()
-        dt, _ = timed_steps(args.steps, one)
+        dt, stats = timer(args.steps, step)
         t1 = time.perf_counter()
     wall = (t1 - t0) / args.steps
-    lines_pre = stats[-1]["nlines_filtered"]
-    lines_post = stats[-1]["nlines"]
+    lines_pre = int(sum(s["nlines_filtered"] for s in stats))
+    lines_post = int(sum(s["nlines"] for s in stats))
     launches = int(sum(s["kernel_launches"] for s in stats))
+    value_rate = lines_pre / dt
 
     # roofline of the dominant kernel: one more step with per-kernel events
-    eng.run(lines_on_device=True, phase_timing=True)
+    eng.run(lines_on_device=True, phase_timing=True, shard=0, nshards=S)
     ps = eng.stats()
-    sp = ps["seconds_phase"]
-    lp = ps["launches_phase"]
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except OSError:
         pass
     if args.precision == "split":
-        # the dominant launch: the half-line-strength split GEMM (k_split_gemm_g),
-        # one launch per step; digit-pair products x 2 x 3 x N x N x Y columns
-        dom = "halfls_gemm"
-        pairs = ps["flops_tensor"] / max(ps["flops_halfls"] + ps["flops_final"], 1.0)
-        flops = pairs * ps["flops_halfls"]
-        ncol = ps["flops_halfls"] / (6.0 * prob.N * prob.N)
-        peak = peaks.get("bf16_tflops", 1900.0)
-        achieved = flops / sp[dom] / 1e12 if sp[dom] else 0.0
-        roof = {"bound": "tensor", "kernel": "k_split_gemm_g (tcgen05 bf16 digit GEMM, "
-                                             "grouped digit layout, half line strength)",
-                "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                "frac": achieved / peak,
-                "traffic": SPLIT_HALFLS_DRAM_BYTES_PER_COL * ncol / lp[dom],
-                "traffic_source": "ncu dram__bytes_read+write of this kernel on the J<=4 part "
-                                  "of the workload, scaled by Y columns",
-                "algorithmic_tflop_per_launch": flops / lp[dom] / 1e12,
-                "digit_pair_products": pairs,
-                "both_gemms_tflops": ps["flops_tensor"] /
-                (sp["halfls_gemm"] + sp["final_gemm"]) / 1e12,
-                "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"
-                if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s"}
+        roof = split_roofline(prob, ps, peaks)
     else:
-        dom = "halfls_gemm"
+        sp, lp = ps["seconds_phase"], ps["launches_phase"]
         fp64_peak = pkg.measure_fp64_peak(local)  # TFLOP/s, DMMA m8n8k4, measured live
-        achieved = ps["flops_halfls"] / sp[dom] / 1e12 if sp[dom] else 0.0
+        achieved = ps["flops_halfls"] / sp["halfls_gemm"] / 1e12 if sp["halfls_gemm"] else 0.0
         roof = {"bound": "tensor", "kernel": "k_gemm_fp64_nt (FP64 DMMA, half line strength)",
                 "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": None,
                 "peak_source": "FP64 DMMA peak measured live by gi_measure_fp64_peak "
-                               "(of measured); MEASURED_PEAKS.json has no FP64 entry"}
-    roof["phase_seconds"] = {k: round(v, 6) for k, v in sp.items()}
-    roof["phase_launches"] = lp
-    roof["launch_avg_ms"] = 1e3 * sp[dom] / max(lp[dom], 1)
+                               "(of measured); MEASURED_PEAKS.json has no FP64 entry",
+                "phase_seconds": sp, "phase_launches": lp}
+    roof["measured_on"] = f"shard 0 of {S}, per-kernel CUDA events on the engine's stream"
 
     # end to end through the C ABI from pinned host buffers
     e2e = None
     if not args.no_e2e:
-        pin = {}
-        mu = torch.from_numpy(prob.mu).pin_memory()
-        for k, b in prob.blocks.items():
-            pin[k] = torch.from_numpy(np.ascontiguousarray(b.vecs)).pin_memory()
-        h2d = mu.numel() * 8 + sum(v.numel() * 8 for v in pin.values())
-        ne = args.e2e_steps or args.steps
-
+        arrays = [prob.mu] + [b.vecs for _, b in sorted(prob.blocks.items())]
+        pinned = register_host(torch, arrays)
+        h2d = sum(a.nbytes for a in arrays)
         parts = {"upload_ms": 0.0, "run_ms": 0.0}
+        d2h = []
 
-        def step():
-            t0 = time.perf_counter()
-            eng.set_dipole(prob.N, mu.numpy())
+        def e2e_step(i):
+            ta = time.perf_counter()
+            eng.set_dipole(prob.N, prob.mu)
             for (J, g), b in sorted(prob.blocks.items()):
-                eng.set_block(J, g, pin[(J, g)].numpy(), b.energies, b.quanta)
-            t1 = time.perf_counter()
-            n = eng.run(lines_on_device=False, graph=True)
-            parts["upload_ms"] += 1e3 * (t1 - t0)
-            parts["run_ms"] += 1e3 * (time.perf_counter() - t1)
-            return n
+                eng.set_block(J, g, b.vecs, b.energies, b.quanta)
+            tb = time.perf_counter()
+            n = eng.run(lines_on_device=False, graph=True, shard=i % S, nshards=S)
+            parts["upload_ms"] += 1e3 * (tb - ta)
+            parts["run_ms"] += 1e3 * (time.perf_counter() - tb)
+            d2h.append(n * 80 + 16)
+            return eng.stats()["nlines_filtered"]
 
-        step()
+        e2e_step(0)
         parts["upload_ms"] = parts["run_ms"] = 0.0
-        te, n = timed_steps(ne, step)
-        st = eng.stats()
-        e2e = {"value": world * st["nlines_filtered"] / te, "unit": METRIC,
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(n * 80 + 16),
-               "ms_per_step": 1e3 * te, "steps": ne,
+        d2h.clear()
+        ne = args.e2e_steps
+        te, n = timer(ne, e2e_step)
+        unregister_host(torch, pinned)
+        e2e = {"value": world * sum(n) / te, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": 1e3 * te / ne,
+               "steps": ne, "host_pinned": bool(len(pinned) == len(arrays)),
                "host_wall_ms_per_step": {k: v / ne for k, v in parts.items()},
-               "last_run_ms": {"wall": 1e3 * st["seconds_total"], "device": 1e3 * st["seconds_gpu"]}}
+               "note": "each step re-uploads the dipole and every block from page-locked host "
+                       "memory, re-cuts the digit planes and reads the shard's lines back"}
 
-    # the same job with the dipole kept in host memory and streamed through
-    # the device in four panels per half-ls GEMM (copies overlap the GEMMs)
-    streamed = None
-    if not args.no_stream:
-        rows = -(-prob.N // 4)
-        rows = -(-rows // 128) * 128
-        eng.set_dipole_streamed(prob.N, prob.mu, panel_rows=rows)
-        eng.run(lines_on_device=True)  # warm-up (and tuning of the panel GEMM shapes)
-        ts, _ = timed_steps(1, lambda: eng.run(lines_on_device=True))
-        ss = eng.stats()
-        nr = ss["launches_phase"]["halfls_gemm"] // -(-prob.N // rows)  # GEMM rounds per step
-        streamed = {"value": world * ss["nlines_filtered"] / ts, "unit": METRIC,
-                    "ms_per_step": 1e3 * ts, "steps": 1, "warmup": 1, "panel_rows": rows,
-                    "panels": -(-prob.N // rows), "rounds": int(nr),
-                    "h2d_bytes_per_step": int(nr * 3 * prob.N * prob.N * 8),
-                    "vs_resident": (ss["nlines_filtered"] / ts) / (lines_pre / dt),
-                    "graph": "eager launches (a streamed dipole is not captured)"}
-        eng.set_dipole(prob.N, prob.mu)
-
-    # the plain FP64 GPU path on the same job, and per-line accuracy of the
-    # split path against it on the J <= 3 part of the workload
-    fp64 = accuracy = None
+    # the plain FP64 GPU path and the split path on the same batch
+    fp64 = None
     if args.precision == "split" and not args.no_fp64:
-        eng.set_params(prob.params, precision=pkg.GI_PREC_FP64)
-        eng.run(lines_on_device=True, graph=True)
-        tf, _ = timed_steps(1, lambda: eng.run(lines_on_device=True, graph=True))
-        fs = eng.stats()
-        fp64 = {"value": world * fs["nlines_filtered"] / tf, "unit": METRIC,
-                "ms_per_step": 1e3 * tf, "steps": 1, "warmup": 1,
-                "speedup_split_over_fp64": (lines_pre / dt) / (fs["nlines_filtered"] / tf)}
+        S4 = 4 * S
+        res = {}
+        for name, p in (("split", pkg.GI_PREC_SPLIT), ("fp64", pkg.GI_PREC_FP64)):
+            eng.set_params(prob.params, precision=p, split_slices=args.slices)
+            eng.run(lines_on_device=True, graph=True, shard=0, nshards=S4)
+            tf, n = timer(1, lambda i: (eng.run(lines_on_device=True, graph=True, shard=0,
+                                                nshards=S4), eng.stats()["nlines_filtered"])[1])
+            res[name] = {"value": world * n[0] / tf, "unit": METRIC, "ms_per_step": 1e3 * tf,
+                         "lines": n[0]}
         eng.set_params(prob.params, precision=prec, split_slices=args.slices)
-        accuracy = split_accuracy(pkg, prob, args.slices, local)
+        fp64 = {"batch": f"shard 0 of {S4} of the job (one fortieth of the initial levels, every "
+                         f"final level)", "fp64": res["fp64"], "split": res["split"],
+                "speedup_split_over_fp64": res["split"]["value"] / res["fp64"]["value"]}
 
-    serving = None
-    if not args.no_serve and world == 1:
-        serving = {"split": serve_bench(pkg, args, local, pkg.GI_PREC_SPLIT)}
-        if not args.no_fp64:
-            serving["fp64"] = serve_bench(pkg, args, local, pkg.GI_PREC_FP64)
+    streamed = None
+    if not args.no_legs and "streamed" in args.legs and world == 1:
+        streamed = leg_streamed(pkg, eng, prob, timer, S, value_rate)
+    eng.close()
+    del prob
+
+    legs = {}
+    if not args.no_legs and world == 1:
+        if "plain" in args.legs and args.workload != "c2v_plain":
+            legs["c2v_plain"] = leg_c2v_plain(pkg, args, local, timer_of)
+        if "precision" in args.legs and args.workload != "c2v_precision":
+            legs["c2v_precision"] = leg_c2v_precision(pkg, args, local, timer_of)
+        if "serving" in args.legs:
+            legs["serving"] = {"split": serve_bench(pkg, args, local, pkg.GI_PREC_SPLIT)}
+    accuracy = None
+    if not args.no_accuracy and world == 1 and args.workload in CPU_SAMPLE:
+        accuracy = accuracy_vs_oracle(pkg, args, local, args.workload)
 
     dt, lines_all, lines_all_post = across_ranks(dt, lines_pre, lines_post, "cuda")
-    out = None
     if rank == 0:
         out = {"metric": METRIC, "value": lines_all / dt, "unit": METRIC,
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-               "ms_per_step": 1e3 * dt, "wall_ms_per_step": 1e3 * wall,
-               "higher_is_better": True, "scaling": "weak",
-               "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-               "config": config_of(args, prob),
-               "lines_per_step": lines_pre, "lines_above_threshold_per_step": lines_post,
+               "ms_per_step": 1e3 * dt / args.steps, "wall_ms_per_step": 1e3 * wall,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "split-bf16x9" if args.precision == "split" and args.slices in (0, 9)
+               else (f"split-bf16x{args.slices}" if args.precision == "split" else "f64"),
+               "dtype_note": "bf16 digit products with exact integer accumulation, FP64 "
+                             "epilogue (S, A, I, filters in FP64)" if args.precision == "split"
+               else "FP64 throughout",
+               "data": "synthetic", "config": cfg,
+               "lines_per_step": lines_pre / args.steps,
                "value_above_threshold": lines_all_post / dt,
-               "gpu_launches": launches, "graph": "each step is one CUDA graph launch (captured "
-               "in warm-up, replayed)", "autotune": autotune, "roofline": roof, "e2e": e2e,
-               "fp64_path": fp64, "accuracy": accuracy, "serving": serving,
-               "dipole_streamed": streamed,
-               "clocks": clk.summary()}
-        if world == 1 and not args.no_cpu_baseline:
-            out["cpu_baseline"] = cpu_baseline(prob)
+               "gpu_launches": launches,
+               "graph": "each step is one CUDA graph launch (one graph per shard)",
+               "setup_s": setup_s, "autotune": autotune, "roofline": roof, "e2e": e2e,
+               "fp64_path": fp64, "accuracy": accuracy, "dipole_streamed": streamed,
+               "legs": legs, "clocks": clk.summary()}
+        if world == 1 and not args.no_cpu_baseline and args.workload in CPU_SAMPLE:
+            out["cpu_baseline"] = cpu_baseline(args)
         print(json.dumps(out))
-    eng.close()
     if world > 1:
         torch.distributed.destroy_process_group()
     return 0

@@ -166,6 +166,7 @@ def lib():
         L.gi_set_block_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.c_void_p, f64p, i32p]
         L.gi_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]
+        L.gi_run_shard.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]
         L.gi_deck_parse.argtypes = [C.c_char_p, C.POINTER(gi_deck), C.c_char_p, C.c_size_t]
         L.gi_trove_read_basis.argtypes = [C.c_char_p, C.c_int, C.c_int, i32p, i32p, i32p, i32p,
                                           i32p, i32p, i32p, C.POINTER(f64p), C.c_char_p,
@@ -450,11 +451,16 @@ class Engine:
 
     # run -----------------------------------------------------------------
     def run(self, lines_on_device: bool = False, phase_timing: bool = False,
-            graph: bool = False) -> int:
+            graph: bool = False, shard: int = 0, nshards: int = 1) -> int:
+        """gi_run, or with nshards > 1 gi_run_shard: the initial levels at
+        positions l % nshards == shard of the level table."""
         n = C.c_int64(0)
         flags = (GI_RUN_LINES_ON_DEVICE if lines_on_device else 0) | \
             (GI_RUN_PHASE_TIMING if phase_timing else 0) | (GI_RUN_GRAPH if graph else 0)
-        self._ck(self._L.gi_run(self._h, flags, C.byref(n)))
+        if nshards > 1:
+            self._ck(self._L.gi_run_shard(self._h, flags, shard, nshards, C.byref(n)))
+        else:
+            self._ck(self._L.gi_run(self._h, flags, C.byref(n)))
         return int(n.value)
 
     def lines(self, offset: int = 0, count: Optional[int] = None) -> np.ndarray:

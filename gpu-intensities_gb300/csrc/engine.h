@@ -96,6 +96,14 @@ struct Basis {
   // (slot, v) -> roots CSR; depends on the dipole size N
   int y_N = -1;
   DevArray<int32_t> d_yptr, d_yroot;
+  // largest iroot_correlat_j0 (checked against N without a pass over the roots)
+  int32_t iroot_max = -1;
+  // device copies of the key -> slot map and of the half-line-strength terms
+  // towards J-1, J, J+1 ([jF - J + 1]; (2 jF + 2) * 6 terms and 2 jF + 2
+  // counts), built when the basis or the 3j table is set
+  DevArray<int32_t> d_slot_of_key;
+  DevArray<StencilTerm> d_pair_st[3];
+  DevArray<int32_t> d_pair_stn[3];
 };
 
 struct Block {
@@ -218,12 +226,21 @@ struct Ctx {
   size_t ck_cap = 0;
   cudaStream_t d2h = nullptr;
 
-  // CUDA graph of the last captured launch sequence (GI_RUN_GRAPH) and the
-  // plan it was captured for
-  cudaGraphExec_t gexec = nullptr;
-  uint64_t gsig = 0, gpending = 0;
-  gi_stats gstats{};
+  // CUDA graphs of captured launch sequences (GI_RUN_GRAPH), one per plan
+  // signature, the most recently used first (at most kGraphCache): runs that
+  // alternate between plans (the shards of a job) replay each one's graph
+  struct GraphEntry {
+    uint64_t sig = 0;
+    cudaGraphExec_t exec = nullptr;
+    gi_stats stats{};  // what the captured sequence adds to a run's counts
+  };
+  static constexpr size_t kGraphCache = 16;
+  std::vector<GraphEntry> graphs;
+  uint64_t gpending = 0;
   int64_t graph_replays = 0;
+  // the part of the initial levels this run takes (gi_run_shard): levels at
+  // positions l of the energy-sorted table with l % nshards == shard
+  int shard = 0, nshards = 1;
 
   // workspaces
   DevArray<double> w_y, w_z, w_h, w_t, w_EI;
@@ -266,6 +283,9 @@ double partition_sum(const Ctx* c, double temperature, double zpe);
 gi_status run_job(Ctx* c, int flags, int64_t* nlines_out);
 // Builds the (slot, v) -> roots table of a basis for the context's dipole size.
 gi_status ensure_ycsr(Ctx* c, Basis& b);
+// Device tables of every basis's half-line-strength terms towards J-1, J, J+1
+// (Basis::d_pair_st), from the context's 3j table where it covers the pair.
+gi_status refresh_pair_tables(Ctx* c, Basis* only = nullptr);
 // Serving: frees device memory for `bytes` more by evicting unpinned blocks
 // other than `keep` (least recently used first).  Caller holds model_mu.
 gi_status server_make_room(Ctx* c, size_t bytes, Block* keep);
@@ -321,7 +341,7 @@ double three_j(int j1, int j2, int j3, int k1, int k2, int k3);
 void precompute_threej(int jmax, std::vector<double>& out);
 // Half-line-strength terms for every final key (2*jF+2 keys, 6 slots each);
 // threej may be null, in which case three_j() supplies the values.
-void stencil_fill(const Basis& bI, const Basis& bF, const double* threej, int tj_jmax,
-                  StencilTerm* st, int32_t* st_n);
+void stencil_fill(const Basis& bI, int jF, const double* threej, int tj_jmax, StencilTerm* st,
+                  int32_t* st_n);
 
 }  // namespace gi

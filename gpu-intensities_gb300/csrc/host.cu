@@ -131,6 +131,7 @@ static gi_status derive_basis(Ctx* c, Basis& b) {
     if (lam < 0 || lam >= b.mat_size) return fail(c, GI_ERR_ARG, "basis J=%d: lambda %d of root %d >= mat_size", b.J, lam, r);
     if (b.k[r] < 0 || b.k[r] > b.J) return fail(c, GI_ERR_ARG, "basis J=%d: k[%d]=%d outside 0..J", b.J, r, b.k[r]);
     if (b.iroot[r] < 0) return fail(c, GI_ERR_ARG, "basis J=%d: negative iroot_correlat_j0", b.J);
+    b.iroot_max = std::max(b.iroot_max, b.iroot[r]);
     b.root_key[r] = 2 * b.k[r] + (b.ktau[r] & 1);
     kmax = std::max(kmax, b.k[r]);
   }
@@ -233,11 +234,11 @@ gi_status ensure_ycsr(Ctx* c, Basis& b) {
 // (-1)^sigmaF (-1)^(sigmaI+kI) L f3j s and dipole component c.
 // Fixed-array core: st holds (2*jF+2)*6 terms, st_n (2*jF+2) counts.  With a
 // null table the 3j values come from three_j() itself (the same numbers the
-// table holds).
-void stencil_fill(const Basis& bI, const Basis& bF, const double* threej, int tj_jmax,
-                  StencilTerm* st, int32_t* st_n) {
+// table holds).  Only the final J enters from the final basis.
+void stencil_fill(const Basis& bI, int jF, const double* threej, int tj_jmax, StencilTerm* st,
+                  int32_t* st_n) {
   const int J1 = tj_jmax + 1;
-  const int jI = bI.J, jF = bF.J;
+  const int jI = bI.J;
   const double sq2 = 1.0 / std::sqrt(2.0);
   const int nkey = 2 * jF + 2;
   for (int i = 0; i < nkey * 6; i++) st[i] = StencilTerm{0, 0, 0.0};
@@ -280,7 +281,28 @@ static void build_stencil(const Basis& bI, const Basis& bF, const std::vector<do
   const int nkey = 2 * bF.J + 2;
   st.resize((size_t)nkey * 6);
   st_n.resize(nkey);
-  stencil_fill(bI, bF, threej.data(), tj_jmax, st.data(), st_n.data());
+  stencil_fill(bI, bF.J, threej.data(), tj_jmax, st.data(), st_n.data());
+}
+
+gi_status refresh_pair_tables(Ctx* c, Basis* only) {
+  for (auto& kv : c->bases) {
+    Basis& b = *kv.second;
+    if (only && &b != only) continue;
+    GI_CUDA(c, b.d_slot_of_key.upload(b.slot_of_key));
+    for (int d = 0; d < 3; d++) {
+      const int jF = b.J - 1 + d;
+      if (jF < 0) continue;
+      const int nkey = 2 * jF + 2;
+      std::vector<StencilTerm> st((size_t)nkey * 6);
+      std::vector<int32_t> stn(nkey);
+      const bool table = c->threej_jmax >= std::max(b.J, jF) && !c->threej.empty();
+      stencil_fill(b, jF, table ? c->threej.data() : nullptr, c->threej_jmax, st.data(),
+                   stn.data());
+      GI_CUDA(c, b.d_pair_st[d].upload(st));
+      GI_CUDA(c, b.d_pair_stn[d].upload(stn));
+    }
+  }
+  return GI_OK;
 }
 
 // ------------------------------------------------------------------ job plan
@@ -422,21 +444,29 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     BlockPlan& bp = kv.second;
     for (int r = 0; r < bp.blk->nvec; r++) {
       if (bp.level_of_rec[r] < 0) continue;
+      const int lvl = bp.level_of_rec[r];     // position in the energy-sorted level table
       if (c->job.on) bp.level_of_rec[r] = r;  // pair jobs report record indices
       const int32_t* q = bp.blk->quanta.data() + (size_t)r * nq;
       const double E = bp.blk->energies[r];
       bp.lower_ok[r] = F.lower(bp.blk->J, E, q);
       bp.upper_ok[r] = F.upper(bp.blk->J, E, q);
-      if (bp.lower_ok[r]) bp.ivec.push_back(r);
+      // a shard takes every nshards-th level as an initial level (cuda_host.cu:1174)
+      if (bp.lower_ok[r] && (c->nshards <= 1 || lvl % c->nshards == c->shard))
+        bp.ivec.push_back(r);
       if (bp.upper_ok[r]) bp.nupper++;
     }
   }
 
   // 3j table
   if (!c->threej_user || c->threej_jmax < jmax) {
+    const bool was_user = c->threej_user;
     precompute_threej(jmax, c->threej);
     c->threej_jmax = jmax;
     c->threej_user = false;
+    if (was_user && !c->parent) {  // the pair tables held the caller's values
+      gi_status s = refresh_pair_tables(c);
+      if (s != GI_OK) return s;
+    }
   }
 
   // block pairs and their stencils (intensity_filter block-level rules,
@@ -883,14 +913,23 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   // With the autotuner on, a new plan first runs eagerly (tuning needs timed,
   // synchronised launches); the next run of the same plan is captured.
   bool capture = use_graph;
-  if (use_graph && c->tune_mode > 0 && !(c->gexec && c->gsig == sig) && c->gpending != sig) {
+  auto cached = [&]() -> Ctx::GraphEntry* {
+    for (size_t k = 0; k < c->graphs.size(); k++)
+      if (c->graphs[k].sig == sig) {
+        std::rotate(c->graphs.begin(), c->graphs.begin() + k, c->graphs.begin() + k + 1);
+        return &c->graphs[0];
+      }
+    return nullptr;
+  };
+  Ctx::GraphEntry* hit = use_graph ? cached() : nullptr;
+  if (use_graph && c->tune_mode > 0 && !hit && c->gpending != sig) {
     capture = false;
     c->gpending = sig;
   }
-  if (use_graph && c->gexec && c->gsig == sig) {
+  if (hit) {
     // replay: the captured sequence with this run's table contents
-    GI_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
-    const gi_stats& g = c->gstats;  // what the captured sequence adds to a run's counts
+    GI_CUDA(c, cudaGraphLaunch(hit->exec, c->stream));
+    const gi_stats& g = hit->stats;
     for (int ph = 0; ph < GI_NPHASE; ph++) c->stats.launches_phase[ph] += g.launches_phase[ph];
     c->stats.kernel_launches += g.kernel_launches;
     c->stats.flops_tensor += g.flops_tensor;
@@ -900,9 +939,6 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     npairs_checked = g.npairs_checked;
     c->graph_replays++;
   } else if (capture) {
-    if (c->gexec) cudaGraphExecDestroy(c->gexec);
-    c->gexec = nullptr;
-    c->gsig = 0;
     const gi_stats pre = c->stats;
     GI_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
     capturing = true;
@@ -915,20 +951,27 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       return st;
     }
     GI_CUDA(c, ce);
-    const cudaError_t ie = cudaGraphInstantiate(&c->gexec, graph, 0);
+    Ctx::GraphEntry ent;
+    ent.sig = sig;
+    const cudaError_t ie = cudaGraphInstantiate(&ent.exec, graph, 0);
     cudaGraphDestroy(graph);
     GI_CUDA(c, ie);
-    GI_CUDA(c, cudaGraphLaunch(c->gexec, c->stream));
-    c->gsig = sig;
-    c->gstats = gi_stats{};
+    GI_CUDA(c, cudaGraphLaunch(ent.exec, c->stream));
     for (int ph = 0; ph < GI_NPHASE; ph++)
-      c->gstats.launches_phase[ph] = c->stats.launches_phase[ph] - pre.launches_phase[ph];
-    c->gstats.kernel_launches = c->stats.kernel_launches - pre.kernel_launches;
-    c->gstats.flops_tensor = c->stats.flops_tensor - pre.flops_tensor;
-    c->gstats.flops_halfls = fl_half;
-    c->gstats.flops_final = fl_final;
-    c->gstats.bytes_correlate = by_corr;
-    c->gstats.npairs_checked = npairs_checked;
+      ent.stats.launches_phase[ph] = c->stats.launches_phase[ph] - pre.launches_phase[ph];
+    ent.stats.kernel_launches = c->stats.kernel_launches - pre.kernel_launches;
+    ent.stats.flops_tensor = c->stats.flops_tensor - pre.flops_tensor;
+    ent.stats.flops_halfls = fl_half;
+    ent.stats.flops_final = fl_final;
+    ent.stats.bytes_correlate = by_corr;
+    ent.stats.npairs_checked = npairs_checked;
+    if (c->graphs.size() >= Ctx::kGraphCache) {
+      // the least recently used graph goes; its last launch is ordered before
+      // this one on the stream, so destroying it here is safe
+      cudaGraphExecDestroy(c->graphs.back().exec);
+      c->graphs.pop_back();
+    }
+    c->graphs.insert(c->graphs.begin(), ent);
   } else {
     gi_status st = issue();
     if (st != GI_OK) return st;
@@ -1064,8 +1107,9 @@ gi_status gi_destroy(gi_ctx* h) {
   cudaSetDevice(c->device);
   server_stop(c);
   trove_meta_release(c);
-  if (c->gexec) cudaGraphExecDestroy(c->gexec);
   cudaStreamSynchronize(c->stream);
+  for (auto& g : c->graphs) cudaGraphExecDestroy(g.exec);
+  c->graphs.clear();
   dipole_stream_release(c);
   ctx_release(c);
   return GI_OK;
@@ -1192,8 +1236,9 @@ gi_status gi_set_basis(gi_ctx* h, int J, int D, int ncase, int max_deg_size, int
   }
   gi_status s = derive_basis(c, *b);
   if (s != GI_OK) return s;
+  Basis* nb = b.get();
   c->bases[J] = std::move(b);
-  return GI_OK;
+  return refresh_pair_tables(c, nb);
 }
 
 gi_status gi_set_threej(gi_ctx* h, int jmax, const double* threej) {
@@ -1203,7 +1248,8 @@ gi_status gi_set_threej(gi_ctx* h, int jmax, const double* threej) {
   c->threej.assign(threej, threej + (size_t)(jmax + 1) * (jmax + 1) * 9);
   c->threej_jmax = jmax;
   c->threej_user = true;
-  return GI_OK;
+  cudaSetDevice(c->device);
+  return refresh_pair_tables(c);
 }
 
 static gi_status set_block(Ctx* c, int J, int gamma, int nsize, int nvec, const double* vecs,
@@ -1291,12 +1337,23 @@ gi_status gi_set_block_device(gi_ctx* h, int J, int gamma, int nsize, int nvec,
 }
 
 gi_status gi_run(gi_ctx* h, int flags, int64_t* nlines) {
+  return gi_run_shard(h, flags, 0, 1, nlines);
+}
+
+gi_status gi_run_shard(gi_ctx* h, int flags, int shard, int nshards, int64_t* nlines) {
   Ctx* c = reinterpret_cast<Ctx*>(h);
   if (!c || !nlines) return GI_ERR_ARG;
+  if (nshards < 1 || shard < 0 || shard >= nshards)
+    return fail(c, GI_ERR_ARG, "gi_run_shard: shard %d of %d", shard, nshards);
   if (c->server) return fail(c, GI_ERR_STATE, "gi_run while serving (gi_serve_stop first)");
   cudaSetDevice(c->device);
   c->err.clear();
-  return run_job(c, flags, nlines);
+  c->shard = shard;
+  c->nshards = nshards;
+  const gi_status st = run_job(c, flags, nlines);
+  c->shard = 0;
+  c->nshards = 1;
+  return st;
 }
 
 gi_status gi_get_lines(gi_ctx* h, int64_t offset, int64_t count, gi_line* out) {
@@ -1378,9 +1435,14 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
   if (s != GI_OK) return s;
   const int jmax = std::max(jI, jF);
   if (c->threej_jmax < jmax) {
+    const bool was_user = c->threej_user;
     precompute_threej(jmax, c->threej);
     c->threej_jmax = jmax;
     c->threej_user = false;
+    if (was_user) {
+      s = refresh_pair_tables(c);
+      if (s != GI_OK) return s;
+    }
   }
   std::vector<StencilTerm> st;
   std::vector<int32_t> stn;

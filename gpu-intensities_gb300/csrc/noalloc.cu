@@ -12,11 +12,14 @@
 // (kScratchBytes), which every GPU that loads the library holds until exit.
 //
 // Scratch use per call: Y (ndeg * nslot * Kp doubles, zeroed at the start of
-// every call because the scatter accumulates into it), Z (3x that, fully
-// written by the GEMM before it is read), the 3j/K-tau term table and the
-// key -> slot map (both copied in at the start of every call).  The array
-// keeps the last call's contents; calls whose work overlaps on the GPU share
-// the array and race, so a caller must order them (one stream, or events).
+// every call because the scatter accumulates into it) and Z (3x that, fully
+// written by the GEMM before it is read).  The 3j/K-tau term tables and the
+// key -> slot map are device tables of the initial basis, built when the basis
+// or the 3j table is set, so a call copies nothing from the host: it checks
+// its arguments against sizes the setters recorded and enqueues device work.
+// The array keeps the last call's contents; calls whose work overlaps on the
+// GPU share the array and race, so a caller must order them (one stream, or
+// events).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -29,11 +32,8 @@ namespace gi {
 namespace {
 
 constexpr int kMaxDevices = 64;
-constexpr size_t kMaxElems = size_t(1) << 19;      // ndeg * nslot * Kp of Y
-constexpr int kMaxKeys = 512;                      // 2*J+2 for J <= 255
-constexpr size_t kYZBytes = 4 * kMaxElems * sizeof(double);  // Y + 3 Z = 16 MiB
-constexpr size_t kStencilBytes = (size_t)kMaxKeys * 6 * sizeof(StencilTerm);
-constexpr size_t kScratchBytes = kYZBytes + kStencilBytes + 2 * kMaxKeys * sizeof(int32_t);
+constexpr size_t kMaxElems = size_t(1) << 19;                     // ndeg * nslot * Kp of Y
+constexpr size_t kScratchBytes = 4 * kMaxElems * sizeof(double);  // Y + 3 Z = 16 MiB
 static_assert(kScratchBytes == GI_NOALLOC_SCRATCH_BYTES, "scratch size stated in gi.h");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -106,19 +106,21 @@ extern "C" gi_status gi_half_ls_noalloc(gi_ctx* h, int jI, int gammaI, int ideg,
   const Basis& bF = *iF->second;
   const int ndeg = c->degen[gammaI];
   const size_t elems = (size_t)ndeg * bI.nslot * c->Kp;
-  if (elems > kMaxElems || 2 * jI + 2 > kMaxKeys || 2 * jF + 2 > kMaxKeys) {
+  if (elems > kMaxElems) {
     char buf[256];
     snprintf(buf, sizeof(buf),
-             "gi_half_ls_noalloc: size beyond the fixed scratch: degen*slots*Kp = %zu > %zu, or "
-             "J > %d (jI=%d, jF=%d); use gi_half_ls",
-             elems, kMaxElems, kMaxKeys / 2 - 1, jI, jF);
+             "gi_half_ls_noalloc: size beyond the fixed scratch: degen*slots*Kp = %zu > %zu "
+             "(jI=%d); use gi_half_ls",
+             elems, kMaxElems, jI);
     return say(GI_ERR_ARG, buf);
   }
   // every row index the kernels use must stay inside its Kp-wide row
-  for (int r = 0; r < bI.D; r++)
-    if (bI.iroot[r] >= c->N) return say(GI_ERR_ARG, "gi_half_ls_noalloc: iroot_correlat_j0 >= N");
-  for (int r = 0; r < bF.D; r++)
-    if (bF.iroot[r] >= c->N) return say(GI_ERR_ARG, "gi_half_ls_noalloc: iroot_correlat_j0 >= N");
+  if (bI.iroot_max >= c->N || bF.iroot_max >= c->N)
+    return say(GI_ERR_ARG, "gi_half_ls_noalloc: iroot_correlat_j0 >= N");
+  const DevArray<StencilTerm>& d_st = bI.d_pair_st[jF - jI + 1];
+  const DevArray<int32_t>& d_stn = bI.d_pair_stn[jF - jI + 1];
+  if (!d_st.p || !d_stn.p || !bI.d_slot_of_key.p)
+    return say(GI_ERR_STATE, "gi_half_ls_noalloc: the basis has no term tables");
   if (cudaSetDevice(c->device) != cudaSuccess)
     return say(GI_ERR_CUDA, "gi_half_ls_noalloc: cudaSetDevice failed");
   unsigned char* base = nullptr;
@@ -126,34 +128,16 @@ extern "C" gi_status gi_half_ls_noalloc(gi_ctx* h, int jI, int gammaI, int ideg,
     return say(GI_ERR_CUDA, "gi_half_ls_noalloc: cudaGetSymbolAddress of the scratch failed");
   double* Y = reinterpret_cast<double*>(base);
   double* Z = Y + elems;
-  StencilTerm* d_st = reinterpret_cast<StencilTerm*>(base + kYZBytes);
-  int32_t* d_stn = reinterpret_cast<int32_t*>(base + kYZBytes + kStencilBytes);
-  int32_t* d_slot = d_stn + kMaxKeys;
   cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : c->stream;
 
-  // host-side tables on the stack; a copy from pageable memory returns once
-  // the source has been staged, so they may go out of scope afterwards
-  StencilTerm st[kMaxKeys * 6];
-  int32_t stn[kMaxKeys];
-  int32_t slot_of_key[kMaxKeys];
-  const bool table = c->threej_jmax >= std::max(jI, jF) && !c->threej.empty();
-  stencil_fill(bI, bF, table ? c->threej.data() : nullptr, c->threej_jmax, st, stn);
-  const int nkeyI = 2 * jI + 2, nkeyF = 2 * jF + 2;
-  for (int k = 0; k < nkeyI; k++) slot_of_key[k] = bI.slot_of_key[k];
-
   cudaError_t e = cudaMemsetAsync(Y, 0, sizeof(double) * elems, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_st, st, sizeof(StencilTerm) * nkeyF * 6, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_stn, stn, sizeof(int32_t) * nkeyF, cudaMemcpyHostToDevice, s);
-  if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_slot, slot_of_key, sizeof(int32_t) * nkeyI, cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) {
     dim3 grid((bI.D + 255) / 256, ndeg);
     k_scatter_y<<<grid, 256, 0, s>>>(vsym_dev, bI.d_root_v.p, bI.d_root_key.p, bI.d_root_case.p,
                                      bI.d_root_lam.p, bI.d_case_iterm[gammaI].p,
                                      bI.d_case_nelem[gammaI].p, bI.d_rep[gammaI].p,
-                                     bI.Ntotal[gammaI], ndeg, d_slot, bI.D, bI.nslot, c->Kp, Y);
+                                     bI.Ntotal[gammaI], ndeg, bI.d_slot_of_key.p, bI.D, bI.nslot,
+                                     c->Kp, Y);
     e = cudaGetLastError();
   }
   const int ncol = ndeg * bI.nslot;
@@ -168,8 +152,8 @@ extern "C" gi_status gi_half_ls_noalloc(gi_ctx* h, int jI, int gammaI, int ideg,
     if (g != GI_OK && e == cudaSuccess) return g;  // a stream/event call failed (c->err set)
   }
   if (e == cudaSuccess)
-    e = launch_half_ls_prim(Z + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF, d_st, d_stn, 6,
-                            half_ls_dev, s);
+    e = launch_half_ls_prim(Z + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF, d_st.p, d_stn.p,
+                            6, half_ls_dev, s);
   if (e != cudaSuccess) {
     c->err = std::string("gi_half_ls_noalloc: ") + cudaGetErrorString(e);
     return GI_ERR_CUDA;

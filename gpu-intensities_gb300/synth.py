@@ -26,6 +26,7 @@ distribution as the first ``nvec`` columns of a full Haar QR).
 from __future__ import annotations
 
 import dataclasses
+from concurrent.futures import ThreadPoolExecutor
 from typing import Dict, List, Optional, Tuple
 
 import numpy as np
@@ -348,9 +349,23 @@ def make_block(rng: np.random.Generator, J: int, g: int, nsize: int, nmodes: int
         vecs = np.ascontiguousarray((q * np.sign(np.diag(r))[None, :]).T)
     elif nvec > 0:
         # large blocks: unit Gaussian vectors (nearly orthogonal at these sizes;
-        # a QR would take minutes and changes nothing the intensity path sees)
-        vecs = rng.standard_normal((nvec, nsize))
-        vecs /= np.linalg.norm(vecs, axis=1, keepdims=True)
+        # a QR would take minutes and changes nothing the intensity path sees),
+        # drawn in row bands by generators spawned from this block's seed, on
+        # threads (numpy releases the GIL while it fills an array)
+        vecs = np.empty((nvec, nsize))
+        seeds = np.random.SeedSequence(int(rng.integers(1 << 62))).spawn(8)
+        bands = np.array_split(np.arange(nvec), len(seeds))
+
+        def fill(k):
+            rows = bands[k]
+            if len(rows):
+                g = np.random.default_rng(seeds[k])
+                g.standard_normal(out=vecs[rows[0]:rows[-1] + 1])
+                vecs[rows[0]:rows[-1] + 1] /= np.linalg.norm(vecs[rows[0]:rows[-1] + 1], axis=1,
+                                                             keepdims=True)
+
+        with ThreadPoolExecutor(len(seeds)) as ex:
+            list(ex.map(fill, range(len(seeds))))
     else:
         vecs = np.zeros((0, nsize))
     quanta = np.zeros((nvec, nmodes + 1), np.int32)

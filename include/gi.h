@@ -232,6 +232,15 @@ gi_status gi_set_block_device(gi_ctx* ctx, int J, int gamma, int nsize, int nvec
 /* Computes every line of the job (all loaded J; |dJ| <= 1; the reference's
    filters).  *nlines receives the count. */
 gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);
+/* The part of the job whose initial levels sit at positions l of the
+   energy-sorted level table with l % nshards == shard: the reference's split
+   of the initial levels over devices (dipole_do_intensities_async_omp(job,
+   device_id, num_devices), cuda_host.cu:995, its loop at cuda_host.cu:1174).
+   The union of the shards 0..nshards-1 is the job's lines; ZPE, the level
+   table and the partition function are the whole job's.  A batch of work for
+   one GPU (one shard per step) or one of several GPUs (one shard per rank).
+   gi_run(ctx, flags, n) is gi_run_shard(ctx, flags, 0, 1, n). */
+gi_status gi_run_shard(gi_ctx* ctx, int flags, int shard, int nshards, int64_t* nlines);
 gi_status gi_get_lines(gi_ctx* ctx, int64_t offset, int64_t count, gi_line* out);
 /* Orders the last run's lines by (initial level, final level), the order of
    the reference's single-device loop (cuda_host.cu:1174-1473); the run
@@ -256,16 +265,18 @@ gi_status gi_half_ls(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF, const do
    nothing: vsym_dev (nsize doubles of block (jI, gammaI)) and half_ls_dev
    (D_F doubles) are device buffers the caller owns, and the scratch is one
    fixed device array of GI_NOALLOC_SCRATCH_BYTES inside the library, held by
-   every GPU that loads it until the process exits.  Limits: degen(gammaI) *
-   (number of (k, tau) slots of J=jI) * round_up(N, 64) <= 2^19 and
-   jI, jF <= 255; larger sizes return GI_ERR_ARG (use gi_half_ls).  The work is
-   enqueued on `stream` (a cudaStream_t; NULL = the context's stream) and the
-   call returns without waiting.  All calls share the scratch array, which
-   keeps the last call's contents: calls whose work overlaps on the GPU race,
-   so order them (one stream, or events).  The first call on a device looks up
-   the array's device address once (cudaGetSymbolAddress) with that device
-   current; make that first call before any stream capture. */
-#define GI_NOALLOC_SCRATCH_BYTES ((16u << 20) + (52u << 10))
+   every GPU that loads it until the process exits.  Limit: degen(gammaI) *
+   (number of (k, tau) slots of J=jI) * round_up(N, 64) <= 2^19; larger sizes
+   return GI_ERR_ARG (use gi_half_ls).  The rotational term tables it reads
+   are built by gi_set_basis / gi_set_threej, so the call copies nothing from
+   the host: the work is enqueued on `stream` (a cudaStream_t; NULL = the
+   context's stream) and the call returns without waiting.  All calls share
+   the scratch array, which keeps the last call's contents: calls whose work
+   overlaps on the GPU race, so order them (one stream, or events).  The first
+   call on a device looks up the array's device address once
+   (cudaGetSymbolAddress) with that device current; make that first call
+   before any stream capture. */
+#define GI_NOALLOC_SCRATCH_BYTES (16u << 20)
 gi_status gi_half_ls_noalloc(gi_ctx* ctx, int jI, int gammaI, int ideg, int jF,
                              const double* vsym_dev, double* half_ls_dev, void* stream);
 

@@ -280,6 +280,183 @@ static int filt_degeneracy(const or_job* job, int gI, int gF, int idegI, int ide
   return 1;
 }
 
+/* ---- Driver-loop arithmetic, two modes ---------------------------------- */
+/* precise = 1 (the checker): every reduction in double-double.  The
+   correlated vectors, the half line strength and the final dot carry a high
+   and a low part, products of (hi + lo) operands are formed with TwoProd and
+   accumulated with TwoSum (Dot2 with double-double inputs), so a transition
+   moment is accurate to ~1e-30 of the sum of its terms' magnitudes and the
+   relative error of a line measures the engine even where its moment is
+   cancelled far below the terms.  precise = 0 (the port timed as the CPU
+   baseline): the reference's own plain FP64 sums in its order. */
+
+typedef struct {
+  double s, c;
+} dd_acc;
+
+/* acc += (ah + al) * (bh + bl); al * bl is below 2^-106 of the term */
+static inline void dd_add(dd_acc* a, double ah, double al, double bh, double bl) {
+  double p = ah * bh;
+  double ep = fma(ah, bh, -p) + (ah * bl + al * bh);
+  double t = a->s + p;
+  double z = t - a->s;
+  double es = (a->s - (t - z)) + (p - z);
+  a->s = t;
+  a->c += es + ep;
+}
+static inline void dd_split(const dd_acc* a, double* hi, double* lo) {
+  double h = a->s + a->c;
+  *lo = a->c - (h - a->s);
+  *hi = h;
+}
+
+/* correlate (dipole_kernals.cu:38-71) into hi/lo (lo = 0 in plain mode) */
+static void corr_mode(const or_basis* b, const int32_t* ijterms, int nrep, const int32_t* degen,
+                      int ideg, int gamma, const double* vsym, int precise, double* hi,
+                      double* lo) {
+  const int D = b->Maxcontracts;
+  const int Ntot = b->Ntotal[gamma];
+  const int sdeg = degen[gamma];
+  const double* irr = b->repres[gamma];
+  for (int r = 0; r < D; r++) {
+    const int irow = b->icontr2icase[r];
+    const int ib = b->icontr2icase[r + D];
+    const int iterm = ijterms[irow + gamma * b->Maxsymcoeffs];
+    const int nelem = b->Nsym[gamma + irow * nrep];
+    const double* rr = irr + (size_t)ideg * Ntot + (size_t)ib * sdeg * Ntot;
+    if (precise) {
+      dd_acc acc = {0.0, 0.0};
+      for (int i = 0; i < nelem; i++) dd_add(&acc, vsym[iterm + i], 0.0, rr[iterm + i], 0.0);
+      dd_split(&acc, &hi[r], &lo[r]);
+    } else {
+      double acc = 0.0;
+      for (int i = 0; i < nelem; i++) acc += vsym[iterm + i] * rr[iterm + i];
+      hi[r] = acc;
+      lo[r] = 0.0;
+    }
+  }
+}
+
+/* Roots of a basis grouped by k, ascending root index within each k. */
+typedef struct {
+  int kmax;
+  int* ptr; /* [kmax+2] */
+  int* idx; /* [D] */
+} kgroups;
+
+static void kgroups_build(const or_basis* b, kgroups* g) {
+  const int D = b->Maxcontracts;
+  int kmax = 0;
+  for (int r = 0; r < D; r++)
+    if (b->k[r] > kmax) kmax = b->k[r];
+  g->kmax = kmax;
+  g->ptr = (int*)calloc((size_t)kmax + 2, sizeof(int));
+  g->idx = (int*)malloc(sizeof(int) * (size_t)(D > 0 ? D : 1));
+  for (int r = 0; r < D; r++) g->ptr[b->k[r] + 1]++;
+  for (int k = 0; k <= kmax; k++) g->ptr[k + 1] += g->ptr[k];
+  int* fill = (int*)malloc(sizeof(int) * ((size_t)kmax + 1));
+  for (int k = 0; k <= kmax; k++) fill[k] = g->ptr[k];
+  for (int r = 0; r < D; r++) g->idx[fill[b->k[r]]++] = r;
+  free(fill);
+}
+static void kgroups_free(kgroups* g) {
+  free(g->ptr);
+  free(g->idx);
+}
+
+/* Half line strength (dipole_kernals.cu:162-227) of one primitive initial
+   vector into hi/lo, one final root per iteration (parallel over rF).  The
+   reference's terms with |kI - kF| > 1 are exact zeros (multiplied by 0) and
+   are skipped: the initial roots of kF-1, kF, kF+1 are visited in ascending
+   root order, the reference's order, by a merge of the three k groups. */
+static void half_ls_mode(const or_basis* bI, const kgroups* gI, const or_basis* bF, int N,
+                         const double* mu, const double* threej, int jmax, const double* vh,
+                         const double* vl, int precise, int nthreads, double* hh, double* hl) {
+  const double sq2 = 1.0 / sqrt(2.0);
+  const size_t N2 = (size_t)N * N;
+  const int J1 = jmax + 1;
+  const int jI = bI->jval, jF = bF->jval;
+  const int DF = bF->Maxcontracts;
+#pragma omp parallel for schedule(dynamic, 64) num_threads(nthreads)
+  for (int rF = 0; rF < DF; rF++) {
+    const int icF = bF->iroot_correlat_j0[rF];
+    const int tauF = bF->ktau[rF] & 1;
+    const int kF = bF->k[rF];
+    const int sigF = (kF % 3) * tauF;
+    int pos[3], end[3], ng = 0;
+    for (int kI = kF - 1; kI <= kF + 1; kI++) {
+      if (kI < 0 || kI > gI->kmax) continue;
+      pos[ng] = gI->ptr[kI];
+      end[ng] = gI->ptr[kI + 1];
+      ng++;
+    }
+    dd_acc acc = {0.0, 0.0};
+    double plain = 0.0;
+    for (;;) {
+      int best = -1, rI = 0;
+      for (int q = 0; q < ng; q++)
+        if (pos[q] < end[q] && (best < 0 || gI->idx[pos[q]] < rI)) {
+          best = q;
+          rI = gI->idx[pos[q]];
+        }
+      if (best < 0) break;
+      pos[best]++;
+      const int kI = bI->k[rI];
+      const int icI = bI->iroot_correlat_j0[rI];
+      const int tauI = bI->ktau[rI] & 1;
+      const int sigI = (kI % 3) * tauI;
+      const double sgnI = ((sigI + kI) & 1) ? -1.0 : 1.0;
+      const double f3j =
+          threej[jI + kI * J1 + (jF - jI + 1) * J1 * J1 + (kF - kI + 1) * J1 * J1 * 3];
+      int c;
+      double L;
+      if (kF == kI) {
+        c = 2;
+        L = (double)(tauF - tauI);
+      } else if (tauF != tauI) {
+        c = 0;
+        L = (double)((tauF - tauI) * (kF - kI));
+      } else {
+        c = 1;
+        L = -1.0;
+      }
+      const double sc = (kI != kF && kI * kF != 0) ? sq2 : 1.0;
+      const double m = mu[(size_t)c * N2 + (size_t)icI + (size_t)icF * N];
+      const double coef = sgnI * L * f3j * sc;
+      if (precise) {
+        /* (coef * m) exactly as a pair, times vI = vh + vl */
+        const double p = coef * m;
+        const double pe = fma(coef, m, -p);
+        dd_add(&acc, p, pe, vh[rI], vl[rI]);
+      } else {
+        plain += coef * m * vh[rI];
+      }
+    }
+    const double sgnF = (sigF & 1) ? -1.0 : 1.0;
+    if (precise) {
+      double h, l;
+      dd_split(&acc, &h, &l);
+      hh[rF] = sgnF * h;
+      hl[rF] = sgnF * l;
+    } else {
+      hh[rF] = sgnF * plain;
+      hl[rF] = 0.0;
+    }
+  }
+}
+
+static double dot_mode(const double* xh, const double* xl, const double* yh, const double* yl,
+                       int n, int precise) {
+  if (precise) {
+    dd_acc acc = {0.0, 0.0};
+    for (int i = 0; i < n; i++) dd_add(&acc, xh[i], xl[i], yh[i], yl[i]);
+    return acc.s + acc.c;
+  }
+  double acc = 0.0;
+  for (int i = 0; i < n; i++) acc += xh[i] * yh[i];
+  return acc;
+}
+
 /* ---- The driver loop (cuda_host.cu:1170-1477) --------------------------- */
 
 int or_run(const or_job* job, or_line** out, size_t* nout) {
@@ -287,6 +464,12 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
   *nout = 0;
   if (job->nrep > 16) return -1;
   const int nrep = job->nrep;
+  const int precise = job->precise;
+#ifdef _OPENMP
+  const int nth = job->nthreads > 0 ? job->nthreads : omp_get_max_threads();
+#else
+  const int nth = 1;
+#endif
   or_ctx x;
   x.job = job;
   x.zpe = or_resolve_zpe(job);
@@ -325,33 +508,50 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
     }
   qsort(lv, (size_t)nl, sizeof(or_level), cmp_level);
 
-  /* symmetric-index offsets per basis */
+  /* symmetric-index offsets and k groups per basis */
   int32_t* ijt[2];
+  kgroups kg[2];
   for (int i = 0; i < 2; i++) {
     ijt[i] = (int32_t*)malloc(sizeof(int32_t) * (size_t)job->basis[i].Maxsymcoeffs * nrep);
     or_compute_ijterms(&job->basis[i], nrep, ijt[i]);
+    kgroups_build(&job->basis[i], &kg[i]);
   }
   int jmax = job->jvals[0] > job->jvals[1] ? job->jvals[0] : job->jvals[1];
   double* threej = (double*)malloc(sizeof(double) * (size_t)(jmax + 1) * (jmax + 1) * 9);
   or_precompute_threej(jmax, threej);
 
-  int dimenmax = job->basis[0].Maxcontracts > job->basis[1].Maxcontracts
-                     ? job->basis[0].Maxcontracts
-                     : job->basis[1].Maxcontracts;
+  const int dimenmax = job->basis[0].Maxcontracts > job->basis[1].Maxcontracts
+                           ? job->basis[0].Maxcontracts
+                           : job->basis[1].Maxcontracts;
   int maxdeg = 1;
   for (int g = 0; g < nrep; g++)
     if (job->degen[g] > maxdeg) maxdeg = job->degen[g];
 
-  /* correlated final vectors, one per (level, ideg), computed once */
-  double* corr = (double*)malloc(sizeof(double) * (size_t)nl * maxdeg * dimenmax + 8);
-#pragma omp parallel for schedule(dynamic, 4) num_threads(job->nthreads > 0 ? job->nthreads : omp_get_max_threads())
-  for (int l = 0; l < nl; l++) {
-    const or_level* F = &lv[l];
-    const or_block* b = &job->blocks[F->jind + 2 * F->gamma];
-    for (int d = 0; d < F->ndeg; d++)
-      or_correlate(&job->basis[F->jind], ijt[F->jind], nrep, job->degen, d, F->gamma,
-                   b->vecs + (size_t)F->rec * b->nsize,
-                   corr + ((size_t)l * maxdeg + d) * dimenmax);
+  /* initial levels that pass the lower filter */
+  int* inits = (int*)malloc(sizeof(int) * (size_t)(nl ? nl : 1));
+  int ninit = 0;
+  for (int li = 0; li < nl; li++)
+    if (filt_lower(&x, lv[li].jval, lv[li].energy, lv[li].quanta)) inits[ninit++] = li;
+
+  /* correlated final vectors: cached for every level when they fit in 2 GiB
+     and more than one initial level uses them, else formed per use */
+  const size_t corr_elems = (size_t)nl * maxdeg * dimenmax;
+  const int cache_corr = ninit > 1 && corr_elems * 2 * sizeof(double) <= ((size_t)2 << 30);
+  double* corr_h = NULL;
+  double* corr_l = NULL;
+  if (cache_corr) {
+    corr_h = (double*)malloc(sizeof(double) * corr_elems + 8);
+    corr_l = (double*)malloc(sizeof(double) * corr_elems + 8);
+#pragma omp parallel for schedule(dynamic, 4) num_threads(nth)
+    for (int l = 0; l < nl; l++) {
+      const or_level* F = &lv[l];
+      const or_block* b = &job->blocks[F->jind + 2 * F->gamma];
+      for (int d = 0; d < F->ndeg; d++) {
+        const size_t o = ((size_t)l * maxdeg + d) * dimenmax;
+        corr_mode(&job->basis[F->jind], ijt[F->jind], nrep, job->degen, d, F->gamma,
+                  b->vecs + (size_t)F->rec * b->nsize, precise, corr_h + o, corr_l + o);
+      }
+    }
   }
 
   /* constants (cuda_host.cu:12-18, 1170) */
@@ -363,49 +563,70 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
       8.0 * pow(10.0, -36.0) * pow(pi, 3.0) * avogno / (3.0 * planck * vellgt);
   const double beta = planck * vellgt / (boltz * job->temperature);
 
-  or_line** per = (or_line**)calloc((size_t)(nl ? nl : 1), sizeof(or_line*));
-  size_t* pern = (size_t*)calloc((size_t)(nl ? nl : 1), sizeof(size_t));
+  /* one line slot per final level of the current initial level */
+  or_line* row = (or_line*)malloc(sizeof(or_line) * (size_t)(nl ? nl : 1));
+  char* keep = (char*)malloc((size_t)(nl ? nl : 1));
+  size_t total = 0, acap = 1024;
+  or_line* all = (or_line*)malloc(sizeof(or_line) * acap);
+  double* vh = (double*)malloc(sizeof(double) * dimenmax);
+  double* vl = (double*)malloc(sizeof(double) * dimenmax);
+  double* hh = (double*)malloc(sizeof(double) * 2 * maxdeg * dimenmax);
+  double* hl = (double*)malloc(sizeof(double) * 2 * maxdeg * dimenmax);
   int err = 0;
 
-#pragma omp parallel num_threads(job->nthreads > 0 ? job->nthreads : omp_get_max_threads())
-  {
-    double* vprim = (double*)malloc(sizeof(double) * dimenmax);
-    double* hls = (double*)malloc(sizeof(double) * 2 * maxdeg * dimenmax);
-    int have[2][2];
-#pragma omp for schedule(dynamic, 1)
-    for (int li = 0; li < nl; li++) {
-      const or_level* I = &lv[li];
-      if (!filt_lower(&x, I->jval, I->energy, I->quanta)) continue;
-      const or_block* bI = &job->blocks[I->jind + 2 * I->gamma];
-      const double* vecI = bI->vecs + (size_t)I->rec * bI->nsize;
-      int gFt = x.igamma_pair[I->gamma];
-      memset(have, 0, sizeof(have));
-      for (int indF = 0; indF < 2; indF++) {
-        int jF = job->jvals[indF];
-        /* indF_filter (trove_functions.cpp:1476-1493) */
-        int any = 0;
-        for (int lf = 0; lf < nl && !any; lf++)
-          if (lv[lf].jval == jF && filt_intensity(&x, I, &lv[lf])) any = 1;
-        if (!any) continue;
-        for (int d = 0; d < I->ndeg; d++) {
-          if (!filt_degeneracy(job, I->gamma, gFt, d, 0)) continue;
-          or_correlate(&job->basis[I->jind], ijt[I->jind], nrep, job->degen, d, I->gamma, vecI,
-                       vprim);
-          or_half_ls(&job->basis[I->jind], &job->basis[indF], job->N, job->mu, threej, jmax,
-                     vprim, hls + ((size_t)indF + 2 * d) * dimenmax);
-          have[indF][d] = 1;
-        }
+  for (int ii = 0; ii < ninit; ii++) {
+    const or_level* I = &lv[inits[ii]];
+    const or_block* bI = &job->blocks[I->jind + 2 * I->gamma];
+    const double* vecI = bI->vecs + (size_t)I->rec * bI->nsize;
+    const int gFt = x.igamma_pair[I->gamma];
+    int have[2][2] = {{0, 0}, {0, 0}};
+    for (int indF = 0; indF < 2; indF++) {
+      const int jF = job->jvals[indF];
+      /* indF_filter (trove_functions.cpp:1476-1493) */
+      int any = 0;
+      for (int lf = 0; lf < nl && !any; lf++)
+        if (lv[lf].jval == jF && filt_intensity(&x, I, &lv[lf])) any = 1;
+      if (!any) continue;
+      for (int d = 0; d < I->ndeg; d++) {
+        if (!filt_degeneracy(job, I->gamma, gFt, d, 0)) continue;
+        corr_mode(&job->basis[I->jind], ijt[I->jind], nrep, job->degen, d, I->gamma, vecI,
+                  precise, vh, vl);
+        const size_t o = ((size_t)indF + 2 * d) * dimenmax;
+        half_ls_mode(&job->basis[I->jind], &kg[I->jind], &job->basis[indF], job->N, job->mu,
+                     threej, jmax, vh, vl, precise, nth, hh + o, hl + o);
+        have[indF][d] = 1;
       }
-      size_t n = 0, ncap = 64;
-      or_line* buf = (or_line*)malloc(sizeof(or_line) * ncap);
+    }
+#pragma omp parallel num_threads(nth)
+    {
+      double* fh = NULL;
+      double* fl = NULL;
+      if (!cache_corr) {
+        fh = (double*)malloc(sizeof(double) * dimenmax);
+        fl = (double*)malloc(sizeof(double) * dimenmax);
+      }
+#pragma omp for schedule(dynamic, 16)
       for (int lf = 0; lf < nl; lf++) {
+        keep[lf] = 0;
         const or_level* F = &lv[lf];
         if (!filt_upper(&x, F->jval, F->energy, F->quanta)) continue;
         if (!filt_intensity(&x, I, F)) continue;
         double t[4] = {0.0, 0.0, 0.0, 0.0};
-        int dimenF = job->basis[F->jind].Maxcontracts;
+        const int dimenF = job->basis[F->jind].Maxcontracts;
+        const or_block* bF = &job->blocks[F->jind + 2 * F->gamma];
         for (int dF = 0; dF < F->ndeg; dF++) {
           if (job->reduced && dF != 0) continue;
+          const double* ch;
+          const double* cl;
+          if (cache_corr) {
+            ch = corr_h + ((size_t)lf * maxdeg + dF) * dimenmax;
+            cl = corr_l + ((size_t)lf * maxdeg + dF) * dimenmax;
+          } else {
+            corr_mode(&job->basis[F->jind], ijt[F->jind], nrep, job->degen, dF, F->gamma,
+                      bF->vecs + (size_t)F->rec * bF->nsize, precise, fh, fl);
+            ch = fh;
+            cl = fl;
+          }
           for (int dI = 0; dI < I->ndeg; dI++) {
             if (!filt_degeneracy(job, I->gamma, F->gamma, dI, dF)) continue;
             if (!have[F->jind][dI]) {
@@ -413,8 +634,8 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
               err = -4;
               continue;
             }
-            t[dI + 2 * dF] = or_dot(corr + ((size_t)lf * maxdeg + dF) * dimenmax,
-                                    hls + ((size_t)F->jind + 2 * dI) * dimenmax, dimenF);
+            const size_t o = ((size_t)F->jind + 2 * dI) * dimenmax;
+            t[dI + 2 * dF] = dot_mode(ch, cl, hh + o, hl + o, dimenF, precise);
           }
         }
         /* epilogue (cuda_host.cu:1388-1407) */
@@ -423,20 +644,16 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
           for (int dI = 0; dI < I->ndeg; dI++) ls += t[dI + 2 * dF] * t[dI + 2 * dF];
         ls /= (double)I->ndeg;
         if (job->reduced && F->ndeg != 1 && I->ndeg != 1) ls *= (double)I->ndeg;
-        double nu = F->energy - I->energy;
-        double anu = fabs(nu);
-        double boltz_fc =
+        const double nu = F->energy - I->energy;
+        const double anu = fabs(nu);
+        const double boltz_fc =
             anu * exp(-(I->energy - x.zpe) * beta) * (1.0 - exp(-anu * beta)) / job->q_stat;
-        double A = A_coef_s_1 * (double)(2 * I->jval + 1) * ls * pow(anu, 3);
-        double S = ls * job->gns[I->gamma] * (double)((2 * I->jval + 1) * (2 * F->jval + 1));
-        double In = S * intens_cm_mol * boltz_fc;
+        const double A = A_coef_s_1 * (double)(2 * I->jval + 1) * ls * pow(anu, 3);
+        const double S = ls * job->gns[I->gamma] * (double)((2 * I->jval + 1) * (2 * F->jval + 1));
+        const double In = S * intens_cm_mol * boltz_fc;
         if (!(S >= job->thresh_linestrength)) continue;
         if (!(In / avogno >= job->thresh_intensity)) continue;
-        if (n == ncap) {
-          ncap *= 2;
-          buf = (or_line*)realloc(buf, sizeof(or_line) * ncap);
-        }
-        or_line* o = &buf[n++];
+        or_line* o = &row[lf];
         o->jI = I->jval;
         o->gammaI = I->gamma;
         o->recI = I->rec;
@@ -452,29 +669,35 @@ int or_run(const or_job* job, or_line** out, size_t* nout) {
         memcpy(o->t, t, sizeof(t));
         o->Elow = I->energy - x.zpe;
         o->Eup = F->energy - x.zpe;
+        keep[lf] = 1;
       }
-      per[li] = buf;
-      pern[li] = n;
+      free(fh);
+      free(fl);
     }
-    free(vprim);
-    free(hls);
+    for (int lf = 0; lf < nl; lf++) {
+      if (!keep[lf]) continue;
+      if (total == acap) {
+        acap *= 2;
+        all = (or_line*)realloc(all, sizeof(or_line) * acap);
+      }
+      all[total++] = row[lf];
+    }
   }
 
-  size_t total = 0;
-  for (int l = 0; l < nl; l++) total += pern[l];
-  or_line* all = (or_line*)malloc(sizeof(or_line) * (total ? total : 1));
-  size_t o = 0;
-  for (int l = 0; l < nl; l++) {
-    if (pern[l]) memcpy(all + o, per[l], sizeof(or_line) * pern[l]);
-    o += pern[l];
-    free(per[l]);
-  }
-  free(per);
-  free(pern);
-  free(corr);
+  free(row);
+  free(keep);
+  free(vh);
+  free(vl);
+  free(hh);
+  free(hl);
+  free(inits);
+  free(corr_h);
+  free(corr_l);
   free(threej);
-  free(ijt[0]);
-  free(ijt[1]);
+  for (int i = 0; i < 2; i++) {
+    free(ijt[i]);
+    kgroups_free(&kg[i]);
+  }
   free(lv);
   if (err) {
     free(all);

@@ -10,10 +10,14 @@
  * (oracle/build_ref.sh -> oracle/_ref/); the rest follows the reference's
  * kernels and driver loop line by line (citations on each function).
  *
- * Accuracy: every reduction (symmetrised->primitive transform, half line
- * strength, final dot) uses Ogita-Rump-Oishi Dot2 (TwoProd via fma +
- * TwoSum), i.e. it is as accurate as a computation in twice the working
- * precision, so tolerances measure the engine and not the oracle.
+ * Accuracy: or_correlate / or_half_ls / or_dot (the kernel-level functions
+ * pinned against the reference's kernels) use Ogita-Rump-Oishi Dot2 (TwoProd
+ * via fma + TwoSum).  or_run with precise = 1 (the checker) carries the
+ * correlated vectors and the half line strength as double-double values into
+ * a double-double final dot, so a transition moment is accurate far below
+ * FP64 rounding of its terms and tolerances measure the engine, also on lines
+ * whose moment cancels.  With precise = 0 it is the reference's plain FP64
+ * arithmetic (the CPU baseline port).
  */
 #ifndef GI_ORACLE_H
 #define GI_ORACLE_H
@@ -72,6 +76,8 @@ typedef struct {
   or_basis basis[2];       /* for jvals[0], jvals[1] */
   const or_block* blocks;  /* [2*nrep]: index jind + 2*gamma */
   int nthreads;            /* OpenMP threads (<=0: library default) */
+  int precise;             /* 1: double-double reductions (the checker);
+                              0: the reference's plain FP64 sums (the timed port) */
 } or_job;
 
 typedef struct {

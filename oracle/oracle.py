@@ -42,7 +42,7 @@ class or_job(C.Structure):
                 ("quanta_lower", i32p), ("quanta_upper", i32p),
                 ("thresh_linestrength", C.c_double), ("thresh_intensity", C.c_double),
                 ("N", C.c_int), ("mu", f64p), ("basis", or_basis * 2),
-                ("blocks", C.POINTER(or_block)), ("nthreads", C.c_int)]
+                ("blocks", C.POINTER(or_block)), ("nthreads", C.c_int), ("precise", C.c_int)]
 
 
 LINE_DTYPE = np.dtype([("jI", np.int32), ("gammaI", np.int32), ("recI", np.int32),
@@ -219,7 +219,7 @@ def make_basis(b, keep: Keep) -> or_basis:
 
 
 def make_job(prob, jvals: Tuple[int, int], keep: Keep, zpe: Optional[float] = None,
-             nthreads: int = 0) -> or_job:
+             nthreads: int = 0, precise: bool = True) -> or_job:
     """An or_job for one reference run over jvals = (jvals[0], jvals[1])."""
     p = prob.params
     j = or_job()
@@ -263,15 +263,18 @@ def make_job(prob, jvals: Tuple[int, int], keep: Keep, zpe: Optional[float] = No
     keep(blocks)
     j.blocks = C.cast(blocks, C.POINTER(or_block))
     j.nthreads = nthreads
+    j.precise = int(precise)
     return j
 
 
 def run_pair(prob, jvals: Tuple[int, int], zpe: Optional[float] = None,
-             nthreads: int = 0) -> np.ndarray:
-    """Lines of one reference run over (jvals[0], jvals[1])."""
+             nthreads: int = 0, precise: bool = True) -> np.ndarray:
+    """Lines of one reference run over (jvals[0], jvals[1]); precise=False runs
+    the reference's plain FP64 arithmetic (the timed CPU port) instead of the
+    double-double checker."""
     L = lib()
     keep = Keep()
-    job = make_job(prob, jvals, keep, zpe, nthreads)
+    job = make_job(prob, jvals, keep, zpe, nthreads, precise)
     out = C.POINTER(or_line)()
     n = C.c_size_t(0)
     rc = L.or_run(C.byref(job), C.byref(out), C.byref(n))
@@ -292,13 +295,14 @@ def resolve_zpe(prob) -> float:
     return float(lib().or_resolve_zpe(C.byref(job)))
 
 
-def run_all(prob, nthreads: int = 0) -> np.ndarray:
+def run_all(prob, nthreads: int = 0, precise: bool = True) -> np.ndarray:
     """All lines of a multi-J job as the union of consecutive reference runs
     (J, J+1) for J = Jmin .. Jmax-1, with the ZPE resolved once and passed
     explicitly to every run, exactly as a user chains the reference."""
     js = prob.jlist
     zpe = resolve_zpe(prob)
-    parts = [run_pair(prob, (js[i], js[i + 1]), zpe, nthreads) for i in range(len(js) - 1)]
+    parts = [run_pair(prob, (js[i], js[i + 1]), zpe, nthreads, precise)
+             for i in range(len(js) - 1)]
     return np.concatenate(parts) if parts else np.empty(0, LINE_DTYPE)
 
 
