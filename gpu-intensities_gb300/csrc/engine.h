@@ -243,6 +243,8 @@ struct Ctx {
   int shard = 0, nshards = 1;
 
   // workspaces
+  DevArray<double> hls_v, hls_y, hls_z, hls_h;  // gi_half_ls (grow-only)
+  DevArray<int32_t> hls_iv;
   DevArray<double> w_y, w_z, w_h, w_t, w_EI;
   DevArray<unsigned long long> w_counter;
   DevArray<int32_t> w_ivec, w_int;
@@ -327,6 +329,12 @@ cudaError_t launch_build_h(const double* Z, size_t zstride_c, int ldz, int nslot
 cudaError_t launch_half_ls_prim(const double* Z, size_t zstride_c, int ldz, const Basis& bF,
                                 const StencilTerm* st, const int32_t* st_n, int st_max,
                                 double* h, cudaStream_t s);
+// h from a Z held as K-split partial products Zp[p][col][c * cstride + v]
+// (Zp already offset to the first column of the wanted degenerate component).
+cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstride, int ldz,
+                                      int cstride, const Basis& bF, const StencilTerm* st,
+                                      const int32_t* st_n, int st_max, double* h,
+                                      cudaStream_t s);
 cudaError_t launch_epilogue(const double* T, int ldt, int nI, int nF, const int32_t* levelI,
                             const double* EI, const int32_t* levelF, const double* EF,
                             const uint8_t* upper_ok, const EpiParams& p, gi_line* out,

@@ -1444,33 +1444,55 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
       if (s != GI_OK) return s;
     }
   }
-  std::vector<StencilTerm> st;
-  std::vector<int32_t> stn;
-  build_stencil(bI, bF, c->threej, c->threej_jmax, st, stn);
+  // the rotational term tables towards jF are the basis's device tables
+  const StencilTerm* dst = bI.d_pair_st[jF - jI + 1].p;
+  const int32_t* dstn = bI.d_pair_stn[jF - jI + 1].p;
+  if (!dst || !dstn) return fail(c, GI_ERR_STATE, "basis J=%d has no term tables", jI);
   const int nsize = bI.Ntotal[gammaI], ld = round_up(nsize, 64), ndeg = c->degen[gammaI];
-  DevArray<double> v, y, z, hh;
-  DevArray<int32_t> iv;
-  DevArray<StencilTerm> dst;
-  DevArray<int32_t> dstn;
-  int32_t zero = 0;
-  GI_CUDA(c, v.alloc(ld));
-  GI_CUDA(c, cudaMemset(v.p, 0, sizeof(double) * ld));
-  GI_CUDA(c, cudaMemcpy(v.p, vsym, sizeof(double) * nsize, cudaMemcpyHostToDevice));
-  GI_CUDA(c, iv.upload(&zero, 1));
-  GI_CUDA(c, dst.upload(st));
-  GI_CUDA(c, dstn.upload(stn));
   const int ncol = ndeg * bI.nslot;
-  GI_CUDA(c, y.alloc((size_t)ncol * c->Kp));
-  GI_CUDA(c, z.alloc((size_t)3 * ncol * c->Kp));
-  GI_CUDA(c, hh.alloc(bF.D));
-  GI_CUDA(c, launch_build_y(v.p, ld, iv.p, 1, ndeg, bI, gammaI, ndeg, c->N, c->Kp, y.p, c->stream));
-  const size_t zc = (size_t)ncol * c->Kp;
-  s = dipole_gemm_fp64(c, y.p, c->Kp, z.p, c->Kp, zc, ncol, c->stream);
-  if (s != GI_OK) return s;
-  GI_CUDA(c, launch_half_ls_prim(z.p + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF, dst.p,
-                                 dstn.p, 6, hh.p, c->stream));
+  // grow-only workspaces of the context: repeated calls allocate nothing
+  GI_CUDA(c, c->hls_v.reserve(ld));
+  GI_CUDA(c, c->hls_iv.reserve(1));
+  GI_CUDA(c, c->hls_y.reserve((size_t)ncol * c->Kp));
+  GI_CUDA(c, c->hls_h.reserve(bF.D));
+  GI_CUDA(c, cudaMemsetAsync(c->hls_v.p, 0, sizeof(double) * ld, c->stream));
+  GI_CUDA(c, cudaMemsetAsync(c->hls_iv.p, 0, sizeof(int32_t), c->stream));
+  GI_CUDA(c, cudaMemcpyAsync(c->hls_v.p, vsym, sizeof(double) * nsize, cudaMemcpyHostToDevice,
+                             c->stream));
+  double* y = c->hls_y.p;
+  double* hh = c->hls_h.p;
+  GI_CUDA(c, launch_build_y(c->hls_v.p, ld, c->hls_iv.p, 1, ndeg, bI, gammaI, ndeg, c->N, c->Kp,
+                            y, c->stream));
+  if (c->have_params && c->params.precision == GI_PREC_SPLIT && !c->streamed()) {
+    // split precision: the narrow digit GEMM, one pass over the dipole digits
+    // with K split over the SMs, its partial products summed by the stencil
+    s = split_prepare(c);
+    if (s != GI_OK) return s;
+    const int max_parts = 8;
+    const size_t ldz_max = (size_t)3 * round_up(c->N, 128);
+    GI_CUDA(c, c->hls_z.reserve((size_t)max_parts * ncol * ldz_max));
+    int nparts = 1, ldz = 0;
+    s = split_gemm_dipole_narrow(c, y, c->Kp, ncol, c->hls_z.p, (size_t)ncol * ldz_max,
+                                 max_parts, &nparts, &ldz);
+    if (s != GI_OK) return s;
+    GI_CUDA(c, launch_half_ls_prim_parts(c->hls_z.p + (size_t)ideg * bI.nslot * ldz, nparts,
+                                         (size_t)ncol * ldz_max, ldz, ldz / 3, bF, dst, dstn, 6,
+                                         hh, c->stream));
+  } else {
+    GI_CUDA(c, c->hls_z.reserve((size_t)3 * ncol * c->Kp));
+    const size_t zc = (size_t)ncol * c->Kp;
+    s = dipole_gemm_fp64(c, y, c->Kp, c->hls_z.p, c->Kp, zc, ncol, c->stream);
+    if (s != GI_OK) return s;
+    GI_CUDA(c, launch_half_ls_prim(c->hls_z.p + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF,
+                                   dst, dstn, 6, hh, c->stream));
+  }
+  GI_CUDA(c, cudaMemcpyAsync(half_ls, hh, sizeof(double) * bF.D, cudaMemcpyDeviceToHost,
+                             c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));
-  GI_CUDA(c, cudaMemcpy(half_ls, hh.p, sizeof(double) * bF.D, cudaMemcpyDeviceToHost));
+  if (c->have_params && c->params.precision == GI_PREC_SPLIT) {
+    s = split_check(c);
+    if (s != GI_OK) return s;
+  }
   return GI_OK;
 }
 

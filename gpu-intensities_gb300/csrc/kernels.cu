@@ -147,6 +147,38 @@ cudaError_t launch_half_ls_prim(const double* Z, size_t zstride_c, int ldz, cons
   return cudaGetLastError();
 }
 
+// The same from a Z split into K parts (the narrow split-precision GEMM):
+// Z_c[col][v] = sum_p Zp[p][col][c * cstride + v], col = colbase + slot.
+__global__ void k_half_ls_prim_parts(const double* __restrict__ Zp, int nparts, size_t pstride,
+                                     int ldz, int cstride, const int32_t* __restrict__ root_v,
+                                     const int32_t* __restrict__ root_key,
+                                     const StencilTerm* __restrict__ st,
+                                     const int32_t* __restrict__ st_n, int st_max, int D,
+                                     double* __restrict__ h) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= D) return;
+  const int v = root_v[r], key = root_key[r];
+  double acc = 0.0;
+  for (int t = 0; t < st_n[key]; ++t) {
+    const StencilTerm term = st[key * st_max + t];
+    const double* z = Zp + (size_t)term.slotI * ldz + (size_t)term.c * cstride + v;
+    double zs = z[0];
+    for (int p = 1; p < nparts; ++p) zs += z[(size_t)p * pstride];
+    acc = fma(term.coef, zs, acc);
+  }
+  h[r] = acc;
+}
+
+cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstride, int ldz,
+                                      int cstride, const Basis& bF, const StencilTerm* st,
+                                      const int32_t* st_n, int st_max, double* h,
+                                      cudaStream_t s) {
+  k_half_ls_prim_parts<<<(bF.D + 255) / 256, 256, 0, s>>>(Zp, nparts, pstride, ldz, cstride,
+                                                          bF.d_root_v.p, bF.d_root_key.p, st,
+                                                          st_n, st_max, bF.D, h);
+  return cudaGetLastError();
+}
+
 // ------------------------------------------------------------------ epilogue
 // Degeneracy sum, S, A_if, I(T), frequency window and thresholds
 // (cuda_host.cu:1376-1408), then a warp-aggregated append of kept lines.

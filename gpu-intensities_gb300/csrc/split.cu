@@ -2107,6 +2107,101 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
   return g;
 }
 
+// The half line strength of a few vectors: Z = mu^T Y for ncol columns, far
+// fewer than one 96-wide tile.  The dipole digits are the data that moves
+// (3 x Mpad x Kp x s bf16), so the GEMM is as fast as one pass over them:
+// the row tiles alone are too few CTAs to draw full HBM bandwidth, so K is
+// split into parts, each a problem of one persistent launch (one CTA per SM)
+// writing its own partial product Zp[part][col][3 * Mpad]; the caller sums the
+// parts.  Streamed dipoles and digit shapes other than the default grouped
+// s = 9 go through the regular GEMM as one part.
+gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, double* Zp,
+                                   size_t part_stride, int max_parts, int* nparts, int* ldz) {
+  SplitState* S = state(c);
+  const SplitState* D = c->parent ? c->parent->split : S;
+  const int K = c->Kp;
+  const int rows = 3 * S->Mpad;
+  *ldz = rows;
+  if (S->panel) {
+    c->err = "split precision: the narrow dipole GEMM needs a resident dipole";
+    return GI_ERR_STATE;
+  }
+  gi_status g = check(c, S->b_slices.reserve((size_t)S->s * ncol * K), "Y slices");
+  if (g != GI_OK) return g;
+  g = check(c, S->b_exp.reserve(ncol), "Y exponents");
+  if (g != GI_OK) return g;
+  g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+              return slice(Y, ldy, ncol, K, ncol, S->s, S->w, S->grouped, S->b_slices.p,
+                           S->b_exp.p, c->stream);
+            }),
+            "slice Y");
+  if (g != GI_OK) return g;
+  c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * c->N * 3;
+  constexpr int SS = 9, BN = bn2_of(SS), D1 = d1_of(SS);
+  const int nM = rows / kBM, nN = (ncol + BN - 1) / BN;
+  // parts: enough to give every SM a tile; each a multiple of 64 in K (whole
+  // pairs of the two-slice ring stages) and at most one exact segment long
+  const int kq = K / 64, pmax = std::min(max_parts, kGpMaxProb);
+  int parts = std::max(1, std::min({std::max(c->nsm, 1) / (nM * nN), pmax, kq}));
+  while (parts < pmax && (kq + parts - 1) / parts * 64 > kKSeg) parts++;
+  const int per = (kq + parts - 1) / parts * 64;
+  parts = (K + per - 1) / per;  // no empty part
+  if (S->s != SS || !S->grouped || getenv("GI_SPLIT_FORCE") || per > kKSeg) {
+    *nparts = 1;
+    gi_status r = GI_OK;
+    timed(c, GI_PHASE_HALFLS_GEMM, [&] {
+      r = gemm(c, D->mu_slices.p, rows, D->mu_exp.p, rows, S->b_slices.p, ncol, S->b_exp.p, Zp,
+               rows, 0, rows, ncol, K, 1);
+      return cudaSuccess;
+    });
+    return r;
+  }
+  *nparts = parts;
+  GpParams* P = new GpParams();
+  P->nprob = parts;
+  P->nitems = 0;
+  const int nq = SS / 4, nt = SS % 4;
+  for (int q = 0; q < parts && g == GI_OK; ++q) {
+    const int k0 = q * per, Kc = std::min(per, K - k0);
+    GpProb& pr = P->p[q];
+    if (Kc <= 0 ||
+        !make_map_groups(&pr.aq, D->mu_slices.p + (size_t)4 * k0, Kc, rows, nq, kBM, K) ||
+        !make_map(&pr.at, D->mu_slices.p + (size_t)4 * nq * rows * K + k0, Kc, rows, nt, kBM, 1,
+                  K) ||
+        !make_map_groups(&pr.bq, S->b_slices.p + (size_t)4 * k0, Kc, ncol, nq, BN, K) ||
+        !make_map(&pr.bt, S->b_slices.p + (size_t)4 * nq * ncol * K + k0, Kc, ncol, nt, BN, 1,
+                  K)) {
+      g = check(c, cudaErrorInvalidValue, "narrow dipole GEMM tensor maps");
+      break;
+    }
+    pr.ea = D->mu_exp.p;
+    pr.eb = S->b_exp.p;
+    pr.C = Zp + (size_t)q * part_stride;
+    pr.ldc = rows;
+    pr.M = rows;
+    pr.Mpad = rows;
+    pr.Nc = ncol;
+    pr.K = Kc;
+    pr.nM = nM;
+    pr.nN = nN;
+    pr.first = P->nitems;
+    P->nitems += nM * nN;
+  }
+  if (g == GI_OK) g = check(c, kernel_attributes(SS), "kernel attributes");
+  if (g == GI_OK) {
+    const int grid = std::min(P->nitems, std::max(c->nsm, 1));
+    const size_t sm = smemg_bytes(SS, BN);
+    g = check(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
+                k_split_gemm_gp<SS, BN, D1><<<grid, kThreadsG, sm, c->stream>>>(*P, S->w,
+                                                                               S->err.p);
+                return cudaGetLastError();
+              }),
+              "narrow dipole GEMM launch");
+  }
+  delete P;
+  return g;
+}
+
 bool split_fused_y(const Ctx* c) { return split_grouped_final(c) && c->Kp <= kFusedYMaxKp; }
 
 gi_status split_build_y_digits(Ctx* c, const double* vecs, int ld, const int32_t* ivec, int nI,

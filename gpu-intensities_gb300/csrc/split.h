@@ -7,6 +7,13 @@ namespace gi {
 // y_digits_ready: split_build_y_digits already wrote Y's digits (Y unused).
 gi_status split_gemm_dipole(Ctx* c, const double* Y, int ldy, double* Z, int ldz, size_t zstride,
                             int ncol, bool y_digits_ready = false);
+// The same for a few columns (the half line strength of single vectors), at
+// the speed of one pass over the dipole digits: K is split into up to
+// max_parts parts whose partial products go to Zp + part * part_stride, laid
+// out [col][*ldz] with component c at rows c * (*ldz / 3); *nparts receives
+// the number of parts to sum.
+gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, double* Zp,
+                                   size_t part_stride, int max_parts, int* nparts, int* ldz);
 // Y of one unit (nI vectors of block `vecs`, ndeg components) built directly
 // into rows [row0, row0 + nI * ndeg * nslot) of the Y digit set of a round of
 // rows_total rows; split_fused_y() says when this path applies.

@@ -1,9 +1,10 @@
 """Engine (CUDA, through the C ABI) against the CPU oracle: identical line
-selection and per-line accuracy in FP64."""
+selection and per-line accuracy in FP64 (relative 1e-11 in S, A and I on
+every line above the workloads' intensity threshold)."""
 import numpy as np
 import pytest
 
-from paritylib import compare
+from paritylib import compare, with_threshold
 
 pytestmark = pytest.mark.gpu
 
@@ -21,6 +22,7 @@ def test_lines_match_oracle(pkg, synth, oracle, case):
         prob = synth.make_c2v(11, 30, [0, 1, 2, 3], nvec_max=8)
     else:
         prob = synth.make_c3v(12, 24, [0, 1, 2, 3], nvec_max=8, reduced=case.endswith("reduced"))
+    with_threshold(prob)
     got, st, _ = run_engine(pkg, prob)
     ref = oracle.run_all(prob)
     res = compare(got, ref)
@@ -30,19 +32,23 @@ def test_lines_match_oracle(pkg, synth, oracle, case):
 
 def test_small_workload_full(pkg, synth, oracle):
     """Every eigenvector of the CPU-sized workload (N=200, J=0..2)."""
-    prob = synth.workload("c2v_small", seed=1)
+    prob = with_threshold(synth.workload("c2v_small", seed=1))
     got, st, _ = run_engine(pkg, prob)
     ref = oracle.run_all(prob)
     res = compare(got, ref)
-    assert res["n"] == 360000
+    assert res["n"] > 50000
     print(res)
 
 
-def test_half_ls_matches_oracle(pkg, synth, oracle):
+@pytest.mark.parametrize("precision", [0, 1])
+def test_half_ls_matches_oracle(pkg, synth, oracle, precision):
+    """gi_half_ls on the FP64 path and on the split path (the narrow digit GEMM
+    with K split over the SMs), normwise within 1e-13 of the oracle."""
     for prob in (synth.make_c2v(3, 16, [1, 2, 3], nvec_max=3),
-                 synth.make_c3v(4, 14, [1, 2, 3], nvec_max=3)):
+                 synth.make_c3v(4, 14, [1, 2, 3], nvec_max=3),
+                 synth.make_c2v(8, 700, [4, 5], nvec_max=2)):
         with pkg.Engine(0) as eng:
-            eng.load(prob)
+            eng.load(prob, precision=precision)
             for (jI, gI), blk in sorted(prob.blocks.items()):
                 if blk.nvec == 0:
                     continue
@@ -59,7 +65,7 @@ def test_half_ls_matches_oracle(pkg, synth, oracle):
 
 
 def test_empty_and_filtered(pkg, synth, oracle):
-    prob = synth.make_c2v(5, 20, [0, 1, 2], nvec_max=6)
+    prob = with_threshold(synth.make_c2v(5, 20, [0, 1, 2], nvec_max=6))
     # an empty block and a symmetry switched off by its spin weight
     b = prob.blocks[(1, 2)]
     prob.blocks[(1, 2)] = synth.Block(1, 2, b.vecs[:0], b.energies[:0], b.quanta[:0])

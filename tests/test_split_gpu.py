@@ -1,9 +1,10 @@
 """Split-precision path (bf16 digit GEMMs on tcgen05) against the CPU oracle:
-identical line selection and <= 1e-10 relative error on S."""
+identical line selection and <= 1e-10 relative error in S, A and I on every
+line above the workloads' intensity threshold."""
 import numpy as np
 import pytest
 
-from paritylib import compare
+from paritylib import compare, with_threshold
 
 pytestmark = pytest.mark.gpu
 
@@ -21,6 +22,7 @@ def test_split_matches_oracle(pkg, synth, oracle, case):
         prob = synth.make_c2v(11, 30, [0, 1, 2, 3], nvec_max=8)
     else:
         prob = synth.make_c3v(12, 24, [0, 1, 2, 3], nvec_max=8, reduced=case.endswith("reduced"))
+    with_threshold(prob)
     got, st = run(pkg, prob)
     res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
     assert st["flops_tensor"] > 0
@@ -28,7 +30,7 @@ def test_split_matches_oracle(pkg, synth, oracle, case):
 
 
 def test_split_small_workload(pkg, synth, oracle):
-    prob = synth.workload("c2v_small", seed=1)
+    prob = with_threshold(synth.workload("c2v_small", seed=1))
     got, st = run(pkg, prob)
     res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
     print(res, st["seconds_gpu"])
@@ -36,7 +38,7 @@ def test_split_small_workload(pkg, synth, oracle):
 
 @pytest.mark.parametrize("slices", [6, 9, 10])
 def test_split_slice_counts(pkg, synth, oracle, slices):
-    prob = synth.make_c2v(4, 40, [0, 1, 2], nvec_max=10)
+    prob = with_threshold(synth.make_c2v(4, 40, [0, 1, 2], nvec_max=10))
     got, _ = run(pkg, prob, slices)
     ref = oracle.run_all(prob)
     tol = {6: 1e-6, 9: 1e-10, 10: 1e-10}[slices]
@@ -77,7 +79,7 @@ def test_every_split_kernel_matches_oracle(pkg, synth, oracle, monkeypatch, conf
     layout, force = config.split("/")
     monkeypatch.setenv("GI_SPLIT_LAYOUT", layout)
     monkeypatch.setenv("GI_SPLIT_FORCE", force)
-    prob = synth.make_c3v(13, 40, [0, 1, 2, 3], nvec_max=20)
+    prob = with_threshold(synth.make_c3v(13, 40, [0, 1, 2, 3], nvec_max=20))
     got, _ = run(pkg, prob)
     res = compare(got, oracle.run_all(prob), rtol_S=1e-10, norm_tol=1e-12)
     print(config, res)
@@ -90,7 +92,7 @@ def test_every_split_kernel_large_k(pkg, synth, monkeypatch, config):
     to ~2100 (final states), where the exact integer diagonal sums reach the
     int64 range, against the FP64 GPU path on the same job."""
     layout, force = config.split("/")
-    prob = synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12)
+    prob = with_threshold(synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12))
     with pkg.Engine(0) as eng:
         eng.load(prob, precision=pkg.GI_PREC_FP64)
         eng.run()
