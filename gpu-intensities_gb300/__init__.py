@@ -65,7 +65,9 @@ class gi_stats(C.Structure):
                 ("flops_halfls", C.c_double), ("flops_final", C.c_double),
                 ("flops_tensor", C.c_double), ("bytes_correlate", C.c_double),
                 ("seconds_phase", C.c_double * 6), ("launches_phase", C.c_int32 * 6),
-                ("kernel_launches", C.c_int32), ("reserved", C.c_int32)]
+                ("kernel_launches", C.c_int32), ("reserved", C.c_int32),
+                ("nlines_doubtful", C.c_int64), ("nlines_handed", C.c_int64),
+                ("nlines_refined", C.c_int64)]
 
 
 class gi_serve_config(C.Structure):
@@ -166,6 +168,7 @@ def lib():
         L.gi_set_block_device.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.c_void_p, f64p, i32p]
         L.gi_run.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_int64)]
+        L.gi_set_refine.argtypes = [C.c_void_p, C.c_int64]
         L.gi_run_shard.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int64)]
         L.gi_deck_parse.argtypes = [C.c_char_p, C.POINTER(gi_deck), C.c_char_p, C.c_size_t]
         L.gi_trove_read_basis.argtypes = [C.c_char_p, C.c_int, C.c_int, i32p, i32p, i32p, i32p,
@@ -366,6 +369,11 @@ class Engine:
         """Split GEMM autotuner: mode 1 times the candidate launch configurations
         on the first GEMM of each new shape class; path keeps the table on disk."""
         self._ck(self._L.gi_set_tuning(self._h, mode, path.encode() if path else None))
+
+    def set_refine(self, max_lines: int):
+        """Re-evaluate up to max_lines doubtful lines per run exactly
+        (gi_set_refine); lines next to a threshold are always re-evaluated."""
+        self._ck(self._L.gi_set_refine(self._h, int(max_lines)))
 
     def set_symmetry(self, sym_type: int):
         self._ck(self._L.gi_set_symmetry(self._h, sym_type))

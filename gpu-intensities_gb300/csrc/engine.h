@@ -74,6 +74,12 @@ struct StencilTerm {
   double coef;
 };
 
+// A line handed to the exact re-evaluation: initial vector i of the part's
+// unit, final record f, and its slot in the line list (-1: not kept).
+struct RefineRec {
+  int32_t part, i, f, slot;
+};
+
 // Process-wide serial numbers: a captured launch sequence is tied to the
 // exact basis objects it read.
 uint64_t next_uid();
@@ -250,6 +256,9 @@ struct Ctx {
   DevArray<int32_t> w_ivec, w_int;
   DevArray<uint8_t> w_upper;
   DevArray<StencilTerm> w_stencil;
+  DevArray<double> w_hn;       // H column norms of a group of final blocks
+  DevArray<RefineRec> w_rec;   // lines handed to the exact re-evaluation
+  int64_t refine_max = 0;      // doubtful lines re-evaluated per run (gi_set_refine)
   DevArray<int32_t> w_stencil_n, w_levelI, w_levelF;
 };
 
@@ -317,7 +326,14 @@ struct EpiParams {
   int jI, jF, ndegI, ndegF, reduced, combo_mask;
   double gns, zpe, beta, q_stat, fw0, fw1, thresh_S, thresh_I;
   double A_coef, intens_cm_mol, avogno;
+  // exact re-evaluation of doubtful lines (refine.cu): the estimated error of
+  // a transition moment per unit of its H column's norm, the relative
+  // accuracy S must reach without it, the part (initial unit x final block)
+  // the launch serves, and whether lines past that accuracy are handed over
+  double err_coef, target;
+  int part, refine_cond;
 };
+
 
 cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int nI, int ndeg,
                            const Basis& b, int gamma, int degen, int N, int Kp, double* Y,
@@ -335,10 +351,38 @@ cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstri
                                       int cstride, const Basis& bF, const StencilTerm* st,
                                       const int32_t* st_n, int st_max, double* h,
                                       cudaStream_t s);
+// What the exact re-evaluation (refine.cu) needs of one epilogue part, an
+// initial unit against one final block; host arrays live for the run.
+struct RefinePart {
+  const Block* bI;
+  const Block* bF;
+  const Basis* basI;
+  const Basis* basF;
+  int gI, gF;
+  const int32_t* rec_i;  // the unit's initial record ids
+  const int32_t* lvl_i;  // their line ids (level table index or record)
+  const double* EI;      // their energies
+  const int32_t* lvl_f;  // line id of every final record
+  const StencilTerm* st_dev;
+  const int32_t* stn_dev;
+  EpiParams ep;
+};
+// Re-evaluates the n handed-over lines exactly and patches the run's line
+// list (c->nlines, the device lines and, when the run copied them there, the
+// host lines).
+gi_status refine_lines(Ctx* c, const std::vector<RefinePart>& parts, const RefineRec* recs,
+                       size_t n, int64_t* refined);
+// counter[0]: lines kept, [1]: lines passing the filters, [2]: lines handed
+// to the exact re-evaluation (records past rec_cap are counted, not stored).
+// hn: the norms of the part's H columns (column (i ndegI + dI) ndegF + dF).
 cudaError_t launch_epilogue(const double* T, int ldt, int nI, int nF, const int32_t* levelI,
                             const double* EI, const int32_t* levelF, const double* EF,
-                            const uint8_t* upper_ok, const EpiParams& p, gi_line* out,
-                            unsigned long long* counter, long long cap, cudaStream_t s);
+                            const uint8_t* upper_ok, const double* hn, const EpiParams& p,
+                            gi_line* out, unsigned long long* counter, long long cap,
+                            RefineRec* rec, long long rec_cap, cudaStream_t s);
+// out[col] = || H[col * ldh + 0 .. n) ||_2 for col < ncol.
+cudaError_t launch_col_norms(const double* H, int ldh, int n, int ncol, double* out,
+                             cudaStream_t s);
 // C[z][n*ldc + m] = sum_k A[z][m*lda + k] * B[n*ldb + k]; K multiple of 16.
 cudaError_t gemm_fp64_nt(const double* A, int lda, size_t strideA, const double* B, int ldb,
                          double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch,

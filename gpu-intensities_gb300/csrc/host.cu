@@ -534,8 +534,10 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   }
   GI_CUDA(c, c->w_int.assign(h_int));
   GI_CUDA(c, c->w_upper.assign(h_upper));
-  GI_CUDA(c, c->w_counter.reserve(2));
-  GI_CUDA(c, cudaMemsetAsync(c->w_counter.p, 0, 2 * sizeof(unsigned long long), c->stream));
+  // [0] lines kept, [1] lines passing the filters, [2] lines handed to the
+  // exact re-evaluation, [3] kept lines whose error estimate passes the target
+  GI_CUDA(c, c->w_counter.reserve(4));
+  GI_CUDA(c, cudaMemsetAsync(c->w_counter.p, 0, 4 * sizeof(unsigned long long), c->stream));
 
   // line buffer: the whole job on the device
   GI_CUDA(c, c->d_lines.reserve(std::max<size_t>(cap_total, 1)));
@@ -679,6 +681,11 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     }
   }
   GI_CUDA(c, c->w_h.reserve(max_h));
+  GI_CUDA(c, c->w_hn.reserve(max_gcols));  // H column norms of a group
+  // lines handed to the exact re-evaluation: the doubtful lines the caller
+  // allows plus room for the lines next to a threshold
+  const long long rec_cap = std::max<long long>(c->refine_max, 0) + 4096;
+  GI_CUDA(c, c->w_rec.reserve((size_t)rec_cap));
   GI_CUDA(c, c->w_t.reserve(max_t));
   if (P.precision == GI_PREC_SPLIT) {
     // every allocation of the launch sequence happens here, before it
@@ -738,9 +745,12 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     for (void* q : {(void*)c->w_y.p, (void*)c->w_z.p, (void*)c->w_h.p, (void*)c->w_t.p,
                     (void*)c->w_EI.p, (void*)c->w_ivec.p, (void*)c->w_int.p, (void*)c->w_upper.p,
                     (void*)c->w_stencil.p, (void*)c->w_stencil_n.p, (void*)c->w_counter.p,
+                    (void*)c->w_hn.p, (void*)c->w_rec.p,
                     (void*)c->d_lines.p})
       mixv(q);
     mixv(c->d_lines.n);
+    mixv(c->refine_max);
+    mixv(rec_cap);
     mixv(c->ck_count);
     mixv(grouped_final);
     mixv(fused_y);
@@ -763,6 +773,67 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
           mixv(T.hcol[k]); mixv(T.parts[k].first->off); mixv(T.parts[k].first->ycol);
           mixv(T.parts[k].second->combo_mask); mixv(T.parts[k].second->st_off);
         }
+      }
+    }
+  }
+
+  // one epilogue part per (unit, final block) of every round: its launch
+  // parameters, and what the exact re-evaluation needs of it
+  auto epi_params = [&](const Unit& u, const PairPlan* pp, const Block& fb, int part) {
+    EpiParams ep{};
+    ep.jI = u.I->blk->J;
+    ep.jF = fb.J;
+    ep.ndegI = c->degen[u.I->blk->gamma];
+    ep.ndegF = c->degen[fb.gamma];
+    ep.reduced = P.reduced;
+    ep.combo_mask = pp->combo_mask;
+    ep.gns = P.gns[u.I->blk->gamma];
+    ep.zpe = zpe;
+    ep.beta = beta;
+    ep.q_stat = qstat;
+    ep.fw0 = P.freq_window[0];
+    ep.fw1 = P.freq_window[1];
+    ep.thresh_S = P.thresh_linestrength;
+    ep.thresh_I = P.thresh_intensity;
+    ep.A_coef = ph.A_coef;
+    ep.intens_cm_mol = ph.intens_cm_mol;
+    ep.avogno = ph.avogno;
+    // a moment's error: ~K units of FP64 rounding of |H col| / sqrt(nsize_F)
+    // (the size of a typical moment of that column); K measured on both paths
+    const double K = P.precision == GI_PREC_SPLIT ? 64.0 : 16.0;
+    ep.err_coef = K * 1.1102230246251565e-16 / std::sqrt((double)std::max(fb.nsize, 1));
+    ep.target = P.precision == GI_PREC_SPLIT ? 1e-11 : 1e-12;
+    ep.part = part;
+    ep.refine_cond = c->refine_max > 0 ? 1 : 0;
+    return ep;
+  };
+  std::vector<RefinePart> rparts;
+  std::vector<std::vector<std::vector<int>>> part_of(rounds.size());  // [round][target][k]
+  for (size_t r = 0; r < rounds.size(); r++) {
+    part_of[r].resize(targets[r].size());
+    for (size_t t = 0; t < targets[r].size(); t++) {
+      const Target& T = targets[r][t];
+      const Block& fb = *T.F->blk;
+      const auto off = farr[T.F];
+      for (size_t k = 0; k < T.parts.size(); k++) {
+        const Unit& u = *T.parts[k].first;
+        const PairPlan* pp = T.parts[k].second;
+        RefinePart rp;
+        rp.bI = u.I->blk;
+        rp.bF = &fb;
+        rp.basI = c->bases[u.I->blk->J].get();
+        rp.basF = c->bases[fb.J].get();
+        rp.gI = u.I->blk->gamma;
+        rp.gF = fb.gamma;
+        rp.rec_i = h_ivec.data() + 2 * u.off;
+        rp.lvl_i = h_ivec.data() + 2 * u.off + u.nI;
+        rp.EI = h_EI.data() + u.off;
+        rp.lvl_f = h_int.data() + off.first;
+        rp.st_dev = c->w_stencil.p + pp->st_off * 6;
+        rp.stn_dev = c->w_stencil_n.p + pp->st_off;
+        rp.ep = epi_params(u, pp, fb, (int)rparts.size());
+        part_of[r][t].push_back((int)rparts.size());
+        rparts.push_back(rp);
       }
     }
   }
@@ -828,6 +899,19 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
                   }));
         }
       }
+      // the norms of every H column of the group (the error scale of its moments)
+      size_t hn_off = 0;
+      std::vector<size_t> hn_at(grp.second - grp.first);
+      for (size_t t = grp.first; t < grp.second; t++) {
+        const Target& T = targets[r][t];
+        const Block& fb = *T.F->blk;
+        hn_at[t - grp.first] = hn_off;
+        GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+                  return launch_col_norms(c->w_h.p + T.hoff, fb.ld, fb.nsize, (int)T.ncolH,
+                                          c->w_hn.p + hn_off, c->stream);
+                }));
+        hn_off += T.ncolH;
+      }
       // the final-state GEMMs: one persistent launch for the group, or one per block
       if (grouped_final) {
         std::vector<FinalJob> jobs;
@@ -862,38 +946,21 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         const Target& T = targets[r][t];
         BlockPlan& Fp = *T.F;
         const Block& fb = *Fp.blk;
-        const int ndegF = c->degen[fb.gamma];
         const int ldt = round_up(fb.nvec, 2);
         fl_final += 2.0 * fb.nsize * (double)fb.nvec * T.ncolH;
         const auto off = farr[&Fp];
         for (size_t k = 0; k < T.parts.size(); k++) {
           const Unit& u = *T.parts[k].first;
-          const PairPlan* pp = T.parts[k].second;
-          EpiParams ep{};
-          ep.jI = u.I->blk->J;
-          ep.jF = fb.J;
-          ep.ndegI = c->degen[u.I->blk->gamma];
-          ep.ndegF = ndegF;
-          ep.reduced = P.reduced;
-          ep.combo_mask = pp->combo_mask;
-          ep.gns = P.gns[u.I->blk->gamma];
-          ep.zpe = zpe;
-          ep.beta = beta;
-          ep.q_stat = qstat;
-          ep.fw0 = P.freq_window[0];
-          ep.fw1 = P.freq_window[1];
-          ep.thresh_S = P.thresh_linestrength;
-          ep.thresh_I = P.thresh_intensity;
-          ep.A_coef = ph.A_coef;
-          ep.intens_cm_mol = ph.intens_cm_mol;
-          ep.avogno = ph.avogno;
+          const EpiParams ep = rparts[part_of[r][t][k]].ep;
           const int32_t* d_lvI = c->w_ivec.p + 2 * u.off + u.nI;
+          const double* hn = c->w_hn.p + hn_at[t - grp.first] + T.hcol[k];
           GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
                     return launch_epilogue(c->w_t.p + T.toff + T.hcol[k] * ldt, ldt, u.nI,
                                            fb.nvec, d_lvI, d_EI.p + u.off,
                                            c->w_int.p + off.first, fb.d_energies.p,
-                                           c->w_upper.p + off.second, ep, c->d_lines.p,
-                                           c->w_counter.p, (long long)c->d_lines.n, c->stream);
+                                           c->w_upper.p + off.second, hn, ep, c->d_lines.p,
+                                           c->w_counter.p, (long long)c->d_lines.n, c->w_rec.p,
+                                           rec_cap, c->stream);
                   }));
           npairs_checked += (int64_t)u.nI * Fp.nupper;
         }
@@ -990,7 +1057,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       }
     }
   }
-  unsigned long long counts[2] = {0, 0};
+  unsigned long long counts[4] = {0, 0, 0, 0};
   GI_CUDA(c, cudaMemcpyAsync(counts, c->w_counter.p, sizeof(counts), cudaMemcpyDeviceToHost, c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));
   if (P.precision == GI_PREC_SPLIT) {
@@ -1025,6 +1092,20 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     GI_CUDA(c, cudaEventElapsedTime(&pm, r.a, r.b));
     c->stats.seconds_phase[r.phase] += pm * 1e-3;
   }
+  // lines next to a threshold, and doubtful lines up to the caller's limit:
+  // exact re-evaluation, then the line list is patched
+  const size_t nrec = (size_t)std::min<unsigned long long>(counts[2], (unsigned long long)rec_cap);
+  int64_t nrefined = 0;
+  if (nrec) {
+    std::vector<RefineRec> recs(nrec);
+    GI_CUDA(c, cudaMemcpy(recs.data(), c->w_rec.p, sizeof(RefineRec) * nrec,
+                          cudaMemcpyDeviceToHost));
+    gi_status s = refine_lines(c, rparts, recs.data(), nrec, &nrefined);
+    if (s != GI_OK) return s;
+  }
+  c->stats.nlines_handed = (int64_t)counts[2];
+  c->stats.nlines_doubtful = (int64_t)counts[3];
+  c->stats.nlines_refined = nrefined;
   c->stats.nlines_filtered = (int64_t)counts[1];
   c->stats.nlines = c->nlines;
   c->stats.npairs_checked = npairs_checked;
@@ -1121,6 +1202,13 @@ gi_status gi_set_tuning(gi_ctx* h, int mode, const char* path) {
   if (c->server) return fail(c, GI_ERR_STATE, "gi_set_tuning while serving");
   c->tune_mode = mode;
   c->tune_path = path ? path : "";
+  return GI_OK;
+}
+
+gi_status gi_set_refine(gi_ctx* h, int64_t max_lines) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || max_lines < 0) return GI_ERR_ARG;
+  c->refine_max = max_lines;
   return GI_OK;
 }
 

@@ -185,16 +185,17 @@ cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstri
 __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF,
                            const int32_t* __restrict__ levelI, const double* __restrict__ EI,
                            const int32_t* __restrict__ levelF, const double* __restrict__ EF,
-                           const uint8_t* __restrict__ upper_ok, EpiParams p,
+                           const uint8_t* __restrict__ upper_ok,
+                           const double* __restrict__ hn, EpiParams p,
                            gi_line* __restrict__ out, unsigned long long* counter,
-                           long long cap) {
+                           long long cap, RefineRec* __restrict__ rec, long long rec_cap) {
   const int f = blockIdx.x * blockDim.x + threadIdx.x;
   const int i = blockIdx.y;
   // the initial level's Boltzmann factor, once per block (FP64 exp is scarce)
   __shared__ double boltz_i;
   if (threadIdx.x == 0) boltz_i = exp(-(EI[i] - p.zpe) * p.beta);
   __syncthreads();
-  bool keep = false, pass = false;
+  bool keep = false, pass = false, doubt = false;
   gi_line L;
   if (f < nF && upper_ok[f]) {
     const double ei = EI[i], ef = EF[f];
@@ -217,6 +218,26 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
       const double S = ls * p.gns * (double)((2 * p.jI + 1) * (2 * p.jF + 1));
       const double In = S * p.intens_cm_mol * boltz_fc;
       keep = (S >= p.thresh_S) && (In / p.avogno >= p.thresh_I);
+      // doubtful lines: the relative error of S estimated from the moments and
+      // their columns' norms (an error of err_coef * |H col| per moment); a
+      // kept line whose estimate passes the target, and any line whose S or I
+      // sits within the estimate of a threshold, is re-evaluated exactly
+      double num = 0.0, den = 0.0;
+      for (int dF = 0; dF < p.ndegF; ++dF)
+        for (int dI = 0; dI < p.ndegI; ++dI)
+          if (p.combo_mask & (1 << (dI + 2 * dF))) {
+            const double tq = t[dI + 2 * dF];
+            num += fabs(tq) * hn[(i * p.ndegI + dI) * p.ndegF + dF];
+            den += tq * tq;
+          }
+      const double rel = den > 0.0 ? 2.0 * p.err_coef * num / den : 0.0;
+      const double band = 4.0 * rel + 1e-14;
+      const bool near_S = p.thresh_S > 0.0 && fabs(S - p.thresh_S) <= band * p.thresh_S;
+      const double Im = In / p.avogno;
+      const bool near_I = p.thresh_I > 0.0 && fabs(Im - p.thresh_I) <= band * p.thresh_I;
+      const bool doubtful = keep && rel > p.target;
+      if (doubtful) atomicAdd(counter + 3, 1ull);
+      doubt = near_S || near_I || (doubtful && p.refine_cond);
       L.level_i = levelI[i];
       L.level_f = levelF[f];
       L.ndeg_i = p.ndegI;
@@ -233,25 +254,56 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
   const unsigned pmask = __ballot_sync(0xffffffffu, pass);
   if (pmask && lane == 0) atomicAdd(counter + 1, (unsigned long long)__popc(pmask));
   const unsigned mask = __ballot_sync(0xffffffffu, keep);
-  if (mask == 0) return;
-  const int leader = __ffs(mask) - 1;
-  unsigned long long base = 0;
-  if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (keep) {
-    const unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
-    if ((long long)pos < cap) out[pos] = L;
+  long long slot = -1;
+  if (mask) {
+    const int leader = __ffs(mask) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (keep) {
+      const unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
+      if ((long long)pos < cap) out[pos] = L;
+      slot = (long long)pos;
+    }
   }
+  if (doubt) {
+    const unsigned long long k = atomicAdd(counter + 2, 1ull);
+    if ((long long)k < rec_cap) rec[k] = RefineRec{p.part, i, f, (int32_t)slot};
+  }
+}
+
+// Euclidean norm of each H column (the scale of its transition moments' error).
+__global__ void k_col_norms(const double* __restrict__ H, int ldh, int n, double* __restrict__ out) {
+  const double* h = H + (size_t)blockIdx.x * ldh;
+  double acc = 0.0;
+  for (int s = threadIdx.x; s < n; s += blockDim.x) acc = fma(h[s], h[s], acc);
+  __shared__ double part[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) out[blockIdx.x] = sqrt(acc);
+  }
+}
+
+cudaError_t launch_col_norms(const double* H, int ldh, int n, int ncol, double* out,
+                             cudaStream_t s) {
+  if (ncol <= 0) return cudaSuccess;
+  k_col_norms<<<ncol, 256, 0, s>>>(H, ldh, n, out);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_epilogue(const double* T, int ldt, int nI, int nF, const int32_t* levelI,
                             const double* EI, const int32_t* levelF, const double* EF,
-                            const uint8_t* upper_ok, const EpiParams& p, gi_line* out,
-                            unsigned long long* counter, long long cap, cudaStream_t s) {
+                            const uint8_t* upper_ok, const double* hn, const EpiParams& p,
+                            gi_line* out, unsigned long long* counter, long long cap,
+                            RefineRec* rec, long long rec_cap, cudaStream_t s) {
   if (nI == 0 || nF == 0) return cudaSuccess;
   dim3 grid((nF + 127) / 128, nI);
-  k_epilogue<<<grid, 128, 0, s>>>(T, ldt, nI, nF, levelI, EI, levelF, EF, upper_ok, p, out,
-                                  counter, cap);
+  k_epilogue<<<grid, 128, 0, s>>>(T, ldt, nI, nF, levelI, EI, levelF, EF, upper_ok, hn, p, out,
+                                  counter, cap, rec, rec_cap);
   return cudaGetLastError();
 }
 

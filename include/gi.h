@@ -140,6 +140,11 @@ typedef struct {
   int32_t launches_phase[GI_NPHASE];
   int32_t kernel_launches; /* kernels launched by the last gi_run */
   int32_t reserved;
+  int64_t nlines_doubtful; /* kept lines whose estimated relative error of S passes the
+                              accuracy target (1e-12 FP64, 1e-11 split) */
+  int64_t nlines_handed;   /* lines handed to the exact re-evaluation: lines within their
+                              error of a threshold, and doubtful lines up to the refine limit */
+  int64_t nlines_refined;  /* of those, re-evaluated (all unless the record buffer overflowed) */
 } gi_stats;
 
 /* Context ---------------------------------------------------------------- */
@@ -162,6 +167,19 @@ gi_status gi_set_stream(gi_ctx* ctx, void* stream);
  * process.  Tuning is skipped inside a CUDA-graph capture.  No counterpart in
  * the reference (fixed launch shapes, dipole_kernals.cu:162-227). */
 gi_status gi_set_tuning(gi_ctx* ctx, int mode, const char* path);
+/* Exact re-evaluation of doubtful lines.  Every transition moment carries an
+ * error of a few units of FP64 rounding of its H column's norm; a line whose
+ * moment cancels far below that column (its estimated relative error of S
+ * passes 1e-12 on the FP64 path or 1e-11 split) is doubtful.  With
+ * max_lines > 0 up to that many doubtful lines per run are recomputed in
+ * double-double arithmetic (their initial column's half line strength, the
+ * final dot) and their S, A, I replaced; 0 (the default) leaves them at the
+ * GEMM paths' accuracy.  Independently of this setting, every line whose S or
+ * I lies within its estimated error of a threshold is re-evaluated before the
+ * keep decision, so line selection does not depend on rounding.  Counts are in
+ * gi_stats.  No counterpart in the reference, which evaluates every line in
+ * plain FP64 (cuda_host.cu:1301-1317). */
+gi_status gi_set_refine(gi_ctx* ctx, int64_t max_lines);
 const char* gi_last_error(const gi_ctx* ctx);
 const char* gi_status_string(gi_status s);
 

@@ -51,9 +51,12 @@ def test_workload_sample_matches_oracle(pkg, samples, name, precision):
     prec = pkg.GI_PREC_SPLIT if precision == "split" else pkg.GI_PREC_FP64
     with pkg.Engine(0) as eng:
         eng.load(prob, precision=prec)
+        eng.set_refine(1 << 20)  # doubtful lines re-evaluated exactly
         eng.run()
         got = pkg.keyed(eng.lines(), eng.levels())
+        st = eng.stats()
     tol = 1e-10 if precision == "split" else 1e-11
     res = compare(got, ref, rtol_S=tol, norm_tol=tol / 10)
-    print(name, precision, res)
+    print(name, precision, res, "doubtful", st["nlines_doubtful"], "refined",
+          st["nlines_refined"])
     assert res["n"] > 1000

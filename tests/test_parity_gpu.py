@@ -9,9 +9,12 @@ from paritylib import compare, with_threshold
 pytestmark = pytest.mark.gpu
 
 
-def run_engine(pkg, prob, **kw):
+def run_engine(pkg, prob, refine=1 << 20, **kw):
+    """One job; doubtful lines (moments cancelled far below their columns)
+    re-evaluated exactly, up to `refine` per run."""
     with pkg.Engine(0) as eng:
         eng.load(prob, **kw)
+        eng.set_refine(refine)
         eng.run()
         return pkg.keyed(eng.lines(), eng.levels()), eng.stats(), eng.levels()
 
@@ -179,3 +182,33 @@ def test_host_readback_equals_device_lines(pkg, synth, budget):
             n = eng.run(lines_on_device=False, graph=graph)
             assert n == len(ref)
             assert np.array_equal(np.sort(eng.lines(), order=["level_i", "level_f"]), ref)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("which", ["S", "I"])
+def test_threshold_guard_band(pkg, synth, oracle, precision, which):
+    """A threshold placed 2e-15 (relative, a few units of rounding) from a
+    line's S or I, on either side: closer than the GEMM paths' error, so
+    without the guard band the keep decision would follow rounding.  The
+    engine re-evaluates lines that close to a threshold exactly before the
+    keep decision, so its selection is the oracle's (double-double) one, on
+    the FP64 and the split path."""
+    prob = with_threshold(synth.make_c2v(21, 30, [0, 1, 2], nvec_max=8))
+    ref = oracle.run_all(prob)
+    assert len(ref) > 100
+    key = "S" if which == "S" else "I"
+    picks = np.argsort(ref[key])[[len(ref) // 5, len(ref) // 2, 4 * len(ref) // 5]]
+    for idx in picks:
+        for side in (-1.0, 1.0):
+            v = float(ref[key][idx]) * (1.0 + side * 2e-15)
+            if which == "S":
+                prob.params.thresh_linestrength = v
+            else:
+                prob.params.thresh_intensity = v / 6.0221415e23
+            want = oracle.run_all(prob)
+            got, st, _ = run_engine(pkg, prob, refine=0, precision=precision)
+            assert st["nlines_handed"] >= 1
+            compare(got, want, rtol_S=1e-10 if precision else 1e-11,
+                    norm_tol=1e-12 if precision else 1e-13)
+        prob.params.thresh_linestrength = 0.0
+        with_threshold(prob)

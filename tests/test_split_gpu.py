@@ -9,9 +9,10 @@ from paritylib import compare, with_threshold
 pytestmark = pytest.mark.gpu
 
 
-def run(pkg, prob, slices=0):
+def run(pkg, prob, slices=0, refine=1 << 20):
     with pkg.Engine(0) as eng:
         eng.load(prob, precision=pkg.GI_PREC_SPLIT, split_slices=slices)
+        eng.set_refine(refine)
         eng.run()
         return pkg.keyed(eng.lines(), eng.levels()), eng.stats()
 
@@ -95,6 +96,7 @@ def test_every_split_kernel_large_k(pkg, synth, monkeypatch, config):
     prob = with_threshold(synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12))
     with pkg.Engine(0) as eng:
         eng.load(prob, precision=pkg.GI_PREC_FP64)
+        eng.set_refine(1 << 20)
         eng.run()
         want = pkg.keyed(eng.lines(), eng.levels())
     monkeypatch.setenv("GI_SPLIT_LAYOUT", layout)
