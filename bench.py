@@ -87,11 +87,15 @@ def parse(argv=None):
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-legs", action="store_true",
                     help="skip the other workloads (c2v_plain, c2v_precision, serving, streamed)")
-    ap.add_argument("--legs", default="plain,precision,serving,streamed")
-    ap.add_argument("--serve-jmax", type=int, default=4,
-                    help="serving: pair jobs of the J <= jmax part of c2v_plain")
+    ap.add_argument("--legs", default="plain,precision,serving,streamed,halfls")
+    ap.add_argument("--only", default=None,
+                    help="run only these legs (comma list) and print their JSON, no headline")
+    ap.add_argument("--serve-jobs", type=int, default=10000, help="serving: jobs (split path)")
+    ap.add_argument("--serve-fp64-jobs", type=int, default=50,
+                    help="serving: the first jobs of the stream again on the FP64 path")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: Poisson jobs/s")
     ap.add_argument("--serve-slots", type=int, default=3)
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0)
     ap.add_argument("--tune-table", default=None,
                     help="autotuner table file: read if present, extended and written")
     return ap.parse_args(argv)
@@ -317,44 +321,98 @@ def main_reference(args):
 
 
 # ---------------------------------------------------------------- serving
-def serve_bench(pkg, args, device, precision):
-    """Pair jobs (J, Gamma) -> (J', Gamma') of the J <= serve_jmax part of
-    c2v_plain, submitted in random order with Poisson arrivals at serve_rate
-    jobs/s to a serving context; latency is submit -> lines on the host."""
-    prob = make_problem(args, workload="c2v_plain", jlist=range(args.serve_jmax + 1))
-    jobs = prob.pair_jobs()
-    rng = np.random.default_rng(args.seed + 17)
-    order = [jobs[i] for i in rng.permutation(len(jobs))]
-    gaps = rng.exponential(1.0 / args.serve_rate, size=len(order))
+def serve_stream(pkg, pool, jobs, gaps, device, precision, args):
+    """Submits the jobs with their Poisson gaps to a serving context over the
+    pool; a reaper thread waits for every job (latency = submit -> lines in
+    host memory) and releases it.  Returns the server's statistics."""
     with pkg.Engine(device) as eng:
-        eng.load(prob, precision=precision, split_slices=args.slices)
-        eng.serve_start(slots=args.serve_slots)
-        eng.job_lines(eng.submit(*order[0]))  # first launch of every kernel
+        eng.load(pool, precision=precision, split_slices=args.slices)
+        eng.serve_start(slots=args.serve_slots, budget=int(args.serve_budget_gb * 1e9))
+        w = eng.submit(*jobs[0])  # first launch of every kernel
+        eng.wait(w)
+        eng.release(w)
         eng.serve_reset_stats()
-        ids = []
+        ids, errors = [], []
+        lock = threading.Lock()
+        done = threading.Event()
+
+        def reap():
+            k = 0
+            while True:
+                with lock:
+                    nxt = ids[k] if k < len(ids) else None
+                if nxt is None:
+                    if done.is_set():
+                        with lock:
+                            if k >= len(ids):
+                                return
+                    time.sleep(0.001)
+                    continue
+                info = eng.wait(nxt, check=False)
+                if info["state"] != pkg.GI_JOB_DONE:
+                    errors.append(info["status"])
+                eng.release(nxt)
+                k += 1
+
+        th = threading.Thread(target=reap, daemon=True)
         t0 = time.perf_counter()
+        th.start()
         due = t0
-        for job, gap in zip(order, gaps):
+        for job, gap in zip(jobs, gaps):
             due += gap
             delay = due - time.perf_counter()
             if delay > 0:
                 time.sleep(delay)
-            ids.append(eng.submit(*job))
-        for i in ids:
-            eng.job_lines(i)
+            i = eng.submit(*job)
+            with lock:
+                ids.append(i)
+        done.set()
+        th.join()
         makespan = time.perf_counter() - t0
         st = eng.serve_stats()
         eng.serve_stop()
-    return {"workload": f"c2v_plain J<={args.serve_jmax} pair jobs", "jobs": len(order),
-            "arrival": f"Poisson {args.serve_rate:g} jobs/s, random order",
-            "slots": st["slots"], "precision": "split" if precision else "fp64",
-            "latency_p50_s": st["latency_p50"], "latency_p99_s": st["latency_p99"],
-            "latency_max_s": st["latency_max"], "latency_mean_s": st["latency_mean"],
-            "queue_p50_s": st["queue_p50"], "queue_p99_s": st["queue_p99"],
-            "makespan_s": makespan, "value": st["lines_filtered"] / makespan, "unit": METRIC,
-            "lines_filtered": st["lines_filtered"], "lines_above_threshold": st["lines"],
-            "failed": st["failed"], "evictions": st["evictions"],
-            "budget_bytes": st["budget_bytes"], "peak_resident_bytes": st["peak_resident_bytes"]}
+    st["makespan_s"] = makespan
+    st["reaped_failures"] = len(errors)
+    return st
+
+
+def serving_leg(pkg, args, device, base):
+    """Config 5: pair jobs drawn from the batched C3v generator (initial block
+    dimensions log-uniform in 500..80k, 100..2000 vectors per block), Poisson
+    arrivals, blocks resident under an HBM budget with LRU eviction of blocks
+    (to pinned host memory) and of cached half line strengths."""
+    from gpu_intensities_gb300 import synth
+    if base is None:
+        base = make_problem(args, workload="c3v_batched")
+    pool = synth.serving_pool(base, seed=args.seed + 40)
+    jobs, gaps = synth.serving_jobs(pool, seed=args.seed + 41, njobs=args.serve_jobs,
+                                    rate=args.serve_rate)
+    out = {"workload": "serving: pool of every C3v J=0..40 block (Nvib=3000) with 100..2000 "
+                       "vectors (log-uniform), pair jobs with initial block dimension "
+                       "log-uniform in 500..80k",
+           "pool_vector_bytes": int(sum(b.vecs.nbytes for b in pool.blocks.values())),
+           "arrival": f"Poisson {args.serve_rate:g} jobs/s", "slots": args.serve_slots,
+           "budget_bytes": int(args.serve_budget_gb * 1e9)}
+    for name, prec, n in (("split", pkg.GI_PREC_SPLIT, args.serve_jobs),
+                          ("fp64", pkg.GI_PREC_FP64, args.serve_fp64_jobs)):
+        if n <= 0:
+            continue
+        st = serve_stream(pkg, pool, jobs[:n], gaps[:n], device, prec, args)
+        out[name] = {"jobs": n, "completed": st["completed"], "failed": st["failed"],
+                     "latency_p50_s": st["latency_p50"], "latency_p99_s": st["latency_p99"],
+                     "latency_max_s": st["latency_max"], "latency_mean_s": st["latency_mean"],
+                     "queue_p50_s": st["queue_p50"], "queue_p99_s": st["queue_p99"],
+                     "makespan_s": st["makespan_s"],
+                     "value": st["lines_filtered"] / st["makespan_s"], "unit": METRIC,
+                     "lines_filtered": st["lines_filtered"], "lines_above_threshold": st["lines"],
+                     "block_evictions": st["evictions"], "block_restores": st["restores"],
+                     "zcache_hits": st["zcache_hits"], "zcache_misses": st["zcache_misses"],
+                     "zcache_evictions": st["zcache_evictions"],
+                     "peak_resident_bytes": st["peak_resident_bytes"]}
+    if "fp64" in out:
+        out["fp64"]["note"] = (f"the first {args.serve_fp64_jobs} jobs of the same stream: the "
+                               "FP64 path cannot keep up with 200 jobs/s, so its queue grows")
+    return out
 
 
 # ---------------------------------------------------------------- helpers
@@ -480,6 +538,43 @@ def leg_c2v_precision(pkg, args, device, timer_of):
     return out
 
 
+def leg_half_ls(pkg, args, device, timer_of, peaks):
+    """The kernel-level drop-in for do_1st_half_ls (gi_half_ls): the half line
+    strength of one initial vector of C2v J = 10 (Nvib = 2000, 22 (k, tau)
+    slots) towards J = 10, per call.  The split path is one pass over the
+    dipole's digit planes (the narrow digit GEMM, K split over the SMs); the
+    FP64 path is the DMMA GEMM."""
+    import torch
+    prob = make_problem(args, workload="c2v_plain", jlist=[9, 10])
+    blk = prob.blocks[(10, 0)]
+    DF = prob.bases[10].Maxcontracts
+    N = prob.N
+    Kp = -(-N // 64) * 64
+    Mpad = -(-N // 128) * 128
+    digit_bytes = 3 * Mpad * Kp * 9 * 2
+    out = {"workload": f"gi_half_ls: one C2v J=10 vector (nsize {blk.nsize}) towards J=10, Nvib={N}",
+           "dipole_fp64_bytes": 3 * N * N * 8, "dipole_digit_bytes": digit_bytes}
+    for name, prec in (("split", pkg.GI_PREC_SPLIT), ("fp64", pkg.GI_PREC_FP64)):
+        with pkg.Engine(device) as eng:
+            stream = torch.cuda.Stream(device=device)
+            eng.set_stream(stream.cuda_stream)
+            timer = timer_of(stream)
+            eng.load(prob, precision=prec)
+            for w in range(3):
+                eng.half_ls(10, 0, 0, 10, blk.vecs[w], DF)
+            k = 20
+            dt, _ = timer(k, lambda i: eng.half_ls(10, 0, 0, 10, blk.vecs[i % blk.nvec], DF))
+            per = dt / k
+            r = {"us_per_call": 1e6 * per, "calls": k,
+                 "note": "device time per call on the engine's stream (Y build, GEMM, stencil, "
+                         "copies of the vector and the result)"}
+            if name == "split":
+                r["digit_gb_per_s_whole_call"] = digit_bytes / per / 1e9
+            out[name] = r
+    out["speedup_split_over_fp64"] = out["fp64"]["us_per_call"] / out["split"]["us_per_call"]
+    return out
+
+
 def leg_streamed(pkg, eng, prob, timer, S, value_rate):
     """The headline batch with the dipole kept in host memory and streamed
     through the device in four panels per half-ls GEMM (copies overlap)."""
@@ -500,6 +595,36 @@ def leg_streamed(pkg, eng, prob, timer, S, value_rate):
 
 
 # ---------------------------------------------------------------- our arm
+def main_only(args):
+    """Selected legs alone (profiling runs): their JSON, no headline."""
+    import torch
+    pkg = G.load_package()
+    local = dist_env()[2]
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+
+    def timer_of(stream):
+        return Timer(torch, stream, lambda: None)
+
+    out = {}
+    for leg in args.only.split(","):
+        if leg == "halfls":
+            out[leg] = leg_half_ls(pkg, args, local, timer_of, peaks)
+        elif leg == "plain":
+            out[leg] = leg_c2v_plain(pkg, args, local, timer_of)
+        elif leg == "precision":
+            out[leg] = leg_c2v_precision(pkg, args, local, timer_of)
+        elif leg == "serving":
+            out[leg] = serving_leg(pkg, args, local, None)
+        else:
+            raise SystemExit(f"unknown leg {leg}")
+    print(json.dumps(out))
+    return 0
+
+
 def main_ours(args):
     import torch
     rank, world, local = dist_env()
@@ -594,11 +719,16 @@ def main_ours(args):
         parts = {"upload_ms": 0.0, "run_ms": 0.0}
         d2h = []
 
+        slowest = []
+
         def e2e_step(i):
             ta = time.perf_counter()
             eng.set_dipole(prob.N, prob.mu)
+            parts["dipole_ms"] = parts.get("dipole_ms", 0.0) + 1e3 * (time.perf_counter() - ta)
             for (J, g), b in sorted(prob.blocks.items()):
+                t = time.perf_counter()
                 eng.set_block(J, g, b.vecs, b.energies, b.quanta)
+                slowest.append((time.perf_counter() - t, b.vecs.nbytes, J, g))
             tb = time.perf_counter()
             n = eng.run(lines_on_device=False, graph=True, shard=i % S, nshards=S)
             parts["upload_ms"] += 1e3 * (tb - ta)
@@ -607,8 +737,9 @@ def main_ours(args):
             return eng.stats()["nlines_filtered"]
 
         e2e_step(0)
-        parts["upload_ms"] = parts["run_ms"] = 0.0
+        parts["upload_ms"] = parts["run_ms"] = parts["dipole_ms"] = 0.0
         d2h.clear()
+        slowest.clear()
         ne = args.e2e_steps
         te, n = timer(ne, e2e_step)
         unregister_host(torch, pinned)
@@ -616,6 +747,9 @@ def main_ours(args):
                "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": 1e3 * te / ne,
                "steps": ne, "host_pinned": bool(len(pinned) == len(arrays)),
                "host_wall_ms_per_step": {k: v / ne for k, v in parts.items()},
+               "upload_gb_per_s": h2d / (parts["upload_ms"] / ne * 1e-3),
+               "slowest_block_uploads": [{"s": round(t, 4), "bytes": int(nb), "J": J, "gamma": g}
+                                         for t, nb, J, g in sorted(slowest, reverse=True)[:4]],
                "note": "each step re-uploads the dipole and every block from page-locked host "
                        "memory, re-cuts the digit planes and reads the shard's lines back"}
 
@@ -640,6 +774,12 @@ def main_ours(args):
     if not args.no_legs and "streamed" in args.legs and world == 1:
         streamed = leg_streamed(pkg, eng, prob, timer, S, value_rate)
     eng.close()
+    # the serving pool reuses the headline's dipole and bases (blocks regenerated)
+    serve_base = None
+    if args.workload == "c3v_batched" and args.jmax is None:
+        from gpu_intensities_gb300 import synth as _synth
+        serve_base = _synth.Problem(prob.sym_type, prob.N, prob.mu, prob.bases, {}, prob.params,
+                                    name=prob.name)
     del prob
 
     legs = {}
@@ -649,7 +789,9 @@ def main_ours(args):
         if "precision" in args.legs and args.workload != "c2v_precision":
             legs["c2v_precision"] = leg_c2v_precision(pkg, args, local, timer_of)
         if "serving" in args.legs:
-            legs["serving"] = {"split": serve_bench(pkg, args, local, pkg.GI_PREC_SPLIT)}
+            legs["serving"] = serving_leg(pkg, args, local, serve_base)
+        if "halfls" in args.legs:
+            legs["half_ls_vector"] = leg_half_ls(pkg, args, local, timer_of, peaks)
     accuracy = None
     if not args.no_accuracy and world == 1 and args.workload in CPU_SAMPLE:
         accuracy = accuracy_vs_oracle(pkg, args, local, args.workload)
@@ -693,6 +835,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return main_reference(args)
+    if args.only:
+        return main_only(args)
     return main_ours(args)
 
 

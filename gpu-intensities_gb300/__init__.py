@@ -71,7 +71,7 @@ class gi_stats(C.Structure):
 
 
 class gi_serve_config(C.Structure):
-    _fields_ = [("slots", C.c_int32), ("reserved", C.c_int32),
+    _fields_ = [("slots", C.c_int32), ("flags", C.c_int32),
                 ("hbm_budget_bytes", C.c_size_t), ("slot_workspace_bytes", C.c_size_t)]
 
 
@@ -91,7 +91,9 @@ class gi_serve_stats(C.Structure):
                 ("queue_p50", C.c_double), ("queue_p99", C.c_double),
                 ("resident_bytes", C.c_size_t), ("peak_resident_bytes", C.c_size_t),
                 ("budget_bytes", C.c_size_t), ("slot_workspace_bytes", C.c_size_t),
-                ("slots", C.c_int32), ("reserved", C.c_int32)]
+                ("slots", C.c_int32), ("reserved", C.c_int32),
+                ("zcache_hits", C.c_int64), ("zcache_misses", C.c_int64),
+                ("zcache_evictions", C.c_int64), ("zcache_bytes", C.c_size_t)]
 
 
 GI_JOB_QUEUED, GI_JOB_RUNNING, GI_JOB_DONE, GI_JOB_FAILED = range(4)
@@ -525,8 +527,9 @@ class Engine:
         return q.value
 
     # serving ---------------------------------------------------------------
-    def serve_start(self, slots: int = 3, budget: int = 0, slot_workspace: int = 0):
-        cfg = gi_serve_config(slots, 0, budget, slot_workspace)
+    def serve_start(self, slots: int = 3, budget: int = 0, slot_workspace: int = 0,
+                    zcache: bool = True):
+        cfg = gi_serve_config(slots, 0 if zcache else 1, budget, slot_workspace)
         self._ck(self._L.gi_serve_start(self._h, C.byref(cfg)))
 
     def serve_stop(self):
@@ -552,6 +555,10 @@ class Engine:
         if release:
             self._ck(self._L.gi_job_release(self._h, job))
         return out
+
+    def release(self, job: int):
+        """Forget a finished job and its lines (gi_job_release)."""
+        self._ck(self._L.gi_job_release(self._h, job))
 
     def serve_stats(self) -> Dict[str, float]:
         s = gi_serve_stats()

@@ -130,6 +130,8 @@ struct Block {
   bool resident = true;
   double* h_vecs = nullptr;  // pinned [nvec][nsize] while evicted
   int pins = 0;              // running jobs that use the block
+  uint64_t uid = next_uid(); // identity and vector version (serving Z cache)
+  uint64_t version = 0;      // bumped whenever the vectors change
   uint64_t last_use = 0;     // serving clock of the last admission
   size_t device_bytes() const {
     return d_vecs.n * sizeof(double) + d_energies.n * sizeof(double) +
@@ -250,6 +252,8 @@ struct Ctx {
 
   // workspaces
   DevArray<double> hls_v, hls_y, hls_z, hls_h;  // gi_half_ls (grow-only)
+  double* hls_pin = nullptr;                     // its pinned host staging
+  size_t hls_pin_cap = 0;
   DevArray<int32_t> hls_iv;
   DevArray<double> w_y, w_z, w_h, w_t, w_EI;
   DevArray<unsigned long long> w_counter;
@@ -298,8 +302,23 @@ gi_status ensure_ycsr(Ctx* c, Basis& b);
 // (Basis::d_pair_st), from the context's 3j table where it covers the pair.
 gi_status refresh_pair_tables(Ctx* c, Basis* only = nullptr);
 // Serving: frees device memory for `bytes` more by evicting unpinned blocks
-// other than `keep` (least recently used first).  Caller holds model_mu.
+// other than `keep` and unused cached half line strengths (least recently
+// used first).  Caller holds model_mu.
 gi_status server_make_room(Ctx* c, size_t bytes, Block* keep);
+// Serving Z cache: the half line strength Z = mu^T Y ([3][ncol][Kp], the run's
+// layout) of an initial block for one selection of its vectors.  acquire
+// (worker context, model lock not held) returns z = null when nothing can be
+// cached; hit: z holds it, else the run writes it there.  release unpins it,
+// keeping it valid after a successful run or dropping it otherwise.
+struct ZEntry;
+struct ZRef {
+  ZEntry* e = nullptr;
+  double* z = nullptr;
+  bool hit = false;
+};
+gi_status zcache_acquire(Ctx* w, const Block* blk, const int32_t* ivec, int nI, size_t elems,
+                         ZRef* out);
+void zcache_release(Ctx* w, ZRef& r, bool ok);
 // Stops the serving loop of c (if any): fails queued jobs, joins the workers.
 gi_status server_stop(Ctx* c);
 void trove_meta_release(Ctx* c);

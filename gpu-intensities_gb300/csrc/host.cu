@@ -841,6 +841,39 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   double fl_half = 0.0, fl_final = 0.0, by_corr = 0.0;
   int64_t npairs_checked = 0;
 
+  // A serving pair job (one initial block, one unit per round): the half line
+  // strength Z of its initial block may come from (or go to) the server's Z
+  // cache, shared by every job with the same initial block and selection of
+  // its vectors.  The entry holds the block's whole Z ([3][columns][Kp]); round
+  // r reads and writes its columns from zoff[r] on.
+  ZRef zref;
+  std::vector<size_t> zoff(rounds.size(), 0);
+  size_t ztotal = 0;
+  if (c->job.on && c->parent && !c->streamed()) {
+    bool one = true;
+    std::vector<int32_t> ids;
+    const Block* zblk = nullptr;
+    for (size_t r = 0; r < rounds.size() && one; r++) {
+      if (rounds[r].units.empty()) continue;
+      const Unit& u = rounds[r].units[0];
+      one = rounds[r].units.size() == 1 && (!zblk || zblk == u.I->blk);
+      zblk = u.I->blk;
+      zoff[r] = ztotal;
+      ztotal += u.ncolY;
+      ids.insert(ids.end(), h_ivec.begin() + 2 * u.off, h_ivec.begin() + 2 * u.off + u.nI);
+    }
+    if (one && zblk && ztotal) {
+      gi_status s = zcache_acquire(c, zblk, ids.data(), (int)ids.size(), 3 * ztotal * Kp, &zref);
+      if (s != GI_OK) return s;
+    }
+  }
+  struct ZRelease {
+    Ctx* c;
+    ZRef* r;
+    bool ok = false;
+    ~ZRelease() { zcache_release(c, *r, ok); }
+  } zrelease{c, &zref};
+
   // the launch sequence of the job, issued eagerly or under stream capture
   bool capturing = false;
   auto issue = [&]() -> gi_status {
@@ -848,8 +881,11 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   for (size_t r = 0; r < rounds.size(); r++) {
     const Round& R = rounds[r];
     if (R.units.empty()) continue;
-    const size_t zc = R.ncolY * Kp;  // stride between dipole components in Z
+    // Z of this round: the workspace, or its columns of the cache entry
+    double* zbase = zref.z ? zref.z + zoff[r] * Kp : c->w_z.p;
+    const size_t zc = (zref.z ? ztotal : R.ncolY) * Kp;  // stride between dipole components
     for (const Unit& u : R.units) {
+      if (zref.hit) break;  // Z of this round is in the cache
       const Basis& bI = *c->bases[u.I->blk->J];
       const int ndegI = c->degen[u.I->blk->gamma];
       if (fused_y) {  // straight into the digit planes of the half-ls GEMM's B operand
@@ -867,15 +903,17 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       }
       by_corr += 8.0 * ((double)u.nI * u.I->blk->nsize + (double)u.ncolY * Kp);
     }
-    if (P.precision == GI_PREC_SPLIT) {
-      gi_status s =
-          split_gemm_dipole(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY, fused_y);
+    if (zref.hit) {
+      // computed by an earlier job
+    } else if (P.precision == GI_PREC_SPLIT) {
+      gi_status s = split_gemm_dipole(c, c->w_y.p, Kp, zbase, Kp, zc, (int)R.ncolY, fused_y);
       if (s != GI_OK) return s;
+      fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
     } else {
-      gi_status s = dipole_gemm_fp64(c, c->w_y.p, Kp, c->w_z.p, Kp, zc, (int)R.ncolY, c->stream);
+      gi_status s = dipole_gemm_fp64(c, c->w_y.p, Kp, zbase, Kp, zc, (int)R.ncolY, c->stream);
       if (s != GI_OK) return s;
+      fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
     }
-    fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
 
     for (const auto& grp : groups[r]) {
       // H of every final block of the group
@@ -891,7 +929,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
           const int ndegI = c->degen[u.I->blk->gamma];
           const int nslot = c->bases[u.I->blk->J]->nslot;
           GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
-                    return launch_build_h(c->w_z.p + u.ycol * Kp, zc, Kp, nslot, ndegI, u.nI, bF,
+                    return launch_build_h(zbase + u.ycol * Kp, zc, Kp, nslot, ndegI, u.nI, bF,
                                           fb.gamma, ndegF, fb.nsize, ldh,
                                           c->w_stencil.p + pp->st_off * 6,
                                           c->w_stencil_n.p + pp->st_off, 6,
@@ -1119,6 +1157,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   c->stats.seconds_total =
       std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
   *nlines_out = c->nlines;
+  zrelease.ok = true;  // a Z this run filled is valid for later jobs
   return GI_OK;
 }
 
@@ -1126,6 +1165,7 @@ void ctx_release(Ctx* c) {
   cudaStreamSynchronize(c->stream);
   split_release(c);
   if (c->h_lines) cudaFreeHost(c->h_lines);
+  if (c->hls_pin) cudaFreeHost(c->hls_pin);
   if (c->d2h) {
     cudaStreamSynchronize(c->d2h);
     cudaStreamDestroy(c->d2h);
@@ -1366,6 +1406,7 @@ static gi_status set_block(Ctx* c, int J, int gamma, int nsize, int nvec, const 
   // allocation at the next run; freeing it would synchronise the device and
   // move the addresses a captured graph reads)
   b->digits_s = 0;
+  b->version++;
   b->energies.assign(energies, energies + nvec);
   const int nq = c->params.nmodes + 1;
   b->quanta.assign(quanta, quanta + (size_t)nvec * nq);
@@ -1545,8 +1586,18 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
   GI_CUDA(c, c->hls_h.reserve(bF.D));
   GI_CUDA(c, cudaMemsetAsync(c->hls_v.p, 0, sizeof(double) * ld, c->stream));
   GI_CUDA(c, cudaMemsetAsync(c->hls_iv.p, 0, sizeof(int32_t), c->stream));
-  GI_CUDA(c, cudaMemcpyAsync(c->hls_v.p, vsym, sizeof(double) * nsize, cudaMemcpyHostToDevice,
-                             c->stream));
+  // the vector and the result pass through pinned staging of the context
+  const size_t stage = std::max<size_t>(nsize, bF.D);
+  if (c->hls_pin_cap < stage) {
+    if (c->hls_pin) cudaFreeHost(c->hls_pin);
+    c->hls_pin = nullptr;
+    c->hls_pin_cap = 0;
+    GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->hls_pin), sizeof(double) * stage));
+    c->hls_pin_cap = stage;
+  }
+  std::memcpy(c->hls_pin, vsym, sizeof(double) * nsize);
+  GI_CUDA(c, cudaMemcpyAsync(c->hls_v.p, c->hls_pin, sizeof(double) * nsize,
+                             cudaMemcpyHostToDevice, c->stream));
   double* y = c->hls_y.p;
   double* hh = c->hls_h.p;
   GI_CUDA(c, launch_build_y(c->hls_v.p, ld, c->hls_iv.p, 1, ndeg, bI, gammaI, ndeg, c->N, c->Kp,
@@ -1574,9 +1625,10 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
     GI_CUDA(c, launch_half_ls_prim(c->hls_z.p + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF,
                                    dst, dstn, 6, hh, c->stream));
   }
-  GI_CUDA(c, cudaMemcpyAsync(half_ls, hh, sizeof(double) * bF.D, cudaMemcpyDeviceToHost,
+  GI_CUDA(c, cudaMemcpyAsync(c->hls_pin, hh, sizeof(double) * bF.D, cudaMemcpyDeviceToHost,
                              c->stream));
   GI_CUDA(c, cudaStreamSynchronize(c->stream));
+  std::memcpy(half_ls, c->hls_pin, sizeof(double) * bF.D);
   if (c->have_params && c->params.precision == GI_PREC_SPLIT) {
     s = split_check(c);
     if (s != GI_OK) return s;

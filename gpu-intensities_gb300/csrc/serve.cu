@@ -18,6 +18,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <thread>
 #include <unordered_map>
 
@@ -48,6 +49,18 @@ struct JobRec {
   double t_submit = 0, t_admit = 0, t_done = 0, seconds_gpu = 0;
 };
 
+// A cached half line strength (see zcache_acquire in engine.h).
+struct ZEntry {
+  uint64_t blk_uid = 0, blk_version = 0;
+  int precision = 0, slices = 0;
+  std::vector<int32_t> ivec;  // the initial records its columns hold
+  DevArray<double> z;
+  bool valid = false;         // written by a finished run
+  int pins = 0;
+  uint64_t last_use = 0;
+  size_t bytes() const { return z.n * sizeof(double); }
+};
+
 struct Server {
   Ctx* owner = nullptr;
   int nslots = 0;
@@ -66,6 +79,11 @@ struct Server {
   int64_t submitted = 0, completed = 0, failed = 0, lines = 0, lines_filtered = 0;
   int64_t evictions = 0, restores = 0;
   size_t peak_resident = 0;
+  // cached half line strengths of initial blocks, shared by the jobs that
+  // start from the same block (the same selection of its vectors)
+  std::vector<std::unique_ptr<ZEntry>> zcache;
+  bool zcache_on = true;
+  int64_t z_hits = 0, z_misses = 0, z_evictions = 0;
 };
 
 // ------------------------------------------------------------------ residency
@@ -73,6 +91,8 @@ static size_t resident_bytes(Ctx* c) {
   size_t b = 0;
   for (auto& kv : c->blocks)
     if (kv.second->resident) b += kv.second->device_bytes();
+  if (c->server)
+    for (auto& e : c->server->zcache) b += e->bytes();
   return b;
 }
 
@@ -135,20 +155,109 @@ gi_status server_make_room(Ctx* c, size_t bytes, Block* keep) {
   const size_t cap = block_budget(s);
   size_t used = resident_bytes(c);
   while (used + bytes > cap) {
+    // the least recently used of the unpinned blocks and cached Z; a cached Z
+    // is dropped (recomputed when a job needs it), a block moves to host
     Block* victim = nullptr;
     for (auto& kv : c->blocks) {
       Block* b = kv.second.get();
       if (!b->resident || b->pins > 0 || b == keep || b->device_bytes() == 0) continue;
       if (!victim || b->last_use < victim->last_use) victim = b;
     }
-    if (!victim)
+    size_t zv = s->zcache.size();
+    for (size_t k = 0; k < s->zcache.size(); k++) {
+      const ZEntry& e = *s->zcache[k];
+      if (e.pins > 0) continue;
+      if (zv == s->zcache.size() || e.last_use < s->zcache[zv]->last_use) zv = k;
+    }
+    // cached Z go before blocks: a Z is recomputed on the GPU, a block comes
+    // back over the host link and has its digit planes cut again
+    if (zv < s->zcache.size()) {
+      s->zcache.erase(s->zcache.begin() + zv);
+      s->z_evictions++;
+    } else if (victim) {
+      gi_status st = evict(c, *victim);
+      if (st != GI_OK) return st;
+    } else {
       return fail(c, GI_ERR_BUDGET, "serving budget: %zu bytes more do not fit (%zu of %zu used)",
                   bytes, used, cap);
-    gi_status st = evict(c, *victim);
-    if (st != GI_OK) return st;
+    }
     used = resident_bytes(c);
   }
   return GI_OK;
+}
+
+// ------------------------------------------------------------------ Z cache
+gi_status zcache_acquire(Ctx* w, const Block* blk, const int32_t* ivec, int nI, size_t elems,
+                         ZRef* out) {
+  *out = ZRef{};
+  Ctx* c = w->parent;
+  Server* s = c ? c->server : nullptr;
+  if (!s || !s->zcache_on || nI <= 0) return GI_OK;
+  std::lock_guard<std::mutex> lk(c->model_mu);
+  const int prec = w->params.precision, sl = w->params.split_slices;
+  for (auto& ep : s->zcache) {
+    ZEntry& e = *ep;
+    if (e.blk_uid != blk->uid || e.blk_version != blk->version || e.precision != prec ||
+        e.slices != sl || (int)e.ivec.size() != nI ||
+        !std::equal(e.ivec.begin(), e.ivec.end(), ivec))
+      continue;
+    if (!e.valid) {  // another job is filling it: compute without the cache
+      s->z_misses++;
+      return GI_OK;
+    }
+    e.pins++;
+    e.last_use = ++s->clock;
+    s->z_hits++;
+    *out = ZRef{&e, e.z.p, true};
+    return GI_OK;
+  }
+  // a new entry, if it fits the budget beside everything the running jobs hold
+  // and takes at most a quarter of it (one large entry would push out many
+  // small ones that are asked for more often)
+  s->z_misses++;
+  const size_t bytes = elems * sizeof(double);
+  if (bytes > block_budget(s) / 4) return GI_OK;
+  if (server_make_room(c, bytes, nullptr) != GI_OK) {
+    c->err.clear();
+    return GI_OK;
+  }
+  auto e = std::make_unique<ZEntry>();
+  e->blk_uid = blk->uid;
+  e->blk_version = blk->version;
+  e->precision = prec;
+  e->slices = sl;
+  e->ivec.assign(ivec, ivec + nI);
+  if (e->z.alloc(elems) != cudaSuccess) {
+    cudaGetLastError();
+    return GI_OK;
+  }
+  e->pins = 1;
+  e->last_use = ++s->clock;
+  *out = ZRef{e.get(), e->z.p, false};
+  s->zcache.push_back(std::move(e));
+  s->peak_resident = std::max(s->peak_resident, resident_bytes(c));
+  return GI_OK;
+}
+
+void zcache_release(Ctx* w, ZRef& r, bool ok) {
+  if (!r.e) return;
+  Ctx* c = w->parent;
+  Server* s = c->server;
+  std::lock_guard<std::mutex> lk(c->model_mu);
+  for (size_t k = 0; k < s->zcache.size(); k++) {
+    if (s->zcache[k].get() != r.e) continue;
+    ZEntry& e = *s->zcache[k];
+    e.pins--;
+    if (!r.hit) {
+      if (ok) {
+        e.valid = true;
+      } else if (e.pins == 0) {
+        s->zcache.erase(s->zcache.begin() + k);
+      }
+    }
+    break;
+  }
+  r = ZRef{};
 }
 
 // ------------------------------------------------------------------ workers
@@ -356,6 +465,7 @@ gi_status gi_serve_start(gi_ctx* h, const gi_serve_config* cfg) {
   s->slot_ws = slot_ws;
   s->precision = c->params.precision;
   s->slices = c->params.split_slices;
+  s->zcache_on = !(cf.flags & GI_SERVE_NO_ZCACHE);
   for (int i = 0; i < slots; i++) {
     Ctx* w = make_worker(c, slot_ws);
     if (!w) {
@@ -517,6 +627,10 @@ gi_status gi_serve_get_stats(gi_ctx* h, gi_serve_stats* out) {
   r.budget_bytes = s->budget;
   r.slot_workspace_bytes = s->slot_ws;
   r.slots = s->nslots;
+  r.zcache_hits = s->z_hits;
+  r.zcache_misses = s->z_misses;
+  r.zcache_evictions = s->z_evictions;
+  for (auto& e : s->zcache) r.zcache_bytes += e->bytes();
   *out = r;
   return GI_OK;
 }
@@ -531,6 +645,7 @@ gi_status gi_serve_reset_stats(gi_ctx* h) {
   s->queued.clear();
   s->submitted = s->completed = s->failed = s->lines = s->lines_filtered = 0;
   s->evictions = s->restores = 0;
+  s->z_hits = s->z_misses = s->z_evictions = 0;
   s->peak_resident = resident_bytes(c);
   return GI_OK;
 }

@@ -598,7 +598,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
                    const __grid_constant__ CUtensorMap tmBq, const __grid_constant__ CUtensorMap tmBt,
                    const int32_t* __restrict__ ea, const int32_t* __restrict__ eb, double* C,
                    int ldc, size_t strideC, int M, int Mpad, int Nc, int K, int w, int nM, int nA,
-                   int nN, int GA, int* err) {
+                   int nN, int GA, int* err, int kpart_steps, size_t strideP) {
   constexpr int NQ = S / 4, NT = S % 4;
   constexpr int NPASS = D1 < S ? 2 : 1;
   constexpr int HALF = BN / 2;                     // columns per epilogue warp
@@ -631,8 +631,11 @@ __global__ void __launch_bounds__(kThreadsG, 1)
   const int gsz = min(GA, nA - grp * GA);
   const int ai = grp * GA + r % gsz;
   const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
-  const int nk = K / kBK;
-  const int nk0 = nk / PK;  // ring slots of pass 0 (K is a multiple of 64)
+  // K parts (grid y): part p contracts K steps [p * kpart_steps, ...) into its
+  // own output C + p * strideP (kpart_steps = 0: one part, the whole K)
+  const int kb0 = (int)blockIdx.y * kpart_steps;
+  const int nk = kpart_steps ? min(kpart_steps, K / kBK - kb0) : K / kBK;
+  const int nk0 = nk / PK;  // ring slots of pass 0 (K parts are multiples of 64)
   const int nslots = nk0 + (NPASS == 2 ? nk : 0);
 
   if (threadIdx.x == 0) {
@@ -667,13 +670,13 @@ __global__ void __launch_bounds__(kThreadsG, 1)
         if (pass == 0 && PK == 2) {
           mbar_expect_tx(&full[st], 2 * (kAq + kBq));
           for (int h = 0; h < 2; ++h) {
-            const int kb = 2 * it + h;
+            const int kb = kb0 + 2 * it + h;
             unsigned char* sh = sa + h * (kAq + kBq);
             tma_load_3d(sh, &tmAq, &full[st], kb * 64, z * Mpad + m0, 0);
             tma_load_3d(sh + kAq, &tmBq, &full[st], kb * 64, n0, 0);
           }
         } else {
-          const int kb = pass ? it - nk0 : it;
+          const int kb = kb0 + (pass ? it - nk0 : it);
           const int np = pass ? S : D1;
           const int gq = min(NQ, (np + 3) / 4), tq = max(0, np - 4 * NQ);
           unsigned char* sb = sa + kAbytes;
@@ -770,7 +773,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
     const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int m = m0 + q4 * 32 + lane;
     const int emr = (m < M) ? ea[z * Mpad + m] : 0;
-    double* Cz = C + (size_t)z * strideC;
+    double* Cz = C + (size_t)z * strideC + (size_t)blockIdx.y * strideP;
     const uint32_t lanes = (uint32_t)(q4 * 32) << 16;
     long long v0[NCH][kChunkG];  // pass 0's exact sums of this thread's columns
     bool ok = true;
@@ -1533,11 +1536,14 @@ cudaError_t kernel_attributes(int s) {
   return cudaErrorInvalidValue;
 }
 
+// kparts > 1 (grouped kernels only): K in parts of kpart_steps 16-wide steps,
+// part p writing its own product to C + p * strideP (grid y).
 template <int S>
 cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea,
                         const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
                         int Nc, int K, int batch, int w, int accum, int* err,
-                        cudaStream_t st) {
+                        cudaStream_t st, int kparts = 1, int kpart_steps = 0,
+                        size_t strideP = 0) {
   const CUtensorMap& tA = mp.a;
   const CUtensorMap& tB = mp.b;
   const bool one = cfg.kind == 0 || cfg.kind == 8;
@@ -1553,22 +1559,24 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
   const int GA = std::max(1, std::min(nA, (int)(((size_t)cfg.ga_mb << 20) / a_tile)));
   if constexpr (S >= 4) {
     if (cfg.kind >= 6 && cfg.kind <= 8) {
-      const int grid = nA * nN;
+      const dim3 grid((unsigned)(nA * nN), (unsigned)std::max(kparts, 1));
+      if (kparts <= 1) kpart_steps = 0;
       if (cfg.kind == 8)
         (accum ? k_split_gemm_g<S, BN1, S, true> : k_split_gemm_g<S, BN1, S, false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
-            err);
+            err, kpart_steps, strideP);
       else if (cfg.kind == 7 && d1b_of(S) != D1)
         (accum ? k_split_gemm_g<S, BN2, d1b_of(S), true> : k_split_gemm_g<S, BN2, d1b_of(S), false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
-            err);
+            err, kpart_steps, strideP);
       else
         (accum ? k_split_gemm_g<S, BN2, D1, true> : k_split_gemm_g<S, BN2, D1, false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
-            err);
+            err, kpart_steps, strideP);
       return cudaGetLastError();
     }
   }
+  if (kparts > 1) return cudaErrorInvalidValue;  // the plain-layout kernels take whole K
   if (one)
     k_split_gemm<S, BN1><<<nA * nN, kThreads, sm, st>>>(
         tA, tB, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA, accum, err);
@@ -1584,12 +1592,13 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
 cudaError_t launch_gemm_s(int s, const GemmConfig& cfg, const Maps& mp, const int32_t* ea,
                           const int32_t* eb, double* C, int ldc, size_t strideC, int M, int Mpad,
                           int Nc, int K, int batch, int w, int accum, int* err,
-                        cudaStream_t st) {
+                          cudaStream_t st, int kparts = 1, int kpart_steps = 0,
+                          size_t strideP = 0) {
   switch (s) {
 #define GI_S(SS)                                                                                \
   case SS:                                                                                      \
     return launch_gemm<SS>(cfg, mp, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, batch, w, accum, err, \
-                            st);
+                            st, kparts, kpart_steps, strideP);
     GI_S(2) GI_S(3) GI_S(4) GI_S(5) GI_S(6) GI_S(7) GI_S(8) GI_S(9) GI_S(10)
 #undef GI_S
   }
@@ -2111,9 +2120,10 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
 // fewer than one 96-wide tile.  The dipole digits are the data that moves
 // (3 x Mpad x Kp x s bf16), so the GEMM is as fast as one pass over them:
 // the row tiles alone are too few CTAs to draw full HBM bandwidth, so K is
-// split into parts, each a problem of one persistent launch (one CTA per SM)
-// writing its own partial product Zp[part][col][3 * Mpad]; the caller sums the
-// parts.  Streamed dipoles and digit shapes other than the default grouped
+// split into parts (the grid's y dimension of one launch of the one-pass
+// kernel: 48-wide tiles, every diagonal in tensor memory, the dipole digits
+// read once), each writing its own partial product Zp[part][col][3 * Mpad];
+// the caller sums the parts.  Streamed dipoles and digit shapes other than the default grouped
 // s = 9 go through the regular GEMM as one part.
 gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, double* Zp,
                                    size_t part_stride, int max_parts, int* nparts, int* ldz) {
@@ -2137,11 +2147,11 @@ gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, d
             "slice Y");
   if (g != GI_OK) return g;
   c->stats.flops_tensor += (double)S->s * (S->s + 1) / 2 * 2.0 * c->N * (double)ncol * c->N * 3;
-  constexpr int SS = 9, BN = bn2_of(SS), D1 = d1_of(SS);
+  constexpr int SS = 9, BN = bn_for(SS);  // the one-pass tile width
   const int nM = rows / kBM, nN = (ncol + BN - 1) / BN;
-  // parts: enough to give every SM a tile; each a multiple of 64 in K (whole
-  // pairs of the two-slice ring stages) and at most one exact segment long
-  const int kq = K / 64, pmax = std::min(max_parts, kGpMaxProb);
+  // parts: enough to give every SM a tile; each a multiple of 64 in K and at
+  // most one exact segment long (a launch does not segment K)
+  const int kq = K / 64, pmax = std::max(1, max_parts);
   int parts = std::max(1, std::min({std::max(c->nsm, 1) / (nM * nN), pmax, kq}));
   while (parts < pmax && (kq + parts - 1) / parts * 64 > kKSeg) parts++;
   const int per = (kq + parts - 1) / parts * 64;
@@ -2157,49 +2167,25 @@ gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, d
     return r;
   }
   *nparts = parts;
-  GpParams* P = new GpParams();
-  P->nprob = parts;
-  P->nitems = 0;
+  // one launch of the one-pass grouped kernel (48-wide tiles, all nine
+  // diagonals in tensor memory, so the dipole digits stream through once),
+  // the K parts on the grid's y dimension
   const int nq = SS / 4, nt = SS % 4;
-  for (int q = 0; q < parts && g == GI_OK; ++q) {
-    const int k0 = q * per, Kc = std::min(per, K - k0);
-    GpProb& pr = P->p[q];
-    if (Kc <= 0 ||
-        !make_map_groups(&pr.aq, D->mu_slices.p + (size_t)4 * k0, Kc, rows, nq, kBM, K) ||
-        !make_map(&pr.at, D->mu_slices.p + (size_t)4 * nq * rows * K + k0, Kc, rows, nt, kBM, 1,
-                  K) ||
-        !make_map_groups(&pr.bq, S->b_slices.p + (size_t)4 * k0, Kc, ncol, nq, BN, K) ||
-        !make_map(&pr.bt, S->b_slices.p + (size_t)4 * nq * ncol * K + k0, Kc, ncol, nt, BN, 1,
-                  K)) {
-      g = check(c, cudaErrorInvalidValue, "narrow dipole GEMM tensor maps");
-      break;
-    }
-    pr.ea = D->mu_exp.p;
-    pr.eb = S->b_exp.p;
-    pr.C = Zp + (size_t)q * part_stride;
-    pr.ldc = rows;
-    pr.M = rows;
-    pr.Mpad = rows;
-    pr.Nc = ncol;
-    pr.K = Kc;
-    pr.nM = nM;
-    pr.nN = nN;
-    pr.first = P->nitems;
-    P->nitems += nM * nN;
-  }
-  if (g == GI_OK) g = check(c, kernel_attributes(SS), "kernel attributes");
-  if (g == GI_OK) {
-    const int grid = std::min(P->nitems, std::max(c->nsm, 1));
-    const size_t sm = smemg_bytes(SS, BN);
-    g = check(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
-                k_split_gemm_gp<SS, BN, D1><<<grid, kThreadsG, sm, c->stream>>>(*P, S->w,
-                                                                               S->err.p);
-                return cudaGetLastError();
-              }),
-              "narrow dipole GEMM launch");
-  }
-  delete P;
-  return g;
+  GemmConfig cfg;
+  cfg.kind = 8;
+  cfg.ga_mb = 64;
+  Maps mp;
+  if (!make_map_groups(&mp.a, D->mu_slices.p, K, rows, nq, kBM, K) ||
+      !make_map(&mp.at, D->mu_slices.p + (size_t)4 * nq * rows * K, K, rows, nt, kBM, 1, K) ||
+      !make_map_groups(&mp.b, S->b_slices.p, K, ncol, nq, BN, K) ||
+      !make_map(&mp.bt, S->b_slices.p + (size_t)4 * nq * ncol * K, K, ncol, nt, BN, 1, K))
+    return check(c, cudaErrorInvalidValue, "narrow dipole GEMM tensor maps");
+  return check(c, timed(c, GI_PHASE_HALFLS_GEMM, [&] {
+                 return launch_gemm_s(SS, cfg, mp, D->mu_exp.p, S->b_exp.p, Zp, rows, 0, rows,
+                                      rows, ncol, K, 1, S->w, 0, S->err.p, c->stream, parts,
+                                      per / kBK, part_stride);
+               }),
+               "narrow dipole GEMM launch");
 }
 
 bool split_fused_y(const Ctx* c) { return split_grouped_final(c) && c->Kp <= kFusedYMaxKp; }

@@ -12,6 +12,9 @@ seed with the shapes, sizes and value distributions of the named workloads:
                   dipole magnitudes log-uniform 1e-8..1
 * ``c3v_batched`` tetratomic C3v (A1, A2, E), Nvib=3000, J=0..40 (blocks up
                   to ~60k), <=1500 vectors under 12000 cm^-1, T=500 K
+* serving     ``serving_pool`` / ``serving_jobs``: the c3v_batched bases with
+                  100..2000 vectors per block (log-uniform), pair jobs with
+                  initial block sizes log-uniform in 500..80k, Poisson arrivals
 
 The contracted basis is the product form TROVE produces for a rigid-rotor
 factor: for each J the "cases" are (k, vibrational function) with
@@ -338,13 +341,13 @@ def make_c3v_basis(J: int, vib_kind: List[int], rng: np.random.Generator) -> Bas
 # ---------------------------------------------------------------- blocks
 def make_block(rng: np.random.Generator, J: int, g: int, nsize: int, nmodes: int,
                nvec_max: Optional[int] = None, ecut: Optional[float] = None,
-               emax: float = 20000.0) -> Block:
+               emax: float = 20000.0, qr_limit: int = 20_000_000) -> Block:
     e = np.sort(rng.uniform(0.0, emax, size=nsize))
     if ecut is not None:
         e = e[e < ecut]
     nvec = len(e) if nvec_max is None else min(nvec_max, len(e))
     e = e[:nvec].copy()
-    if nvec > 0 and nsize * nvec <= 20_000_000:
+    if nvec > 0 and nsize * nvec <= qr_limit:
         q, r = np.linalg.qr(rng.standard_normal((nsize, nvec)))
         vecs = np.ascontiguousarray((q * np.sign(np.diag(r))[None, :]).T)
     elif nvec > 0:
@@ -463,6 +466,51 @@ def workload(name: str, seed: int = 1, **kw) -> Problem:
                         nvec_max=kw.pop("nvec_max", 1500), ecut=kw.pop("ecut", 12000.0),
                         name=name, **kw)
     raise KeyError(name)
+
+
+# ---------------------------------------------------------------- serving
+def serving_pool(prob: Problem, seed: int = 5, nvec_range: Tuple[float, float] = (100.0, 2000.0),
+                 ecut: float = 12000.0) -> Problem:
+    """The block pool of the serving workload: every (J, Gamma) block of a
+    batched C3v problem's bases (the same dipole, bases and parameters), each
+    with its own vector count drawn log-uniform in nvec_range (at most the
+    levels under ecut), as unit Gaussian vectors."""
+    rng = np.random.default_rng(seed)
+    blocks = {}
+    lo, hi = np.log(nvec_range[0]), np.log(nvec_range[1])
+    for J in sorted(prob.bases):
+        b = prob.bases[J]
+        for g in range(len(b.Ntotal)):
+            nmax = int(round(np.exp(rng.uniform(lo, hi))))
+            blocks[(J, g)] = make_block(rng, J, g, int(b.Ntotal[g]), prob.params.nmodes, nmax,
+                                        ecut, emax=ecut * 4 / 3, qr_limit=0)
+    return Problem(prob.sym_type, prob.N, prob.mu, prob.bases, blocks, prob.params,
+                   name=prob.name + "_serving_pool")
+
+
+def serving_jobs(pool: Problem, seed: int = 6, njobs: int = 10000, rate: float = 200.0,
+                 dims: Tuple[float, float] = (500.0, 80000.0)):
+    """Pair jobs (J, Gamma) -> (J', Gamma') of the serving workload: the
+    initial block's dimension drawn log-uniform in `dims` (the pool block of
+    the nearest size), Gamma' its selection partner, J' uniform among the J-1,
+    J, J+1 that carry lines; and Poisson inter-arrival gaps at `rate` jobs/s."""
+    rng = np.random.default_rng(seed)
+    keys = sorted(k for k, b in pool.blocks.items() if b.nvec > 0)
+    logsz = np.log(np.array([pool.blocks[k].nsize for k in keys], dtype=np.float64))
+    jmin = min(pool.jlist)
+    jobs = []
+    while len(jobs) < njobs:
+        d = rng.uniform(np.log(dims[0]), np.log(dims[1]))
+        J, g = keys[int(np.argmin(np.abs(logsz - d)))]
+        gF = pool.partner(g)
+        cands = [jF for jF in (J - 1, J, J + 1)
+                 if (jF, gF) in pool.blocks and pool.blocks[(jF, gF)].nvec > 0 and J + jF >= 1
+                 and not (J == jmin and jF == jmin)]
+        if not cands:
+            continue
+        jobs.append((J, g, int(cands[rng.integers(len(cands))]), gF))
+    gaps = rng.exponential(1.0 / rate, size=njobs)
+    return jobs, gaps
 
 
 # ---------------------------------------------------------------- persistence

@@ -381,12 +381,19 @@ gi_status gi_partition_function(gi_ctx* ctx, double temperature, double* q);
  * host memory when room is needed.  A job's lines are the lines of that block
  * pair that gi_run over all loaded blocks produces (same filters, ZPE and J
  * range), with level_i / level_f holding record indices within the two blocks.
+ * The half line strength of an initial block (its Z = mu^T Y, the GEMM most of
+ * a job's work goes to) is kept in a cache under the same budget and shared by
+ * later jobs that start from the same block with the same selection of its
+ * vectors (until the block's vectors change); cached entries and blocks are
+ * evicted together, least recently used first (GI_SERVE_NO_ZCACHE turns the
+ * cache off).
  * While serving, gi_set_block / gi_set_block_device / gi_set_params (except
  * precision and split_slices) / gi_submit and the job calls may be used from
  * the context's thread; the other setters and gi_run return GI_ERR_STATE. */
+#define GI_SERVE_NO_ZCACHE 1 /* do not keep initial blocks' half line strengths */
 typedef struct {
   int32_t slots;                /* jobs in flight, one stream each (0: 3) */
-  int32_t reserved;
+  int32_t flags;                /* GI_SERVE_* */
   size_t hbm_budget_bytes;      /* device bytes for resident blocks and slot
                                    workspaces (0: the context's budget, else
                                    80 % of the free memory) */
@@ -418,6 +425,10 @@ typedef struct {
   size_t resident_bytes, peak_resident_bytes, budget_bytes, slot_workspace_bytes;
   int32_t slots;
   int32_t reserved;
+  /* the Z cache: jobs whose initial block's half line strength was cached
+     (hits) or computed (misses), entries dropped for room, bytes held */
+  int64_t zcache_hits, zcache_misses, zcache_evictions;
+  size_t zcache_bytes;
 } gi_serve_stats;
 
 gi_status gi_serve_start(gi_ctx* ctx, const gi_serve_config* cfg);

@@ -38,10 +38,11 @@ def as_dict(arr):
     return {tuple(int(r[k]) for k in KEY): (r["S"], r["A"], r["I"], r["nu"]) for r in arr}
 
 
-def serve_all(pkg, prob, jobs, precision, slots=3, budget=0, slot_ws=0, order=None):
+def serve_all(pkg, prob, jobs, precision, slots=3, budget=0, slot_ws=0, order=None,
+              zcache=True):
     with pkg.Engine(0) as eng:
         eng.load(prob, precision=precision)
-        eng.serve_start(slots=slots, budget=budget, slot_workspace=slot_ws)
+        eng.serve_start(slots=slots, budget=budget, slot_workspace=slot_ws, zcache=zcache)
         ids = [eng.submit(*j) for j in (order or jobs)]
         res = {}
         for j, i in zip(order or jobs, ids):
@@ -97,13 +98,14 @@ def test_same_alone_and_in_the_mix(pkg, synth):
 def test_eviction_to_host_keeps_results(pkg, synth):
     prob = synth.make_c2v(23, 48, [0, 1, 2, 3, 4], nvec_max=40)
     jobs = pair_jobs(prob)
-    big, st_big = serve_all(pkg, prob, jobs, 1, slots=2)
+    big, st_big = serve_all(pkg, prob, jobs, 1, slots=2, zcache=False)
     assert st_big["evictions"] == 0
     blk = max(b.vecs.nbytes for b in prob.blocks.values())
     slot_ws = 8 << 20
     # room for the slot workspaces and a few blocks (with their digit planes)
     budget = 2 * slot_ws + 40 * blk
-    small, st = serve_all(pkg, prob, jobs, 1, slots=2, budget=budget, slot_ws=slot_ws)
+    small, st = serve_all(pkg, prob, jobs, 1, slots=2, budget=budget, slot_ws=slot_ws,
+                          zcache=False)
     assert st["evictions"] > 0 and st["restores"] > 0
     assert st["peak_resident_bytes"] <= budget - 2 * slot_ws
     for j in jobs:
@@ -121,3 +123,30 @@ def test_job_larger_than_budget_fails_cleanly(pkg, synth):
         assert info["state"] == pkg.GI_JOB_FAILED
         assert info["status"] == pkg.GI_ERR_BUDGET
         eng.serve_stop()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_zcache_shares_initial_blocks(pkg, synth, precision):
+    """Jobs that start from the same initial block reuse its cached half line
+    strength: the lines are bit for bit those of jobs that compute it, with a
+    cache large enough for every block and with one so small that entries are
+    evicted and recomputed."""
+    prob = synth.make_c3v(25, 36, [0, 1, 2, 3], nvec_max=12)
+    jobs = [j for j in pair_jobs(prob) if j[3] == prob.partner(j[1])]
+    plain, st0 = serve_all(pkg, prob, jobs, precision, slots=3, zcache=False)
+    cached, st = serve_all(pkg, prob, jobs, precision, slots=3)
+    assert st0["zcache_hits"] == 0
+    assert st["zcache_hits"] > 0 and st["zcache_misses"] > 0
+    assert st["zcache_hits"] + st["zcache_misses"] <= len(jobs)
+    for j in jobs:
+        assert np.array_equal(np.sort(cached[j], order=["level_i", "level_f"]),
+                              np.sort(plain[j], order=["level_i", "level_f"]))
+    slot_ws = 8 << 20
+    # room for the slot workspaces and a few final blocks with their digit
+    # planes and cached Z: entries and blocks take turns
+    tight, st2 = serve_all(pkg, prob, jobs, precision, slots=2, budget=2 * slot_ws + (1 << 20),
+                           slot_ws=slot_ws)
+    assert st2["zcache_evictions"] > 0 or st2["evictions"] > 0
+    for j in jobs:
+        assert np.array_equal(np.sort(tight[j], order=["level_i", "level_f"]),
+                              np.sort(plain[j], order=["level_i", "level_f"]))
