@@ -90,7 +90,7 @@ def parse(argv=None):
     ap.add_argument("--legs", default="plain,precision,serving,streamed,halfls")
     ap.add_argument("--only", default=None,
                     help="run only these legs (comma list) and print their JSON, no headline")
-    ap.add_argument("--serve-jobs", type=int, default=10000, help="serving: jobs (split path)")
+    ap.add_argument("--serve-jobs", type=int, default=2000, help="serving: jobs (split path)")
     ap.add_argument("--serve-fp64-jobs", type=int, default=50,
                     help="serving: the first jobs of the stream again on the FP64 path")
     ap.add_argument("--serve-rate", type=float, default=200.0, help="serving: Poisson jobs/s")

@@ -80,6 +80,30 @@ struct RefineRec {
   int32_t part, i, f, slot;
 };
 
+struct EpiParams {
+  int jI, jF, ndegI, ndegF, reduced, combo_mask;
+  double gns, zpe, beta, q_stat, fw0, fw1, thresh_S, thresh_I;
+  double A_coef, intens_cm_mol, avogno;
+  // exact re-evaluation of doubtful lines (refine.cu): the estimated error of
+  // a transition moment per unit of its H column's norm, the relative
+  // accuracy S must reach without it, the part (initial unit x final block)
+  // the launch serves, and whether lines past that accuracy are handed over
+  double err_coef, target;
+  int part, refine_cond;
+};
+
+// One part of a final block's T in the fused epilogue of the persistent final
+// GEMM: columns [c0, c1) hold the moments of nI initial levels of one unit,
+// grp = ndegI * ndegF consecutive columns per level.
+struct EpiPart {
+  int c0, c1, grp, pad;
+  const double* EI;     // the unit's initial energies
+  const double* BI;     // their Boltzmann factors exp(-(E - zpe) beta)
+  const int32_t* lvI;   // their line ids
+  const double* hn;     // norms of the part's H columns
+  EpiParams ep;
+};
+
 // Process-wide serial numbers: a captured launch sequence is tied to the
 // exact basis objects it read.
 uint64_t next_uid();
@@ -261,6 +285,8 @@ struct Ctx {
   DevArray<uint8_t> w_upper;
   DevArray<StencilTerm> w_stencil;
   DevArray<double> w_hn;       // H column norms of a group of final blocks
+  DevArray<double> w_BI;       // Boltzmann factors of the run's initial levels
+  DevArray<EpiPart> w_epi;     // parts of the fused epilogue
   DevArray<RefineRec> w_rec;   // lines handed to the exact re-evaluation
   int64_t refine_max = 0;      // doubtful lines re-evaluated per run (gi_set_refine)
   DevArray<int32_t> w_stencil_n, w_levelI, w_levelF;
@@ -341,17 +367,7 @@ void dipole_stream_release(Ctx* c);
 int dipole_panel_rows(const Ctx* c);
 
 // ------------------------------------------------------------------ kernels
-struct EpiParams {
-  int jI, jF, ndegI, ndegF, reduced, combo_mask;
-  double gns, zpe, beta, q_stat, fw0, fw1, thresh_S, thresh_I;
-  double A_coef, intens_cm_mol, avogno;
-  // exact re-evaluation of doubtful lines (refine.cu): the estimated error of
-  // a transition moment per unit of its H column's norm, the relative
-  // accuracy S must reach without it, the part (initial unit x final block)
-  // the launch serves, and whether lines past that accuracy are handed over
-  double err_coef, target;
-  int part, refine_cond;
-};
+
 
 
 cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int nI, int ndeg,
@@ -370,6 +386,11 @@ cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstri
                                       int cstride, const Basis& bF, const StencilTerm* st,
                                       const int32_t* st_n, int st_max, double* h,
                                       cudaStream_t s);
+
+// out[k] = exp(-(E[k] - zpe) beta) (the epilogue's initial-level factor).
+cudaError_t launch_boltz(const double* E, int n, double zpe, double beta, double* out,
+                         cudaStream_t s);
+
 // What the exact re-evaluation (refine.cu) needs of one epilogue part, an
 // initial unit against one final block; host arrays live for the run.
 struct RefinePart {

@@ -648,6 +648,9 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     grouped_final = split_grouped_final(c);
     fused_y = split_fused_y(c);
   }
+  // the persistent final GEMM forms the lines itself (no T round trip, no
+  // epilogue launches)
+  const bool fused_epi = grouped_final && split_fused_epilogue(c);
   // Final blocks go through the final-state GEMM in groups: with the persistent
   // grouped launch, consecutive blocks of a round until the group has work for
   // ~16 waves of the GPU (and at most the launch's problem count), so the lines
@@ -706,7 +709,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   // capacity bound would pin more than 16 GiB: then the copy follows the run)
   size_t nck = 0;
   for (size_t r = 0; r < rounds.size(); r++)
-    if (!rounds[r].units.empty()) nck += targets[r].size();
+    if (!rounds[r].units.empty()) nck += fused_epi ? groups[r].size() : targets[r].size();
   if (c->ck_cap < nck) {
     if (c->ck_count) cudaFreeHost(c->ck_count);
     c->ck_count = nullptr;
@@ -841,6 +844,44 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   double fl_half = 0.0, fl_final = 0.0, by_corr = 0.0;
   int64_t npairs_checked = 0;
 
+  // the fused epilogue's parts of every final block (in column order) and the
+  // initial levels' Boltzmann factors it reads
+  std::vector<std::vector<size_t>> epi_at(rounds.size());
+  if (fused_epi) {
+    std::vector<EpiPart> h_epi;
+    GI_CUDA(c, c->w_BI.reserve(std::max<size_t>(h_EI.size(), 1)));
+    for (size_t r = 0; r < rounds.size(); r++) {
+      epi_at[r].resize(targets[r].size());
+      for (const auto& grp : groups[r]) {
+        size_t hn_off = 0;
+        for (size_t t = grp.first; t < grp.second; t++) {
+          const Target& T = targets[r][t];
+          epi_at[r][t] = h_epi.size();
+          for (size_t k = 0; k < T.parts.size(); k++) {
+            const Unit& u = *T.parts[k].first;
+            const int g = c->degen[u.I->blk->gamma] * c->degen[T.F->blk->gamma];
+            EpiPart e;
+            e.c0 = (int)T.hcol[k];
+            e.c1 = (int)(T.hcol[k] + (size_t)u.nI * g);
+            e.grp = g;
+            e.pad = 0;
+            e.EI = c->w_EI.p + u.off;
+            e.BI = c->w_BI.p + u.off;
+            e.lvI = c->w_ivec.p + 2 * u.off + u.nI;
+            e.hn = c->w_hn.p + hn_off + T.hcol[k];
+            e.ep = rparts[part_of[r][t][k]].ep;
+            h_epi.push_back(e);
+          }
+          hn_off += T.ncolH;
+        }
+      }
+    }
+    GI_CUDA(c, c->w_epi.assign(h_epi));
+    mixv(c->w_epi.p);
+    mixv(c->w_BI.p);
+  }
+  mixv(fused_epi);
+
   // A serving pair job (one initial block, one unit per round): the half line
   // strength Z of its initial block may come from (or go to) the server's Z
   // cache, shared by every job with the same initial block and selection of
@@ -878,6 +919,10 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   bool capturing = false;
   auto issue = [&]() -> gi_status {
   size_t ck = 0;
+  if (fused_epi)
+    GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+              return launch_boltz(c->w_EI.p, (int)h_EI.size(), zpe, beta, c->w_BI.p, c->stream);
+            }));
   for (size_t r = 0; r < rounds.size(); r++) {
     const Round& R = rounds[r];
     if (R.units.empty()) continue;
@@ -956,10 +1001,21 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         for (size_t t = grp.first; t < grp.second; t++) {
           const Target& T = targets[r][t];
           Block& fb = *T.F->blk;
-          jobs.push_back(FinalJob{&fb, c->w_h.p + T.hoff, fb.ld, (int)T.ncolH, c->w_t.p + T.toff,
-                                  round_up(fb.nvec, 2)});
+          FinalJob j{&fb, c->w_h.p + T.hoff, fb.ld, (int)T.ncolH, c->w_t.p + T.toff,
+                     round_up(fb.nvec, 2)};
+          if (fused_epi) {
+            const auto off = farr[T.F];
+            j.parts = c->w_epi.p + epi_at[r][t];
+            j.nparts = (int)T.parts.size();
+            j.EF = fb.d_energies.p;
+            j.upper = c->w_upper.p + off.second;
+            j.lvF = c->w_int.p + off.first;
+          }
+          jobs.push_back(j);
         }
-        gi_status s = split_gemm_final_grouped(c, jobs);
+        const FusedLines fl{c->d_lines.p, c->w_counter.p, (long long)c->d_lines.n, c->w_rec.p,
+                            rec_cap};
+        gi_status s = split_gemm_final_grouped(c, jobs, fused_epi ? &fl : nullptr);
         if (s != GI_OK) return s;
       } else {
         for (size_t t = grp.first; t < grp.second; t++) {
@@ -989,6 +1045,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         const auto off = farr[&Fp];
         for (size_t k = 0; k < T.parts.size(); k++) {
           const Unit& u = *T.parts[k].first;
+          npairs_checked += (int64_t)u.nI * Fp.nupper;
+          if (fused_epi) continue;  // formed by the final GEMM's epilogue warps
           const EpiParams ep = rparts[part_of[r][t][k]].ep;
           const int32_t* d_lvI = c->w_ivec.p + 2 * u.off + u.nI;
           const double* hn = c->w_hn.p + hn_at[t - grp.first] + T.hcol[k];
@@ -1000,8 +1058,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
                                            c->w_counter.p, (long long)c->d_lines.n, c->w_rec.p,
                                            rec_cap, c->stream);
                   }));
-          npairs_checked += (int64_t)u.nI * Fp.nupper;
         }
+        if (fused_epi && t + 1 < grp.second) continue;  // one checkpoint per group
         // checkpoint: every line of this final block is written once this fires
         GI_CUDA(c, cudaMemcpyAsync(c->ck_count + ck, c->w_counter.p, sizeof(unsigned long long),
                                    cudaMemcpyDeviceToHost, c->stream));

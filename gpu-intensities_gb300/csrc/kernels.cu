@@ -15,6 +15,7 @@
 #include <cuda_runtime.h>
 
 #include "engine.h"
+#include "epilogue.cuh"
 
 namespace gi {
 
@@ -180,8 +181,8 @@ cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstri
 }
 
 // ------------------------------------------------------------------ epilogue
-// Degeneracy sum, S, A_if, I(T), frequency window and thresholds
-// (cuda_host.cu:1376-1408), then a warp-aggregated append of kept lines.
+// One thread per (initial level i, final level f) of a part: the per-line
+// epilogue of epilogue.cuh on the moments of T.
 __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF,
                            const int32_t* __restrict__ levelI, const double* __restrict__ EI,
                            const int32_t* __restrict__ levelF, const double* __restrict__ EF,
@@ -195,81 +196,33 @@ __global__ void k_epilogue(const double* __restrict__ T, int ldt, int nI, int nF
   __shared__ double boltz_i;
   if (threadIdx.x == 0) boltz_i = exp(-(EI[i] - p.zpe) * p.beta);
   __syncthreads();
-  bool keep = false, pass = false, doubt = false;
-  gi_line L;
-  if (f < nF && upper_ok[f]) {
-    const double ei = EI[i], ef = EF[f];
-    const double nu = ef - ei;
-    if (nu >= p.fw0 && nu <= p.fw1) {
-      pass = true;
-      double t[4] = {0.0, 0.0, 0.0, 0.0};
-      for (int dF = 0; dF < p.ndegF; ++dF)
-        for (int dI = 0; dI < p.ndegI; ++dI)
-          if (p.combo_mask & (1 << (dI + 2 * dF)))
-            t[dI + 2 * dF] = T[((size_t)(i * p.ndegI + dI) * p.ndegF + dF) * ldt + f];
-      double ls = 0.0;
-      for (int dF = 0; dF < p.ndegF; ++dF)
-        for (int dI = 0; dI < p.ndegI; ++dI) ls += t[dI + 2 * dF] * t[dI + 2 * dF];
-      ls /= (double)p.ndegI;
-      if (p.reduced && p.ndegF != 1 && p.ndegI != 1) ls *= (double)p.ndegI;
-      const double anu = fabs(nu);
-      const double boltz_fc = anu * boltz_i * (1.0 - exp(-anu * p.beta)) / p.q_stat;
-      const double A = p.A_coef * (double)(2 * p.jI + 1) * ls * (anu * anu * anu);
-      const double S = ls * p.gns * (double)((2 * p.jI + 1) * (2 * p.jF + 1));
-      const double In = S * p.intens_cm_mol * boltz_fc;
-      keep = (S >= p.thresh_S) && (In / p.avogno >= p.thresh_I);
-      // doubtful lines: the relative error of S estimated from the moments and
-      // their columns' norms (an error of err_coef * |H col| per moment); a
-      // kept line whose estimate passes the target, and any line whose S or I
-      // sits within the estimate of a threshold, is re-evaluated exactly
-      double num = 0.0, den = 0.0;
-      for (int dF = 0; dF < p.ndegF; ++dF)
-        for (int dI = 0; dI < p.ndegI; ++dI)
-          if (p.combo_mask & (1 << (dI + 2 * dF))) {
-            const double tq = t[dI + 2 * dF];
-            num += fabs(tq) * hn[(i * p.ndegI + dI) * p.ndegF + dF];
-            den += tq * tq;
-          }
-      const double rel = den > 0.0 ? 2.0 * p.err_coef * num / den : 0.0;
-      const double band = 4.0 * rel + 1e-14;
-      const bool near_S = p.thresh_S > 0.0 && fabs(S - p.thresh_S) <= band * p.thresh_S;
-      const double Im = In / p.avogno;
-      const bool near_I = p.thresh_I > 0.0 && fabs(Im - p.thresh_I) <= band * p.thresh_I;
-      const bool doubtful = keep && rel > p.target;
-      if (doubtful) atomicAdd(counter + 3, 1ull);
-      doubt = near_S || near_I || (doubtful && p.refine_cond);
-      L.level_i = levelI[i];
-      L.level_f = levelF[f];
-      L.ndeg_i = p.ndegI;
-      L.ndeg_f = p.ndegF;
-      L.nu = nu;
-      L.S = S;
-      L.A = A;
-      L.I = In;
-#pragma unroll
-      for (int q = 0; q < 4; ++q) L.t[q] = t[q];
-    }
-  }
-  const int lane = threadIdx.x & 31;
-  const unsigned pmask = __ballot_sync(0xffffffffu, pass);
-  if (pmask && lane == 0) atomicAdd(counter + 1, (unsigned long long)__popc(pmask));
-  const unsigned mask = __ballot_sync(0xffffffffu, keep);
-  long long slot = -1;
-  if (mask) {
-    const int leader = __ffs(mask) - 1;
-    unsigned long long base = 0;
-    if (lane == leader) base = atomicAdd(counter, (unsigned long long)__popc(mask));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (keep) {
-      const unsigned long long pos = base + __popc(mask & ((1u << lane) - 1u));
-      if ((long long)pos < cap) out[pos] = L;
-      slot = (long long)pos;
-    }
-  }
-  if (doubt) {
-    const unsigned long long k = atomicAdd(counter + 2, 1ull);
-    if ((long long)k < rec_cap) rec[k] = RefineRec{p.part, i, f, (int32_t)slot};
-  }
+  double t[4] = {0.0, 0.0, 0.0, 0.0}, hnq[4] = {0.0, 0.0, 0.0, 0.0};
+  const bool ok_f = f < nF && upper_ok[f];
+  if (ok_f)
+    for (int dF = 0; dF < p.ndegF; ++dF)
+      for (int dI = 0; dI < p.ndegI; ++dI)
+        if (p.combo_mask & (1 << (dI + 2 * dF))) {
+          const int col = (i * p.ndegI + dI) * p.ndegF + dF;
+          t[dI + 2 * dF] = T[(size_t)col * ldt + f];
+          hnq[dI + 2 * dF] = hn[col];
+        }
+  LineEval r;
+  eval_line(p, t, hnq, EI[i], ok_f ? EF[f] : 0.0, boltz_i, ok_f, levelI[i],
+            ok_f ? levelF[f] : -1, r);
+  append_line(r, p.part, i, f, out, counter, cap, rec, rec_cap);
+}
+
+__global__ void k_boltz(const double* __restrict__ E, int n, double zpe, double beta,
+                        double* __restrict__ out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = exp(-(E[k] - zpe) * beta);
+}
+
+cudaError_t launch_boltz(const double* E, int n, double zpe, double beta, double* out,
+                         cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_boltz<<<(n + 255) / 256, 256, 0, s>>>(E, n, zpe, beta, out);
+  return cudaGetLastError();
 }
 
 // Euclidean norm of each H column (the scale of its transition moments' error).

@@ -46,6 +46,7 @@
 #include <tuple>
 
 #include "split.h"
+#include "epilogue.cuh"
 #include "../../include/gi_probe.h"
 
 namespace gi {
@@ -592,7 +593,7 @@ __device__ __forceinline__ void tmem_wait_ld() {
 
 // ACC: add to C (the later launches of a K-segmented GEMM); a template
 // argument, so the first launch's code carries no trace of it.
-template <int S, int BN, int D1, bool ACC>
+template <int S, int BN, int D1, bool ACC, bool KPARTS = false>
 __global__ void __launch_bounds__(kThreadsG, 1)
     k_split_gemm_g(const __grid_constant__ CUtensorMap tmAq, const __grid_constant__ CUtensorMap tmAt,
                    const __grid_constant__ CUtensorMap tmBq, const __grid_constant__ CUtensorMap tmBt,
@@ -633,8 +634,8 @@ __global__ void __launch_bounds__(kThreadsG, 1)
   const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
   // K parts (grid y): part p contracts K steps [p * kpart_steps, ...) into its
   // own output C + p * strideP (kpart_steps = 0: one part, the whole K)
-  const int kb0 = (int)blockIdx.y * kpart_steps;
-  const int nk = kpart_steps ? min(kpart_steps, K / kBK - kb0) : K / kBK;
+  const int kb0 = KPARTS ? (int)blockIdx.y * kpart_steps : 0;
+  const int nk = KPARTS ? min(kpart_steps, K / kBK - kb0) : K / kBK;
   const int nk0 = nk / PK;  // ring slots of pass 0 (K parts are multiples of 64)
   const int nslots = nk0 + (NPASS == 2 ? nk : 0);
 
@@ -773,7 +774,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
     const int q4 = warp & 3, half = (warp - 2) >> 2;
     const int m = m0 + q4 * 32 + lane;
     const int emr = (m < M) ? ea[z * Mpad + m] : 0;
-    double* Cz = C + (size_t)z * strideC + (size_t)blockIdx.y * strideP;
+    double* Cz = C + (size_t)z * strideC + (KPARTS ? (size_t)blockIdx.y * strideP : 0);
     const uint32_t lanes = (uint32_t)(q4 * 32) << 16;
     long long v0[NCH][kChunkG];  // pass 0's exact sums of this thread's columns
     bool ok = true;
@@ -856,7 +857,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
 // the barriers that hand it between the MMA issuer and the epilogue count
 // segments: accf[p] completes once per segment and pass, tfree0 / tfree1 once
 // per segment after the epilogue has read pass 0 / pass 1.
-constexpr int kGpMaxProb = 44;  // 44 x 576 B of kernel parameters (limit 32,764 B)
+constexpr int kGpMaxProb = 44;  // 44 x 640 B of kernel parameters (limit 32,764 B)
 
 struct GpProb {
   CUtensorMap aq, at, bq, bt;
@@ -864,11 +865,62 @@ struct GpProb {
   const int32_t* eb;
   double* C;
   int ldc, M, Mpad, Nc, K, nM, nN, first;  // first: the problem's first work item
+  // the fused epilogue: the block's parts (initial units, sorted by column)
+  // and its final levels' energies, upper-filter flags and line ids
+  const EpiPart* parts;
+  const double* EF;
+  const uint8_t* upper;
+  const int32_t* lvF;
+  int nparts;
 };
+static_assert(sizeof(GpProb) <= 640, "problem parameters");
 struct GpParams {
   GpProb p[kGpMaxProb];
   int nprob, nitems;
+  // fused: the last K segment's epilogue forms the lines (epilogue.cuh)
+  // instead of storing T
+  int fused;
+  gi_line* out;
+  unsigned long long* counter;
+  long long cap;
+  RefineRec* rec;
+  long long rec_cap;
 };
+static_assert(sizeof(GpParams) <= 32764, "kernel parameter limit");
+
+// The fused epilogue of one 8-column chunk of a final block's T, held by one
+// thread for final level f = m: groups of G consecutive columns are the
+// moments of one initial level (G = ndegI * ndegF combinations).
+template <int G>
+__device__ __forceinline__ void fused_chunk(const GpParams& P, const GpProb& pr, int nbase, int m,
+                                            bool row_ok, const double* outv) {
+#pragma unroll
+  for (int g0 = 0; g0 < kChunkG; g0 += G) {
+    const int n = nbase + g0;
+    if (n >= pr.Nc) break;  // the same for every lane of the warp
+    int q = 0;
+    while (q + 1 < pr.nparts && pr.parts[q + 1].c0 <= n) ++q;
+    const EpiPart& pt = pr.parts[q];
+    const EpiParams& ep = pt.ep;
+    const int i = (n - pt.c0) / G;
+    // column offset dI * ndegF + dF within the group -> moment index dI + 2 dF
+    double t[4] = {0.0, 0.0, 0.0, 0.0}, hnq[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll
+    for (int o = 0; o < G; ++o) {
+      const int dI = (G == 4) ? (o >> 1) : (G == 2 ? (ep.ndegF == 1 ? o : 0) : 0);
+      const int dF = (G == 4) ? (o & 1) : (G == 2 ? (ep.ndegF == 1 ? 0 : o) : 0);
+      if (ep.combo_mask & (1 << (dI + 2 * dF))) {
+        t[dI + 2 * dF] = outv[g0 + o];
+        hnq[dI + 2 * dF] = pt.hn[i * G + o];
+      }
+    }
+    const bool ok_f = row_ok && pr.upper[m];
+    LineEval r;
+    eval_line(ep, t, hnq, pt.EI[i], ok_f ? pr.EF[m] : 0.0, pt.BI[i], ok_f, pt.lvI[i],
+              ok_f ? pr.lvF[m] : -1, r);
+    append_line(r, ep.part, i, m, P.out, P.counter, P.cap, P.rec, P.rec_cap);
+  }
+}
 
 template <int S, int BN, int D1>
 __global__ void __launch_bounds__(kThreadsG, 1)
@@ -1099,18 +1151,34 @@ __global__ void __launch_bounds__(kThreadsG, 1)
             if (pass == 0) {
 #pragma unroll
               for (int j = 0; j < kChunkG; ++j) v0[ch][j] = v[j];
-            } else if (m < pr.M) {
+            } else {
+              // the last segment of a fused launch forms the lines; every
+              // other segment stores its sum for the next one
+              const bool row_ok = m < pr.M;
+              const bool lines = P.fused && k0 + kKSeg >= pr.K;
+              double outv[kChunkG];
 #pragma unroll
               for (int j = 0; j < kChunkG; ++j) {
                 const int n = n0 + c0 + j;
-                if (n < pr.Nc) {
+                outv[j] = 0.0;
+                if (row_ok && n < pr.Nc) {
                   const int base = emr + pr.eb[n] - 2 * w;
                   double out = scaled_int(v0[ch][j], base - w * (D1 - 1)) +
                                scaled_int(v[j], base - w * (S - 1));
                   double* dst = pr.C + (size_t)n * pr.ldc + m;
                   if (k0 > 0) out += ld_acc(dst);  // the earlier segments' sum
-                  *dst = out;
+                  if (!lines) *dst = out;
+                  outv[j] = out;
                 }
+              }
+              if (lines) {
+                const int G = pr.parts[0].grp;
+                if (G == 4)
+                  fused_chunk<4>(P, pr, n0 + c0, m, row_ok, outv);
+                else if (G == 2)
+                  fused_chunk<2>(P, pr, n0 + c0, m, row_ok, outv);
+                else
+                  fused_chunk<1>(P, pr, n0 + c0, m, row_ok, outv);
               }
             }
           }
@@ -1511,6 +1579,10 @@ cudaError_t set_attributes() {
         status = set_smem(k_split_gemm_g<S, BN2, d1b_of(S), false>, smemg_bytes(S, BN2), k_split_gemm_g<S, BN2, d1b_of(S), true>);
       if (status == cudaSuccess)
         status = set_smem(k_split_gemm_g<S, BN1, S, false>, smemg_bytes(S, BN1), k_split_gemm_g<S, BN1, S, true>);
+      if (status == cudaSuccess)
+        status = cudaFuncSetAttribute(k_split_gemm_g<S, BN1, S, false, true>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smemg_bytes(S, BN1));
       if constexpr (S == 9) {
         if (status == cudaSuccess)
           status = cudaFuncSetAttribute(k_split_gemm_gp<S, BN2, D1>,
@@ -1560,7 +1632,13 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
   if constexpr (S >= 4) {
     if (cfg.kind >= 6 && cfg.kind <= 8) {
       const dim3 grid((unsigned)(nA * nN), (unsigned)std::max(kparts, 1));
-      if (kparts <= 1) kpart_steps = 0;
+      if (kparts > 1) {  // K parts: the one-pass kernel only
+        if (cfg.kind != 8 || accum) return cudaErrorInvalidValue;
+        k_split_gemm_g<S, BN1, S, false, true><<<grid, kThreadsG, sm, st>>>(
+            mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
+            err, kpart_steps, strideP);
+        return cudaGetLastError();
+      }
       if (cfg.kind == 8)
         (accum ? k_split_gemm_g<S, BN1, S, true> : k_split_gemm_g<S, BN1, S, false>)<<<grid, kThreadsG, sm, st>>>(
             mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M, Mpad, Nc, K, w, nM, nA, nN, GA,
@@ -2033,7 +2111,14 @@ int split_grouped_items(int nvec, int ncol) {
   return (round_up(nvec, kBM) / kBM) * ((ncol + bn2_of(9) - 1) / bn2_of(9));
 }
 
-gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
+bool split_fused_epilogue(const Ctx* c) {
+  if (!split_grouped_final(c)) return false;
+  const char* e = getenv("GI_SPLIT_FUSED_EPI");
+  return !(e && std::strcmp(e, "0") == 0);
+}
+
+gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs,
+                                   const FusedLines* lines) {
   SplitState* S = state(c);
   constexpr int SS = 9, BN = bn2_of(SS), D1 = d1_of(SS);
   if (S->s != SS || !S->grouped || jobs.empty() || (int)jobs.size() > kGpMaxProb) {
@@ -2055,9 +2140,17 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
   for (size_t i = 0; i < jobs.size(); ++i) order[i] = (int)i;
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return jobs[a].ldh > jobs[b].ldh; });
-  GpParams* P = new GpParams();  // ~25 KB: not on the host stack
+  GpParams* P = new GpParams();  // ~28 KB: not on the host stack
   P->nprob = (int)jobs.size();
   P->nitems = 0;
+  P->fused = lines ? 1 : 0;
+  if (lines) {
+    P->out = lines->out;
+    P->counter = lines->counter;
+    P->cap = lines->cap;
+    P->rec = lines->rec;
+    P->rec_cap = lines->rec_cap;
+  }
   size_t eoff = 0, boff = 0;
   double flops = 0.0;
   for (int q = 0; q < (int)jobs.size() && g == GI_OK; ++q) {
@@ -2093,6 +2186,15 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs) {
     pr.nM = vpad / kBM;
     pr.nN = (j.ncol + BN - 1) / BN;
     pr.first = P->nitems;
+    pr.parts = j.parts;
+    pr.nparts = j.nparts;
+    pr.EF = j.EF;
+    pr.upper = j.upper;
+    pr.lvF = j.lvF;
+    if (lines && (!j.parts || j.nparts <= 0)) {
+      g = check(c, cudaErrorInvalidValue, "fused epilogue without parts");
+      break;
+    }
     P->nitems += pr.nM * pr.nN;
     boff += (size_t)SS * j.ncol * K;
     eoff += j.ncol;

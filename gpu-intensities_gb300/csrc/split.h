@@ -36,11 +36,32 @@ struct FinalJob {
   int ldh, ncol;
   double* T;
   int ldt;
+  // the fused epilogue (split_gemm_final_grouped with lines != null): the
+  // block's parts and its final levels' energies, upper flags and line ids
+  const EpiPart* parts = nullptr;
+  int nparts = 0;
+  const double* EF = nullptr;
+  const uint8_t* upper = nullptr;
+  const int32_t* lvF = nullptr;
+};
+// Where the fused epilogue puts its lines (the stand-alone epilogue's
+// arguments, epilogue.cuh).
+struct FusedLines {
+  gi_line* out;
+  unsigned long long* counter;
+  long long cap;
+  RefineRec* rec;
+  long long rec_cap;
 };
 bool split_grouped_final(const Ctx* c);  // the persistent grouped launch applies
 int split_grouped_max_jobs();
 int split_grouped_items(int nvec, int ncol);  // work items of one job
-gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs);
+// With lines != null the epilogue warps form every job's lines (S, A, I,
+// filters, thresholds) on the last K segment instead of storing T.
+gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs,
+                                   const FusedLines* lines = nullptr);
+// The fused epilogue applies (GI_SPLIT_FUSED_EPI=0 turns it off).
+bool split_fused_epilogue(const Ctx* c);
 // Called once per run before the launch loop (sizes workspaces, slices the dipole).
 gi_status split_prepare(Ctx* c);
 // Before a launch sequence that must not allocate (graph capture): the B

@@ -134,3 +134,44 @@ def test_persistent_grouped_final_gemm(pkg, synth, monkeypatch, case, budget):
     assert len(a) > 1000 and lb < la
     for f in a.dtype.names:
         assert np.array_equal(a[f], b[f]), f
+
+
+@pytest.mark.parametrize("case,budget,thresh", [("c3v", 0, 0.0), ("c3v", 24 << 20, 1e-30),
+                                                ("c2v_large_k", 0, 1e-30),
+                                                ("c3v_many_blocks", 0, 0.0),
+                                                ("c3v_reduced", 0, 1e-30)])
+def test_fused_epilogue_matches_separate(pkg, synth, monkeypatch, case, budget, thresh):
+    """The S/A/I epilogue formed by the persistent final GEMM's epilogue warps
+    on the last K segment gives the lines of the separate epilogue launches,
+    bit for bit (every field), with fewer launches: one round or many, two K
+    segments per tile, groups split at the launch's problem limit, degenerate
+    symmetries with the reduced combination rule; with graph replay too."""
+    if case.startswith("c3v") and case != "c3v_many_blocks":
+        prob = synth.make_c3v(71, 40, [0, 1, 2, 3, 4], nvec_max=30,
+                              reduced=case.endswith("reduced"))
+    elif case == "c2v_large_k":
+        prob = synth.make_c2v(61, 1200, [0, 1, 2, 3], nvec_max=12)
+    else:
+        prob = synth.make_c3v(72, 24, list(range(21)), nvec_max=6)
+    prob.params.thresh_intensity = thresh
+    out = {}
+    for mode in ("0", "1"):
+        monkeypatch.setenv("GI_SPLIT_FUSED_EPI", mode)
+        with pkg.Engine(0, hbm_budget=budget) as eng:
+            eng.load(prob, precision=1)
+            eng.run()
+            st = eng.stats()
+            lines = pkg.keyed(eng.lines(), eng.levels())
+            eng.run(graph=True)
+            eng.run(graph=True)  # a replay
+            again = pkg.keyed(eng.lines(), eng.levels())
+        out[mode] = (lines, again, st)
+    order = ["jI", "gammaI", "recI", "jF", "gammaF", "recF"]
+    (a, a2, sa), (b, b2, sb) = out["0"], out["1"]
+    a, b = np.sort(a, order=order), np.sort(b, order=order)
+    b2 = np.sort(b2, order=order)
+    assert len(a) > 1000 and sb["kernel_launches"] < sa["kernel_launches"]
+    assert sb["nlines_filtered"] == sa["nlines_filtered"]
+    for f in a.dtype.names:
+        assert np.array_equal(a[f], b[f]), f
+        assert np.array_equal(b[f], b2[f]), f
