@@ -30,6 +30,7 @@ GI_PREC_FP64, GI_PREC_SPLIT = 0, 1
 GI_RUN_LINES_ON_DEVICE = 1
 GI_RUN_PHASE_TIMING = 2
 GI_RUN_GRAPH = 4
+GI_RUN_COMPACT_LINES = 8
 PHASES = ("correlate", "halfls_gemm", "stencil", "final_gemm", "epilogue", "slice")
 GI_MAX_REP, GI_MAX_MODES = 8, 16
 
@@ -55,6 +56,9 @@ LINE_DTYPE = np.dtype([("level_i", np.int32), ("level_f", np.int32), ("ndeg_i", 
 LEVEL_DTYPE = np.dtype([("J", np.int32), ("gamma", np.int32), ("rec", np.int32),
                         ("ndeg", np.int32), ("krot", np.int32), ("taurot", np.int32),
                         ("energy", np.float64)])
+# gi_line_compact: the 40-byte record of GI_RUN_COMPACT_LINES
+LINE_COMPACT_DTYPE = np.dtype([("level_i", np.int32), ("level_f", np.int32), ("nu", np.float64),
+                               ("S", np.float64), ("A", np.float64), ("I", np.float64)])
 
 
 class gi_stats(C.Structure):
@@ -195,6 +199,7 @@ def lib():
         L.gi_serve_reset_stats.argtypes = [C.c_void_p]
         L.gi_get_lines.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
         L.gi_sort_lines.argtypes = [C.c_void_p]
+        L.gi_get_lines_compact.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p]
         L.gi_num_levels.argtypes = [C.c_void_p, C.POINTER(C.c_int32)]
         L.gi_get_levels.argtypes = [C.c_void_p, C.c_int32, C.c_void_p]
         L.gi_get_stats.argtypes = [C.c_void_p, C.POINTER(gi_stats)]
@@ -461,12 +466,14 @@ class Engine:
 
     # run -----------------------------------------------------------------
     def run(self, lines_on_device: bool = False, phase_timing: bool = False,
-            graph: bool = False, shard: int = 0, nshards: int = 1) -> int:
+            graph: bool = False, shard: int = 0, nshards: int = 1, compact: bool = False) -> int:
         """gi_run, or with nshards > 1 gi_run_shard: the initial levels at
-        positions l % nshards == shard of the level table."""
+        positions l % nshards == shard of the level table.  compact: the
+        lines come back to host memory as 40-byte records (lines_compact)."""
         n = C.c_int64(0)
         flags = (GI_RUN_LINES_ON_DEVICE if lines_on_device else 0) | \
-            (GI_RUN_PHASE_TIMING if phase_timing else 0) | (GI_RUN_GRAPH if graph else 0)
+            (GI_RUN_PHASE_TIMING if phase_timing else 0) | (GI_RUN_GRAPH if graph else 0) | \
+            (GI_RUN_COMPACT_LINES if compact else 0)
         if nshards > 1:
             self._ck(self._L.gi_run_shard(self._h, flags, shard, nshards, C.byref(n)))
         else:
@@ -480,6 +487,16 @@ class Engine:
         out = np.empty(count, LINE_DTYPE)
         if count:
             self._ck(self._L.gi_get_lines(self._h, offset, count, out.ctypes.data))
+        return out
+
+    def lines_compact(self, offset: int = 0, count: Optional[int] = None) -> np.ndarray:
+        """The last run's lines as gi_line_compact records."""
+        total = self.stats()["nlines"]
+        if count is None:
+            count = total - offset
+        out = np.empty(count, LINE_COMPACT_DTYPE)
+        if count:
+            self._ck(self._L.gi_get_lines_compact(self._h, offset, count, out.ctypes.data))
         return out
 
     def sort_lines(self):

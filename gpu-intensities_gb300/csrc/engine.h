@@ -152,7 +152,10 @@ struct Block {
   // residency under a serving budget: an evicted block keeps its vectors in
   // pinned host memory and has no device arrays
   bool resident = true;
-  double* h_vecs = nullptr;  // pinned [nvec][nsize] while evicted
+  double* h_vecs = nullptr;  // pinned [nvec][nsize]: the vectors while evicted, and
+                             // kept after a restore, so that a later eviction of
+                             // the same version copies nothing
+  uint64_t h_version = ~0ull;  // the version h_vecs holds
   int pins = 0;              // running jobs that use the block
   uint64_t uid = next_uid(); // identity and vector version (serving Z cache)
   uint64_t version = 0;      // bumped whenever the vectors change
@@ -229,6 +232,12 @@ struct Ctx {
   size_t h_lines_cap = 0;
   DevArray<gi_line> d_lines;
   bool lines_on_device = false;
+  // GI_RUN_COMPACT_LINES: the read-back is packed into d_compact on the
+  // device, and the host receives 40-byte records in h_compact
+  bool compact_lines = false;
+  DevArray<gi_line_compact> d_compact;
+  gi_line_compact* h_compact = nullptr;
+  size_t h_compact_cap = 0;
   int64_t nlines = 0;
   gi_stats stats{};
 
@@ -388,6 +397,8 @@ cudaError_t launch_half_ls_prim_parts(const double* Zp, int nparts, size_t pstri
                                       cudaStream_t s);
 
 // out[k] = exp(-(E[k] - zpe) beta) (the epilogue's initial-level factor).
+cudaError_t launch_pack_lines(const gi_line* in, gi_line_compact* out, long long n,
+                              cudaStream_t st);
 cudaError_t launch_boltz(const double* E, int n, double zpe, double beta, double* out,
                          cudaStream_t s);
 

@@ -521,6 +521,7 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   size_t cap_total = 0;
   for (auto& pp : pairs) cap_total += (size_t)pp.I->ivec.size() * pp.F->nupper;
   c->lines_on_device = (flags & GI_RUN_LINES_ON_DEVICE) != 0;
+  c->compact_lines = !c->lines_on_device && (flags & GI_RUN_COMPACT_LINES) != 0;
 
   // per-block device side arrays (levels, energies, upper flags) - uploaded once
   std::map<BlockPlan*, std::pair<size_t, size_t>> farr;  // offsets into w_int / w_upper
@@ -726,13 +727,38 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   if (!c->d2h) GI_CUDA(c, cudaStreamCreateWithFlags(&c->d2h, cudaStreamNonBlocking));
   const size_t cap_lines = c->d_lines.n;
   const bool overlap_d2h = !c->lines_on_device && cap_lines * sizeof(gi_line) <= ((size_t)16 << 30);
-  if (overlap_d2h && c->h_lines_cap < cap_lines) {
+  if (overlap_d2h && !c->compact_lines && c->h_lines_cap < cap_lines) {
     if (c->h_lines) cudaFreeHost(c->h_lines);
     c->h_lines = nullptr;
     c->h_lines_cap = 0;
     GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_lines), sizeof(gi_line) * cap_lines));
     c->h_lines_cap = cap_lines;
   }
+  if (c->compact_lines) {
+    if (c->d_compact.n < cap_lines) GI_CUDA(c, c->d_compact.alloc(cap_lines));
+    if (overlap_d2h && c->h_compact_cap < cap_lines) {
+      if (c->h_compact) cudaFreeHost(c->h_compact);
+      c->h_compact = nullptr;
+      c->h_compact_cap = 0;
+      GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_compact),
+                                sizeof(gi_line_compact) * cap_lines));
+      c->h_compact_cap = cap_lines;
+    }
+  }
+  // read-back of lines [a, b): full records, or packed on the device first
+  auto read_back = [&](unsigned long long a, unsigned long long b, cudaStream_t st) -> gi_status {
+    if (b <= a) return GI_OK;
+    if (c->compact_lines) {
+      GI_CUDA(c, launch_pack_lines(c->d_lines.p + a, c->d_compact.p + a, (long long)(b - a), st));
+      c->stats.kernel_launches++;
+      GI_CUDA(c, cudaMemcpyAsync(c->h_compact + a, c->d_compact.p + a,
+                                 sizeof(gi_line_compact) * (b - a), cudaMemcpyDeviceToHost, st));
+    } else {
+      GI_CUDA(c, cudaMemcpyAsync(c->h_lines + a, c->d_lines.p + a, sizeof(gi_line) * (b - a),
+                                 cudaMemcpyDeviceToHost, st));
+    }
+    return GI_OK;
+  };
 
   // The plan's identity for graph replay: every pointer, size and value the
   // launch sequence passes to a kernel follows from these.
@@ -1147,8 +1173,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       GI_CUDA(c, cudaEventSynchronize(c->ck_ev[k]));
       const unsigned long long n = std::min<unsigned long long>(c->ck_count[k], cap_lines);
       if (n > copied) {
-        GI_CUDA(c, cudaMemcpyAsync(c->h_lines + copied, c->d_lines.p + copied,
-                                   sizeof(gi_line) * (n - copied), cudaMemcpyDeviceToHost, c->d2h));
+        gi_status s = read_back(copied, n, c->d2h);
+        if (s != GI_OK) return s;
         copied = n;
       }
     }
@@ -1164,21 +1190,26 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
   if (count > c->d_lines.n) return fail(c, GI_ERR_DEVICE, "line buffer overflow (%llu lines)", count);
   c->nlines = (int64_t)count;
   if (overlap_d2h) {
-    if (count > copied)
-      GI_CUDA(c, cudaMemcpyAsync(c->h_lines + copied, c->d_lines.p + copied,
-                                 sizeof(gi_line) * (count - copied), cudaMemcpyDeviceToHost,
-                                 c->d2h));
+    gi_status s = read_back(copied, count, c->d2h);
+    if (s != GI_OK) return s;
     GI_CUDA(c, cudaStreamSynchronize(c->d2h));
   } else if (!c->lines_on_device && count) {
-    if (c->h_lines_cap < count) {
+    if (c->compact_lines && c->h_compact_cap < count) {
+      if (c->h_compact) cudaFreeHost(c->h_compact);
+      c->h_compact = nullptr;
+      c->h_compact_cap = 0;
+      GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_compact),
+                                sizeof(gi_line_compact) * count));
+      c->h_compact_cap = count;
+    } else if (!c->compact_lines && c->h_lines_cap < count) {
       if (c->h_lines) cudaFreeHost(c->h_lines);
       c->h_lines = nullptr;
       c->h_lines_cap = 0;
       GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&c->h_lines), sizeof(gi_line) * count));
       c->h_lines_cap = count;
     }
-    GI_CUDA(c, cudaMemcpyAsync(c->h_lines, c->d_lines.p, sizeof(gi_line) * count,
-                               cudaMemcpyDeviceToHost, c->stream));
+    gi_status s = read_back(0, count, c->stream);
+    if (s != GI_OK) return s;
     GI_CUDA(c, cudaStreamSynchronize(c->stream));
   }
   float ms = 0.f;
@@ -1223,6 +1254,7 @@ void ctx_release(Ctx* c) {
   cudaStreamSynchronize(c->stream);
   split_release(c);
   if (c->h_lines) cudaFreeHost(c->h_lines);
+  if (c->h_compact) cudaFreeHost(c->h_compact);
   if (c->hls_pin) cudaFreeHost(c->hls_pin);
   if (c->d2h) {
     cudaStreamSynchronize(c->d2h);
@@ -1480,6 +1512,7 @@ static gi_status set_block(Ctx* c, int J, int gamma, int nsize, int nvec, const 
         GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&b->h_vecs), sizeof(double) * n));
         GI_CUDA(c, cudaMemcpy(b->h_vecs, vecs, sizeof(double) * n,
                               vecs_on_device ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+        b->h_version = b->version;
       }
       if (b->d_energies.n != (size_t)std::max(nvec, 1)) GI_CUDA(c, b->d_energies.alloc(nvec));
       if (nvec)
@@ -1548,11 +1581,35 @@ gi_status gi_get_lines(gi_ctx* h, int64_t offset, int64_t count, gi_line* out) {
   if (!c || offset < 0 || count < 0 || (count && !out)) return GI_ERR_ARG;
   if (offset + count > c->nlines) return fail(c, GI_ERR_ARG, "line range past the end");
   if (!count) return GI_OK;
-  if (c->lines_on_device) {
+  if (c->lines_on_device || c->compact_lines) {
+    cudaSetDevice(c->device);
     GI_CUDA(c, cudaMemcpy(out, c->d_lines.p + offset, sizeof(gi_line) * count, cudaMemcpyDeviceToHost));
   } else {
     std::memcpy(out, c->h_lines + offset, sizeof(gi_line) * count);
   }
+  return GI_OK;
+}
+
+gi_status gi_get_lines_compact(gi_ctx* h, int64_t offset, int64_t count, gi_line_compact* out) {
+  Ctx* c = reinterpret_cast<Ctx*>(h);
+  if (!c || offset < 0 || count < 0 || (count && !out)) return GI_ERR_ARG;
+  if (offset + count > c->nlines) return fail(c, GI_ERR_ARG, "line range past the end");
+  if (!count) return GI_OK;
+  if (c->compact_lines) {
+    std::memcpy(out, c->h_compact + offset, sizeof(gi_line_compact) * count);
+    return GI_OK;
+  }
+  std::vector<gi_line> tmp;
+  const gi_line* L = c->h_lines + offset;
+  if (c->lines_on_device) {
+    cudaSetDevice(c->device);
+    tmp.resize((size_t)count);
+    GI_CUDA(c, cudaMemcpy(tmp.data(), c->d_lines.p + offset, sizeof(gi_line) * count,
+                          cudaMemcpyDeviceToHost));
+    L = tmp.data();
+  }
+  for (int64_t i = 0; i < count; i++)
+    out[i] = gi_line_compact{L[i].level_i, L[i].level_f, L[i].nu, L[i].S, L[i].A, L[i].I};
   return GI_OK;
 }
 
@@ -1565,7 +1622,8 @@ gi_status gi_sort_lines(gi_ctx* h) {
   cudaSetDevice(c->device);
   std::vector<gi_line> tmp;
   gi_line* L = c->h_lines;
-  if (c->lines_on_device) {
+  const bool dev = c->lines_on_device || c->compact_lines;  // the full records live there
+  if (dev) {
     tmp.resize(n);
     GI_CUDA(c, cudaMemcpy(tmp.data(), c->d_lines.p, sizeof(gi_line) * n, cudaMemcpyDeviceToHost));
     L = tmp.data();
@@ -1573,8 +1631,12 @@ gi_status gi_sort_lines(gi_ctx* h) {
   std::sort(L, L + n, [](const gi_line& a, const gi_line& b) {
     return a.level_i != b.level_i ? a.level_i < b.level_i : a.level_f < b.level_f;
   });
-  if (c->lines_on_device)
+  if (dev)
     GI_CUDA(c, cudaMemcpy(c->d_lines.p, tmp.data(), sizeof(gi_line) * n, cudaMemcpyHostToDevice));
+  if (c->compact_lines)  // one line per level pair: the same order
+    std::sort(c->h_compact, c->h_compact + n, [](const gi_line_compact& a, const gi_line_compact& b) {
+      return a.level_i != b.level_i ? a.level_i < b.level_i : a.level_f < b.level_f;
+    });
   return GI_OK;
 }
 

@@ -14,6 +14,8 @@
 //   H[s] = sum_lambda repres_F[s, idegF, lambda] * h[root(case(s), lambda)].
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "engine.h"
 #include "epilogue.cuh"
 
@@ -216,6 +218,31 @@ __global__ void k_boltz(const double* __restrict__ E, int n, double zpe, double 
                         double* __restrict__ out) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) out[k] = exp(-(E[k] - zpe) * beta);
+}
+
+// Full line records -> compact ones (the read-back of GI_RUN_COMPACT_LINES).
+__global__ void k_pack_lines(const gi_line* __restrict__ in, gi_line_compact* __restrict__ out,
+                             long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const gi_line& L = in[i];
+    gi_line_compact o;
+    o.level_i = L.level_i;
+    o.level_f = L.level_f;
+    o.nu = L.nu;
+    o.S = L.S;
+    o.A = L.A;
+    o.I = L.I;
+    out[i] = o;
+  }
+}
+
+cudaError_t launch_pack_lines(const gi_line* in, gi_line_compact* out, long long n,
+                              cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  const long long blocks = std::min<long long>((n + 255) / 256, 152 * 16);
+  k_pack_lines<<<(unsigned)blocks, 256, 0, st>>>(in, out, n);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_boltz(const double* E, int n, double zpe, double beta, double* out,

@@ -287,7 +287,16 @@ gi_status refine_lines(Ctx* c, const std::vector<RefinePart>& parts, const Refin
   const int64_t need = count + (int64_t)add.size();
   if ((size_t)need > c->d_lines.n)
     return fail(c, GI_ERR_DEVICE, "line buffer overflow after refinement");
-  if (host && c->h_lines_cap < (size_t)need) {
+  const bool compact = host && c->compact_lines;  // the host holds compact records
+  if (compact && c->h_compact_cap < (size_t)need) {
+    gi_line_compact* nh = nullptr;
+    GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&nh), sizeof(gi_line_compact) * need));
+    if (count) memcpy(nh, c->h_compact, sizeof(gi_line_compact) * count);
+    if (c->h_compact) cudaFreeHost(c->h_compact);
+    c->h_compact = nh;
+    c->h_compact_cap = need;
+  }
+  if (host && !compact && c->h_lines_cap < (size_t)need) {
     gi_line* nh = nullptr;
     GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&nh), sizeof(gi_line) * need));
     if (count) memcpy(nh, c->h_lines, sizeof(gi_line) * count);
@@ -297,7 +306,10 @@ gi_status refine_lines(Ctx* c, const std::vector<RefinePart>& parts, const Refin
   }
   auto put = [&](int64_t slot, const gi_line& L) -> gi_status {
     GI_CUDA(c, cudaMemcpy(d + slot, &L, sizeof(gi_line), cudaMemcpyHostToDevice));
-    if (host) c->h_lines[slot] = L;
+    if (compact)
+      c->h_compact[slot] = gi_line_compact{L.level_i, L.level_f, L.nu, L.S, L.A, L.I};
+    else if (host)
+      c->h_lines[slot] = L;
     return GI_OK;
   };
   for (size_t k = 0; k < upd.size(); k++) {
@@ -314,7 +326,7 @@ gi_status refine_lines(Ctx* c, const std::vector<RefinePart>& parts, const Refin
     const int64_t last = --count;
     if (slot != last) {
       gi_line L;
-      if (host) {
+      if (host && !compact) {
         L = c->h_lines[last];
       } else {
         GI_CUDA(c, cudaMemcpy(&L, d + last, sizeof(gi_line), cudaMemcpyDeviceToHost));

@@ -102,14 +102,17 @@ static size_t block_budget(const Server* s) {
 }
 
 // Moves a block's vectors to pinned host memory and frees its device arrays
-// (the digits are recut when it comes back).
+// (the digits are recut when it comes back).  A host copy of the same
+// version, kept from an earlier eviction, makes this free.
 static gi_status evict(Ctx* c, Block& b) {
   if (!b.resident) return GI_OK;
   const size_t n = (size_t)b.nvec * b.nsize;
-  if (n) {
-    GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&b.h_vecs), sizeof(double) * n));
+  if (n && !(b.h_vecs && b.h_version == b.version)) {
+    if (!b.h_vecs)
+      GI_CUDA(c, cudaMallocHost(reinterpret_cast<void**>(&b.h_vecs), sizeof(double) * n));
     GI_CUDA(c, cudaMemcpy2D(b.h_vecs, sizeof(double) * b.nsize, b.d_vecs.p, sizeof(double) * b.ld,
                             sizeof(double) * b.nsize, b.nvec, cudaMemcpyDeviceToHost));
+    b.h_version = b.version;
   }
   b.d_vecs.reset();
   b.d_digits.reset();
@@ -129,9 +132,7 @@ static gi_status restore(Ctx* c, Block& b) {
     GI_CUDA(c, cudaMemcpy2D(b.d_vecs.p, sizeof(double) * b.ld, b.h_vecs, sizeof(double) * b.nsize,
                             sizeof(double) * b.nsize, b.nvec, cudaMemcpyHostToDevice));
   GI_CUDA(c, cudaStreamSynchronize(cudaStreamLegacy));
-  if (b.h_vecs) cudaFreeHost(b.h_vecs);
-  b.h_vecs = nullptr;
-  b.resident = true;
+  b.resident = true;  // h_vecs stays: the next eviction of this version is free
   c->server->restores++;
   return GI_OK;
 }
@@ -155,8 +156,9 @@ gi_status server_make_room(Ctx* c, size_t bytes, Block* keep) {
   const size_t cap = block_budget(s);
   size_t used = resident_bytes(c);
   while (used + bytes > cap) {
-    // the least recently used of the unpinned blocks and cached Z; a cached Z
-    // is dropped (recomputed when a job needs it), a block moves to host
+    // the least recently used of the unpinned blocks and cached Z (one clock
+    // for both); a cached Z is dropped (recomputed when a job needs it), a
+    // block moves to pinned host memory
     Block* victim = nullptr;
     for (auto& kv : c->blocks) {
       Block* b = kv.second.get();
@@ -169,9 +171,7 @@ gi_status server_make_room(Ctx* c, size_t bytes, Block* keep) {
       if (e.pins > 0) continue;
       if (zv == s->zcache.size() || e.last_use < s->zcache[zv]->last_use) zv = k;
     }
-    // cached Z go before blocks: a Z is recomputed on the GPU, a block comes
-    // back over the host link and has its digit planes cut again
-    if (zv < s->zcache.size()) {
+    if (zv < s->zcache.size() && (!victim || s->zcache[zv]->last_use < victim->last_use)) {
       s->zcache.erase(s->zcache.begin() + zv);
       s->z_evictions++;
     } else if (victim) {

@@ -105,11 +105,14 @@ __device__ __forceinline__ uint64_t gtimer() {
 // raises the abort itself and records the error).
 // `sleep_ns` backs the poll off so that a waiting warp leaves the issue slots of
 // its SM sub-partition to the MMA-issuing warp.
+// CL: cluster-scope acquire (barriers that the peer CTA of a pair completes).
+__device__ __forceinline__ uint32_t mbar_try_cl(uint64_t* b, uint32_t parity);
+template <bool CL = false>
 __device__ bool mbar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err,
                           int code, unsigned sleep_ns = 0) {
   uint64_t t0 = 0;
   for (uint32_t it = 1;; ++it) {
-    if (mbar_try(b, parity)) return true;
+    if (CL ? mbar_try_cl(b, parity) : mbar_try(b, parity)) return true;
     if (sleep_ns) __nanosleep(sleep_ns);
     if ((it & 63) == 0) {
       if (*abort_flag) return false;
@@ -202,6 +205,65 @@ __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
           sptr(bar))
+      : "memory");
+}
+// ---- the 2-SM pair (cta_group::2): a cluster of two CTAs on one TPC, the
+// MMA issued by rank 0 over both CTAs' shared memory (rows 0-127 of A and the
+// first half of B's rows from rank 0, the rest from rank 1, at the same
+// offsets), each CTA's tensor memory holding its 128 rows of the product.
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+// The shared::cluster address of the same shared-memory location in CTA `rank`.
+__device__ __forceinline__ uint32_t mapa_shared(uint32_t addr, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(addr), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void cluster_sync_all() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\nbarrier.cluster.wait.acquire.aligned;\n" ::
+                   : "memory");
+}
+// Try-wait with cluster-scope acquire: phases completed by the peer CTA's
+// arrivals or TMA bytes.
+__device__ __forceinline__ uint32_t mbar_try_cl(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(sptr(b)), "r"(parity)
+      : "memory");
+  return ok;
+}
+__device__ __forceinline__ void mbar_arrive_cl(uint32_t bar_cluster) {
+  asm volatile("mbarrier.arrive.release.cluster.shared::cluster.b64 _, [%0];\n" ::"r"(bar_cluster)
+               : "memory");
+}
+// TMA into this CTA's shared memory, completing its bytes on a barrier of
+// either CTA of the pair (bar_cluster: a shared::cluster address).
+__device__ __forceinline__ void tma_load_3d_pair(void* dst, const CUtensorMap* map,
+                                                 uint32_t bar_cluster, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes.cta_group::2"
+      " [%0], [%1, {%3, %4, %5}], [%2];\n" ::"r"(sptr(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(bar_cluster), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+__device__ __forceinline__ void mma_bf16_pair(uint32_t tmem_d, uint64_t a, uint64_t b,
+                                              uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::2.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+// Completion of the pair's MMAs so far, on one barrier (own or peer's).
+__device__ __forceinline__ void mma_commit_pair(uint32_t bar_cluster) {
+  asm volatile(
+      "tcgen05.commit.cta_group::2.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
+          bar_cluster)
       : "memory");
 }
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
@@ -593,7 +655,16 @@ __device__ __forceinline__ void tmem_wait_ld() {
 
 // ACC: add to C (the later launches of a K-segmented GEMM); a template
 // argument, so the first launch's code carries no trace of it.
-template <int S, int BN, int D1, bool ACC, bool KPARTS = false>
+// PAIR: the tile is 256 x BN, computed by a cluster of two CTAs with
+// tcgen05.mma.cta_group::2 (M = 256).  Each CTA loads its 128 rows of A and
+// BN/2 rows of B; rank 0 waits for both CTAs' bytes on its own barriers (the
+// rank-1 loads complete there), issues the MMAs and commits them to the
+// barriers of both CTAs; both CTAs' epilogue warps read their own tensor
+// memory (the tile's rows rank * 128 + lane, all BN columns).  Per SM, one
+// MMA step reads 128 + BN/2 operand rows from shared memory instead of
+// 128 + BN: the single-CTA kernel at BN = 96 is bound by that bandwidth.
+constexpr int kStagesP = 4;
+template <int S, int BN, int D1, bool ACC, bool KPARTS = false, bool PAIR = false>
 __global__ void __launch_bounds__(kThreadsG, 1)
     k_split_gemm_g(const __grid_constant__ CUtensorMap tmAq, const __grid_constant__ CUtensorMap tmAt,
                    const __grid_constant__ CUtensorMap tmBq, const __grid_constant__ CUtensorMap tmBt,
@@ -604,20 +675,22 @@ __global__ void __launch_bounds__(kThreadsG, 1)
   constexpr int NPASS = D1 < S ? 2 : 1;
   constexpr int HALF = BN / 2;                     // columns per epilogue warp
   constexpr int NCH = HALF / kChunkG;              // chunks per epilogue warp
+  constexpr int BNL = PAIR ? BN / 2 : BN;          // B rows this CTA loads
   static_assert(D1 * BN <= 512 && (S - D1) * BN <= 512, "tensor memory columns");
-  static_assert((BN * 128) % 1024 == 0, "128-byte-swizzle tiles stay 1024-byte aligned");
+  static_assert((BNL * 128) % 1024 == 0, "128-byte-swizzle tiles stay 1024-byte aligned");
   static_assert(HALF % kChunkG == 0, "epilogue chunks");
+  static_assert(!PAIR || (NPASS == 2 && !KPARTS && BN % 32 == 0), "pair: two-pass tiles");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  constexpr uint32_t kAq = kBM * 128, kAt = kBM * 32, kBq = BN * 128, kBt = BN * 32;
+  constexpr uint32_t kAq = kBM * 128, kAt = kBM * 32, kBq = BNL * 128, kBt = BNL * 32;
   constexpr uint32_t kAbytes = NQ * kAq + NT * kAt;
-  constexpr uint32_t kStage = stage_bytes_g(S, BN);  // rounded up to 1024 bytes
+  constexpr uint32_t kStage = stage_bytes_g(S, BNL);  // rounded up to 1024 bytes
   static_assert(kAbytes % 1024 == 0 && kStage >= kAbytes + NQ * kBq + NT * kBt, "stage layout");
   // pass 0 of a two-pass tile: D1 <= 4 planes are group 0 alone; two K slices
   // of it share a slot when they fit
   constexpr int PK = (NPASS == 2 && D1 <= 4 && 2 * (kAq + kBq) <= kStage) ? 2 : 1;
-  constexpr int ST = kStages2;
+  constexpr int ST = PAIR ? kStagesP : kStages2;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + ST * kStage);
   uint64_t* empty = full + ST;
   uint64_t* accf = empty + ST;
@@ -626,12 +699,16 @@ __global__ void __launch_bounds__(kThreadsG, 1)
   volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int t = blockIdx.x;
+  const uint32_t rank = PAIR ? cluster_rank() : 0u;
+  const int t = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
   const int grp = t / (GA * nN);
   const int r = t - grp * GA * nN;
   const int gsz = min(GA, nA - grp * GA);
   const int ai = grp * GA + r % gsz;
-  const int n0 = (r / gsz) * BN, m0 = (ai % nM) * kBM, z = ai / nM;
+  // a pair's tile has 256 rows (nM counts 256-row tiles); this CTA's are the
+  // rank-th 128 of them
+  const int n0 = (r / gsz) * BN, z = ai / nM;
+  const int m0 = (ai % nM) * (PAIR ? 2 * kBM : kBM) + (int)rank * kBM;
   // K parts (grid y): part p contracts K steps [p * kpart_steps, ...) into its
   // own output C + p * strideP (kpart_steps = 0: one part, the whole K)
   const int kb0 = KPARTS ? (int)blockIdx.y * kpart_steps : 0;
@@ -646,76 +723,117 @@ __global__ void __launch_bounds__(kThreadsG, 1)
     }
     mbar_init(&accf[0], 1);
     mbar_init(&accf[1], 1);
-    mbar_init(tfree, 256);
+    mbar_init(tfree, PAIR ? 2 * 8 : 256);  // a pair: one arrival per epilogue warp of both CTAs
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
   if (warp == 1) {
-    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
-                     sptr(tmem_slot)));
-    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    if constexpr (PAIR) {
+      asm volatile("tcgen05.alloc.cta_group::2.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                       sptr(tmem_slot)));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::2.sync.aligned;\n");
+    } else {
+      asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], 512;\n" ::"r"(
+                       sptr(tmem_slot)));
+      asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n");
+    }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
+  // a pair: both CTAs' barriers are initialised before either signals the other's
+  if constexpr (PAIR) cluster_sync_all();
   asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
   const uint32_t tmem = *tmem_slot;
+  // rank 0's barrier of a slot, as a shared::cluster address (pairs)
+  auto lead = [&](uint64_t* b) -> uint32_t { return PAIR ? mapa_shared(sptr(b), 0) : sptr(b); };
 
   if (warp == 0) {
     if (lane == 0) {  // TMA producer: both passes, one continuous slot ring
       int issued = 0;
+      auto load = [&](void* dst, const CUtensorMap* map, int st, int c0, int c1, int c2) {
+        if constexpr (PAIR) tma_load_3d_pair(dst, map, lead(&full[st]), c0, c1, c2);
+        else tma_load_3d(dst, map, &full[st], c0, c1, c2);
+      };
+      // rank 0 expects the bytes of both CTAs (equal boxes); rank 1's loads
+      // complete on rank 0's barrier, before or after that expectation
+      auto expect = [&](int st, uint32_t bytes) {
+        if (rank == 0) mbar_expect_tx(&full[st], PAIR ? 2 * bytes : bytes);
+      };
+      const int nb0 = n0 + (int)rank * BNL;  // this CTA's B rows
       for (int it = 0; it < nslots; ++it) {
         const int pass = it >= nk0, st = it % ST;
-        if (it >= ST && !mbar_wait(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 21))
+        if (it >= ST && !mbar_wait<PAIR>(&empty[st], ((it / ST) - 1) & 1, abort_flag, err, 21))
           break;
         unsigned char* sa = smem + st * kStage;
         if (pass == 0 && PK == 2) {
-          mbar_expect_tx(&full[st], 2 * (kAq + kBq));
+          expect(st, 2 * (kAq + kBq));
           for (int h = 0; h < 2; ++h) {
             const int kb = kb0 + 2 * it + h;
             unsigned char* sh = sa + h * (kAq + kBq);
-            tma_load_3d(sh, &tmAq, &full[st], kb * 64, z * Mpad + m0, 0);
-            tma_load_3d(sh + kAq, &tmBq, &full[st], kb * 64, n0, 0);
+            load(sh, &tmAq, st, kb * 64, z * Mpad + m0, 0);
+            load(sh + kAq, &tmBq, st, kb * 64, nb0, 0);
           }
         } else {
           const int kb = kb0 + (pass ? it - nk0 : it);
           const int np = pass ? S : D1;
           const int gq = min(NQ, (np + 3) / 4), tq = max(0, np - 4 * NQ);
           unsigned char* sb = sa + kAbytes;
-          mbar_expect_tx(&full[st], gq * (kAq + kBq) + tq * (kAt + kBt));
+          expect(st, gq * (kAq + kBq) + tq * (kAt + kBt));
           for (int g = 0; g < gq; ++g) {
-            tma_load_3d(sa + g * kAq, &tmAq, &full[st], kb * 64, z * Mpad + m0, g);
-            tma_load_3d(sb + g * kBq, &tmBq, &full[st], kb * 64, n0, g);
+            load(sa + g * kAq, &tmAq, st, kb * 64, z * Mpad + m0, g);
+            load(sb + g * kBq, &tmBq, st, kb * 64, nb0, g);
           }
           for (int q = 0; q < tq; ++q) {
-            tma_load_3d(sa + NQ * kAq + q * kAt, &tmAt, &full[st], kb * kBK, z * Mpad + m0, q);
-            tma_load_3d(sb + NQ * kBq + q * kBt, &tmBt, &full[st], kb * kBK, n0, q);
+            load(sa + NQ * kAq + q * kAt, &tmAt, st, kb * kBK, z * Mpad + m0, q);
+            load(sb + NQ * kBq + q * kBt, &tmBt, st, kb * kBK, nb0, q);
           }
         }
         issued = it + 1;
       }
       if (*abort_flag) {
-        for (int it = (issued > ST ? issued - ST : 0); it < issued; ++it) {
-          uint64_t t0 = gtimer();
-          while (!mbar_try(&full[it % ST], (it / ST) & 1) && gtimer() - t0 < 1000000000ull) {
+        if (rank == 0) {
+          for (int it = (issued > ST ? issued - ST : 0); it < issued; ++it) {
+            uint64_t t0 = gtimer();
+            while (!(PAIR ? mbar_try_cl(&full[it % ST], (it / ST) & 1)
+                          : mbar_try(&full[it % ST], (it / ST) & 1)) &&
+                   gtimer() - t0 < 1000000000ull) {
+            }
           }
+        } else {
+          // rank 1 cannot observe its loads (they complete on rank 0's
+          // barriers): give them far longer than a load takes
+          const uint64_t t0 = gtimer();
+          while (gtimer() - t0 < 2000000ull) __nanosleep(1000);
         }
       }
     }
   } else if (warp == 1) {
-    if (lane == 0) {  // MMA issuer
-      const uint32_t idesc = idesc_bf16(kBM, BN);
+    if (lane == 0 && rank == 0) {  // MMA issuer (rank 0 of a pair)
+      const uint32_t idesc = idesc_bf16(PAIR ? 2 * kBM : kBM, BN);
+      auto commit = [&](uint64_t* b) {
+        if constexpr (PAIR) {
+          mma_commit_pair(sptr(b));                   // this CTA's barrier
+          mma_commit_pair(mapa_shared(sptr(b), 1));   // and rank 1's
+        } else {
+          mma_commit(b);
+        }
+      };
+      auto mma = [&](uint32_t d, uint64_t a, uint64_t b, uint32_t idesc_, uint32_t acc) {
+        if constexpr (PAIR) mma_bf16_pair(d, a, b, idesc_, acc);
+        else mma_bf16(d, a, b, idesc_, acc);
+      };
       bool ok = true;
       int last = 0;
       for (int it = 0; it < nslots && ok; ++it) {
         const int pass = it >= nk0, st = it % ST;
         if (pass == 1 && it == nk0) {  // pass 1 reuses pass 0's tensor memory
-          mma_commit(&accf[0]);
+          commit(&accf[0]);
           last = 1;
-          ok = mbar_wait(tfree, 0, abort_flag, err, 24);
+          ok = mbar_wait<PAIR>(tfree, 0, abort_flag, err, 24);
           asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
           if (!ok) break;
         }
-        if (!mbar_wait(&full[st], (it / ST) & 1, abort_flag, err, 22)) {
+        if (!mbar_wait<PAIR>(&full[st], (it / ST) & 1, abort_flag, err, 22)) {
           ok = false;
           break;
         }
@@ -730,7 +848,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
             for (int d = 0; d < D1; ++d)
 #pragma unroll
               for (int p = 0; p <= d; ++p)
-                mma_bf16(tmem + d * BN, sdesc_sw128(a0 + p * 32), sdesc_sw128(b0 + (d - p) * 32),
+                mma(tmem + d * BN, sdesc_sw128(a0 + p * 32), sdesc_sw128(b0 + (d - p) * 32),
                          idesc, (!first || p > 0) ? 1u : 0u);
           }
         } else {
@@ -749,23 +867,24 @@ __global__ void __launch_bounds__(kThreadsG, 1)
             for (int d = 0; d < D1; ++d)
 #pragma unroll
               for (int p = 0; p <= d; ++p)
-                mma_bf16(tmem + d * BN, adesc(p), bdesc(d - p), idesc,
+                mma(tmem + d * BN, adesc(p), bdesc(d - p), idesc,
                          (kb > 0 || p > 0) ? 1u : 0u);
           } else {
 #pragma unroll
             for (int d = D1; d < S; ++d)
 #pragma unroll
               for (int p = 0; p <= d; ++p)
-                mma_bf16(tmem + (d - D1) * BN, adesc(p), bdesc(d - p), idesc,
+                mma(tmem + (d - D1) * BN, adesc(p), bdesc(d - p), idesc,
                          (kb > 0 || p > 0) ? 1u : 0u);
           }
         }
-        mma_commit(&empty[st]);
+        commit(&empty[st]);
       }
-      if (ok) mma_commit(&accf[NPASS - 1]);
+      if (ok) commit(&accf[NPASS - 1]);
       if (*abort_flag) {
         uint64_t t0 = gtimer();
-        while (!mbar_try(&accf[last], 0) && gtimer() - t0 < 1000000000ull) {
+        while (!(PAIR ? mbar_try_cl(&accf[last], 0) : mbar_try(&accf[last], 0)) &&
+               gtimer() - t0 < 1000000000ull) {
         }
       }
     }
@@ -779,7 +898,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
     long long v0[NCH][kChunkG];  // pass 0's exact sums of this thread's columns
     bool ok = true;
     for (int pass = 0; pass < NPASS && ok; ++pass) {
-      ok = mbar_wait(&accf[pass], 0, abort_flag, err, 23, 256);
+      ok = mbar_wait<PAIR>(&accf[pass], 0, abort_flag, err, 23, 256);
       asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
       if (!ok) break;
       const int d0 = pass ? D1 : 0, d1 = pass ? S : D1;
@@ -833,15 +952,26 @@ __global__ void __launch_bounds__(kThreadsG, 1)
       }
       if (pass == 0 && NPASS == 2) {  // all reads done: pass 1 may overwrite the columns
         asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
-        asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
+        if constexpr (PAIR) {  // one arrival per warp, on rank 0's barrier
+          __syncwarp();
+          if (lane == 0) mbar_arrive_cl(lead(tfree));
+        } else {
+          asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(sptr(tfree)) : "memory");
+        }
       }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory");
   __syncthreads();
+  // a pair: neither CTA frees its tensor memory or exits (its shared memory
+  // and barriers) while the other may still address them
+  if constexpr (PAIR) cluster_sync_all();
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+    if constexpr (PAIR)
+      asm volatile("tcgen05.dealloc.cta_group::2.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
+    else
+      asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, 512;\n" ::"r"(tmem));
   }
 }
 
@@ -1501,7 +1631,9 @@ struct GemmConfig {
   int kind = 1;  // 0: k_split_gemm (one pass); 1, 2: k_split_gemm2 (two passes,
                  // diagonals split at s/2 or s - s/2); these read the plain
                  // layout.  6, 7, 8: k_split_gemm_g on the grouped layout (two
-                 // passes split at s/2 or s - s/2, or one pass).  3-5 are unused.
+                 // passes split at s/2 or s - s/2, or one pass); 9: its 2-SM
+                 // pair form (256-row tiles, two passes split at s/2, s = 9).
+                 // 3-5 are unused.
   int ga_mb = 64;
 };
 
@@ -1517,6 +1649,10 @@ size_t smemg_bytes(int s, int bn) {
   const size_t need = (size_t)kStages2 * stage_bytes_g(s, bn) + 1024 + 256;
   return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;  // one CTA per SM
 }
+// the 2-SM pair: each CTA stages 128 A rows and bn/2 B rows, in kStagesP slots
+size_t smemp_bytes(int s, int bn) {
+  return (size_t)kStagesP * stage_bytes_g(s, bn / 2) + 1024 + 256;
+}
 size_t smem2_bytes(int s, int bn) {
   const size_t need = (size_t)kStages2 * s * (kBM + bn) * kBK * 2 + 1024 + 256;
   return need < (size_t)120 * 1024 ? (size_t)120 * 1024 : need;  // one CTA per SM
@@ -1526,7 +1662,8 @@ int tile_n(int s, int kind) { return (kind == 0 || kind == 8) ? bn_for(s) : bn2_
 // Kernels that read the context's digit layout (grouped needs s >= 4; below
 // that the grouped layout is the plain one).
 bool kind_valid(int s, int kind, bool grouped) {
-  if (grouped && s >= 4) return kind == 6 || kind == 8 || (kind == 7 && (s & 1));
+  if (grouped && s >= 4)
+    return kind == 6 || kind == 8 || (kind == 7 && (s & 1)) || (kind == 9 && s == 9);
   return kind == 0 || kind == 1 || (kind == 2 && (s & 1));
 }
 GemmConfig default_config(int s, bool grouped) {
@@ -1589,6 +1726,9 @@ cudaError_t set_attributes() {
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)smemg_bytes(S, BN2));
         if (status == cudaSuccess)
+          status = set_smem(k_split_gemm_g<S, BN2, D1, false, false, true>, smemp_bytes(S, BN2),
+                            k_split_gemm_g<S, BN2, D1, true, false, true>);
+        if (status == cudaSuccess)
           status = cudaFuncSetAttribute(k_build_y_digits<S>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(kFusedYMaxKp * sizeof(double)));
@@ -1629,6 +1769,29 @@ cudaError_t launch_gemm(const GemmConfig& cfg, const Maps& mp, const int32_t* ea
   // row tiles per L2 group: their digit planes (128 x K x S bf16 each) within ga_mb MB
   const size_t a_tile = (size_t)kBM * K * S * 2;
   const int GA = std::max(1, std::min(nA, (int)(((size_t)cfg.ga_mb << 20) / a_tile)));
+  if constexpr (S == 9) {
+    if (cfg.kind == 9) {  // 2-SM pairs: clusters of two CTAs, 256-row tiles
+      if (kparts > 1) return cudaErrorInvalidValue;
+      const int nM2 = (M + 2 * kBM - 1) / (2 * kBM), nA2 = nM2 * batch;
+      const int GA2 = std::max(1, std::min(nA2, (int)(((size_t)cfg.ga_mb << 20) / (2 * a_tile))));
+      cudaLaunchConfig_t lc = {};
+      lc.gridDim = dim3((unsigned)(2 * nA2 * nN));
+      lc.blockDim = dim3(kThreadsG);
+      lc.dynamicSmemBytes = smemp_bytes(S, BN2);
+      lc.stream = st;
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = 2;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      lc.attrs = at;
+      lc.numAttrs = 1;
+      auto kern = accum ? k_split_gemm_g<S, BN2, D1, true, false, true>
+                        : k_split_gemm_g<S, BN2, D1, false, false, true>;
+      return cudaLaunchKernelEx(&lc, kern, mp.a, mp.at, mp.b, mp.bt, ea, eb, C, ldc, strideC, M,
+                                Mpad, Nc, K, w, nM2, nA2, nN, GA2, err, 0, (size_t)0);
+    }
+  }
   if constexpr (S >= 4) {
     if (cfg.kind >= 6 && cfg.kind <= 8) {
       const dim3 grid((unsigned)(nA * nN), (unsigned)std::max(kparts, 1));
@@ -1827,7 +1990,8 @@ static Tuner& tuner() {
 }
 static const GemmConfig kCandidates[] = {{1, 64}, {1, 32}, {1, 128}, {1, 16}, {2, 64},
                                          {2, 32}, {0, 64}, {0, 32}, {6, 64}, {6, 32},
-                                         {6, 128}, {7, 64}, {7, 32}, {8, 64}, {8, 32}};
+                                         {6, 128}, {7, 64}, {7, 32}, {8, 64}, {8, 32},
+                                         {9, 64}, {9, 32}, {9, 128}};
 
 static void tune_load(Tuner& t, const std::string& path) {
   t.loaded = path;
@@ -1872,6 +2036,7 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
   c->stats.kernel_launches += nseg - 1;
   auto run = [&](const GemmConfig& g) -> cudaError_t {
     const int bn = tile_n(S->s, g.kind);
+    const int bbox = g.kind == 9 ? bn / 2 : bn;  // B rows one CTA loads
     for (int k0 = 0; k0 < K; k0 += kKSeg) {
       const int Kc = std::min(kKSeg, K - k0);
       Maps mp;
@@ -1881,11 +2046,11 @@ static gi_status gemm(Ctx* c, const uint16_t* Aslices, int Arows_total, const in
         const uint16_t* At = Aslices + (size_t)4 * nq * Arows_total * K + k0;
         const uint16_t* Bt = Bslices + (size_t)4 * nq * Brows * K + k0;
         if (!make_map_groups(&mp.a, Aslices + (size_t)4 * k0, Kc, Arows_total, nq, kBM, K) ||
-            !make_map_groups(&mp.b, Bslices + (size_t)4 * k0, Kc, Brows, nq, bn, K))
+            !make_map_groups(&mp.b, Bslices + (size_t)4 * k0, Kc, Brows, nq, bbox, K))
           return cudaErrorInvalidValue;
         if (nt) {
           if (!make_map(&mp.at, At, Kc, Arows_total, nt, kBM, 1, K) ||
-              !make_map(&mp.bt, Bt, Kc, Brows, nt, bn, 1, K))
+              !make_map(&mp.bt, Bt, Kc, Brows, nt, bbox, 1, K))
             return cudaErrorInvalidValue;
         } else {
           mp.at = mp.a;  // no plain planes: never read

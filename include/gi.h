@@ -102,6 +102,13 @@ typedef struct {
   double t[4]; /* transition moments, Debye: t[ideg_i + 2*ideg_f] */
 } gi_line;
 
+/* The compact form of a line (GI_RUN_COMPACT_LINES): the fields a line list
+   needs, 40 bytes instead of 80 (no degeneracies, no transition moments). */
+typedef struct {
+  int32_t level_i, level_f;
+  double nu, S, A, I;
+} gi_line_compact;
+
 /* One level (TO_PTeigen, trove_objects.h:113-127). */
 typedef struct {
   int32_t J, gamma;
@@ -247,6 +254,9 @@ gi_status gi_set_block_device(gi_ctx* ctx, int J, int gamma, int nsize, int nvec
                                     the first run of a plan, replayed while the plan (blocks,
                                     parameters, sizes, buffers) is unchanged; ignored with
                                     GI_RUN_PHASE_TIMING */
+#define GI_RUN_COMPACT_LINES 8   /* the lines read back to host memory during the run are
+                                    gi_line_compact records (half the bytes); read them
+                                    with gi_get_lines_compact */
 /* Computes every line of the job (all loaded J; |dJ| <= 1; the reference's
    filters).  *nlines receives the count. */
 gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);
@@ -260,6 +270,12 @@ gi_status gi_run(gi_ctx* ctx, int flags, int64_t* nlines);
    gi_run(ctx, flags, n) is gi_run_shard(ctx, flags, 0, 1, n). */
 gi_status gi_run_shard(gi_ctx* ctx, int flags, int shard, int nshards, int64_t* nlines);
 gi_status gi_get_lines(gi_ctx* ctx, int64_t offset, int64_t count, gi_line* out);
+/* The last run's lines as compact records.  After a run with
+   GI_RUN_COMPACT_LINES (and without GI_RUN_LINES_ON_DEVICE) they are already
+   in host memory; otherwise they are converted from the full records.
+   gi_get_lines still returns the full records after a compact run (copied
+   from device memory, where the full records stay until the next run). */
+gi_status gi_get_lines_compact(gi_ctx* ctx, int64_t offset, int64_t count, gi_line_compact* out);
 /* Orders the last run's lines by (initial level, final level), the order of
    the reference's single-device loop (cuda_host.cu:1174-1473); the run
    itself appends lines in the order its blocks finish. */

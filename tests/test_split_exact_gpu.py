@@ -14,8 +14,8 @@ import pytest
 
 pytestmark = pytest.mark.gpu
 
-KINDS = ["6:64", "7:64", "8:64"]
-PLAIN = ["0:64", "1:64", "2:64", "3:64", "4:64", "5:64"]
+KINDS = ["9:64", "6:64", "7:64", "8:64"]  # 9: the 2-SM pair (cta_group::2)
+PLAIN = ["0:64", "1:64", "2:64"]
 
 
 def rel_err(got, want):

@@ -64,17 +64,18 @@ def test_autotuner_table_and_results(pkg, synth, tmp_path, monkeypatch):
         got = np.sort(eng.lines(), order=["level_i", "level_f"])
     rows = [l.split() for l in open(path).read().splitlines()]
     assert len(rows) >= 2 and all(len(r) == 8 for r in rows)
-    assert all(r[5] in ("6", "7", "8") for r in rows)  # the grouped layout's kernels
+    assert all(r[5] in ("6", "7", "8", "9") for r in rows)  # the grouped layout's kernels
     assert np.array_equal(got[["level_i", "level_f"]], ref[["level_i", "level_f"]])
     assert np.allclose(got["S"], ref["S"], rtol=1e-12, atol=0)
 
 
-@pytest.mark.parametrize("config", ["plain/0:64", "plain/1:16", "plain/1:128", "plain/1:1",
-                                    "plain/2:32", "grouped/6:64", "grouped/6:1", "grouped/7:32",
-                                    "grouped/8:64"])
+@pytest.mark.parametrize("config", ["grouped/9:64", "grouped/9:1", "plain/0:64", "plain/1:16",
+                                    "plain/1:128", "plain/1:1", "plain/2:32", "grouped/6:64",
+                                    "grouped/6:1", "grouped/7:32", "grouped/8:64"])
 def test_every_split_kernel_matches_oracle(pkg, synth, oracle, monkeypatch, config):
     """Each launch configuration the autotuner can pick (one-pass, two-pass at
-    either split point, the grouped-layout kernels, several L2 groups), pinned
+    either split point, the grouped-layout kernels and their 2-SM pair form,
+    several L2 groups), pinned
     with GI_SPLIT_FORCE on its digit layout.  Row and column tile counts are
     odd here, so tiles past the edge run too."""
     layout, force = config.split("/")
@@ -86,8 +87,8 @@ def test_every_split_kernel_matches_oracle(pkg, synth, oracle, monkeypatch, conf
     print(config, res)
 
 
-@pytest.mark.parametrize("config", ["plain/0:64", "plain/1:64", "plain/2:64", "grouped/6:64",
-                                    "grouped/7:64", "grouped/8:64"])
+@pytest.mark.parametrize("config", ["grouped/9:64", "plain/0:64", "plain/1:64", "plain/2:64",
+                                    "grouped/6:64", "grouped/7:64", "grouped/8:64"])
 def test_every_split_kernel_large_k(pkg, synth, monkeypatch, config):
     """Each configuration at contraction lengths of 1216 (half line strength)
     to ~2100 (final states), where the exact integer diagonal sums reach the
