@@ -74,6 +74,40 @@ struct StencilTerm {
   double coef;
 };
 
+// One H build of a batched launch (launch_build_h's arguments); blk0 is its
+// first block in the launch's 1-D grid, nblk its blocks (ldh/256 per kHCols
+// of its ncol initial columns).
+constexpr int kHCols = 16;  // initial columns per block of the batched H build
+struct HItem {
+  const double* Z;
+  size_t zc;
+  int ldz, nslotI, ndegF, nsizeF, ldh, Ntot, st_max, ncol;
+  const int32_t *s_case, *case_ptr, *case_roots, *root_v, *root_key, *root_lam;
+  const double* rep;
+  const StencilTerm* st;
+  const int32_t* st_n;
+  double* H;
+  long long blk0, nblk;
+};
+// One unit's Y rows of a batched digit build (split_build_y_digits' arguments):
+// rows [row0, row0 + rows) of the round's Y.
+struct YItem {
+  const double* vecs;
+  const int32_t* ivec;
+  const int32_t *yptr, *yroot, *root_case, *root_lam, *case_iterm, *case_nelem;
+  const double* rep;
+  int ld, ndeg, Ntot, nslot;
+  long long row0, rows;
+};
+// The column norms of several H in one launch: item k's columns are
+// [col0, col0 + ncol) of the grid.
+struct NormItem {
+  const double* H;
+  double* out;
+  int ldh, n;
+  long long col0, ncol;
+};
+
 // A line handed to the exact re-evaluation: initial vector i of the part's
 // unit, final record f, and its slot in the line list (-1: not kept).
 struct RefineRec {
@@ -296,6 +330,9 @@ struct Ctx {
   DevArray<double> w_hn;       // H column norms of a group of final blocks
   DevArray<double> w_BI;       // Boltzmann factors of the run's initial levels
   DevArray<EpiPart> w_epi;     // parts of the fused epilogue
+  DevArray<HItem> w_hitems;    // the H builds of every group (one launch per group)
+  DevArray<NormItem> w_nitems; // the H column norms of every group
+  DevArray<YItem> w_yitems;    // the Y digit builds of every round (one launch per round)
   DevArray<RefineRec> w_rec;   // lines handed to the exact re-evaluation
   int64_t refine_max = 0;      // doubtful lines re-evaluated per run (gi_set_refine)
   DevArray<int32_t> w_stencil_n, w_levelI, w_levelF;
@@ -386,6 +423,13 @@ cudaError_t launch_build_h(const double* Z, size_t zstride_c, int ldz, int nslot
                            int nI, const Basis& bF, int gammaF, int degF, int nsizeF, int ldh,
                            const StencilTerm* st, const int32_t* st_n, int st_max, double* H,
                            cudaStream_t s);
+HItem make_h_item(const double* Z, size_t zstride_c, int ldz, int nslotI, int ndegI, int nI,
+                  const Basis& bF, int gammaF, int degF, int nsizeF, int ldh,
+                  const StencilTerm* st, const int32_t* st_n, int st_max, double* H,
+                  long long blk0);
+// Every item of a device table in one launch (nblocks = the items' blocks).
+cudaError_t launch_build_h_items(const HItem* items, int nitems, long long nblocks,
+                                 cudaStream_t st);
 cudaError_t launch_half_ls_prim(const double* Z, size_t zstride_c, int ldz, const Basis& bF,
                                 const StencilTerm* st, const int32_t* st_n, int st_max,
                                 double* h, cudaStream_t s);
@@ -434,6 +478,9 @@ cudaError_t launch_epilogue(const double* T, int ldt, int nI, int nF, const int3
 // out[col] = || H[col * ldh + 0 .. n) ||_2 for col < ncol.
 cudaError_t launch_col_norms(const double* H, int ldh, int n, int ncol, double* out,
                              cudaStream_t s);
+// The same for the H of several final blocks in one launch (NormItem).
+cudaError_t launch_col_norms_items(const NormItem* items, int nitems, long long ncol,
+                                   cudaStream_t s);
 // C[z][n*ldc + m] = sum_k A[z][m*lda + k] * B[n*ldb + k]; K multiple of 16.
 cudaError_t gemm_fp64_nt(const double* A, int lda, size_t strideA, const double* B, int ldb,
                          double* C, int ldc, size_t strideC, int M, int Nc, int K, int batch,

@@ -941,6 +941,94 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     ~ZRelease() { zcache_release(c, *r, ok); }
   } zrelease{c, &zref};
 
+  // The H builds and the H column norms of each group as device work lists,
+  // one launch each per group (GI_BATCH_SMALL=0: one launch per item); the
+  // lists are uploaded before any capture, at addresses the plan keeps
+  struct GroupLists {
+    int h0 = 0, hn = 0, n0 = 0, nn = 0;
+    long long hblocks = 0, ncols = 0;
+  };
+  std::vector<std::vector<GroupLists>> glists(rounds.size());
+  std::vector<std::pair<int, int>> ylists(rounds.size(), {0, 0});  // Y digit items per round
+  const char* bs_env = getenv("GI_BATCH_SMALL");
+  const bool batch_small = !(bs_env && bs_env[0] == '0');
+  if (batch_small) {
+    std::vector<HItem> hitems;
+    std::vector<NormItem> nitems;
+    std::vector<YItem> yitems;
+    for (size_t r = 0; r < rounds.size(); r++) {
+      const Round& R = rounds[r];
+      if (fused_y && !zref.hit) {  // the round's Y rows, unit by unit
+        ylists[r].first = (int)yitems.size();
+        for (const Unit& u : R.units) {
+          const Block& b = *u.I->blk;
+          const Basis& bI = *c->bases[b.J];
+          const int ndegI = c->degen[b.gamma];
+          YItem y{};
+          y.vecs = b.d_vecs.p;
+          y.ivec = c->w_ivec.p + 2 * u.off;
+          y.yptr = bI.d_yptr.p;
+          y.yroot = bI.d_yroot.p;
+          y.root_case = bI.d_root_case.p;
+          y.root_lam = bI.d_root_lam.p;
+          y.case_iterm = bI.d_case_iterm[b.gamma].p;
+          y.case_nelem = bI.d_case_nelem[b.gamma].p;
+          y.rep = bI.d_rep[b.gamma].p;
+          y.ld = b.ld;
+          y.ndeg = ndegI;
+          y.Ntot = bI.Ntotal[b.gamma];
+          y.nslot = bI.nslot;
+          y.row0 = (long long)u.ycol;
+          y.rows = (long long)u.nI * ndegI * bI.nslot;
+          if (y.rows) yitems.push_back(y);
+        }
+        ylists[r].second = (int)yitems.size() - ylists[r].first;
+      }
+      double* zbase = zref.z ? zref.z + zoff[r] * Kp : c->w_z.p;
+      const size_t zc = (zref.z ? ztotal : R.ncolY) * Kp;
+      for (const auto& grp : groups[r]) {
+        GroupLists gl;
+        gl.h0 = (int)hitems.size();
+        for (size_t t = grp.first; t < grp.second; t++) {
+          const Target& T = targets[r][t];
+          const Block& fb = *T.F->blk;
+          const Basis& bF = *c->bases[fb.J];
+          for (size_t k = 0; k < T.parts.size(); k++) {
+            const Unit& u = *T.parts[k].first;
+            const PairPlan* pp = T.parts[k].second;
+            const HItem it = make_h_item(
+                zbase + u.ycol * Kp, zc, Kp, c->bases[u.I->blk->J]->nslot,
+                c->degen[u.I->blk->gamma], u.nI, bF, fb.gamma, c->degen[fb.gamma], fb.nsize,
+                fb.ld, c->w_stencil.p + pp->st_off * 6, c->w_stencil_n.p + pp->st_off, 6,
+                c->w_h.p + T.hoff + T.hcol[k] * fb.ld, gl.hblocks);
+            if (it.nblk == 0) continue;
+            gl.hblocks += it.nblk;
+            hitems.push_back(it);
+          }
+        }
+        gl.hn = (int)hitems.size() - gl.h0;
+        gl.n0 = (int)nitems.size();
+        for (size_t t = grp.first; t < grp.second; t++) {
+          const Target& T = targets[r][t];
+          const Block& fb = *T.F->blk;
+          if (T.ncolH)
+            nitems.push_back(NormItem{c->w_h.p + T.hoff, c->w_hn.p + gl.ncols, fb.ld, fb.nsize,
+                                      gl.ncols, (long long)T.ncolH});
+          gl.ncols += (long long)T.ncolH;
+        }
+        gl.nn = (int)nitems.size() - gl.n0;
+        glists[r].push_back(gl);
+      }
+    }
+    GI_CUDA(c, c->w_hitems.assign(hitems));
+    GI_CUDA(c, c->w_nitems.assign(nitems));
+    GI_CUDA(c, c->w_yitems.assign(yitems));
+    mixv(c->w_hitems.p);
+    mixv(c->w_nitems.p);
+    mixv(c->w_yitems.p);
+  }
+  mixv(batch_small);
+
   // the launch sequence of the job, issued eagerly or under stream capture
   bool capturing = false;
   auto issue = [&]() -> gi_status {
@@ -955,11 +1043,18 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
     // Z of this round: the workspace, or its columns of the cache entry
     double* zbase = zref.z ? zref.z + zoff[r] * Kp : c->w_z.p;
     const size_t zc = (zref.z ? ztotal : R.ncolY) * Kp;  // stride between dipole components
+    if (fused_y && batch_small && ylists[r].second) {  // every unit's Y rows in one launch
+      gi_status s = split_build_y_digits_items(c, c->w_yitems.p + ylists[r].first,
+                                               ylists[r].second, (long long)R.ncolY, R.ncolY);
+      if (s != GI_OK) return s;
+    }
     for (const Unit& u : R.units) {
       if (zref.hit) break;  // Z of this round is in the cache
       const Basis& bI = *c->bases[u.I->blk->J];
       const int ndegI = c->degen[u.I->blk->gamma];
-      if (fused_y) {  // straight into the digit planes of the half-ls GEMM's B operand
+      if (fused_y && batch_small) {
+        // built above
+      } else if (fused_y) {  // straight into the digit planes of the half-ls GEMM's B operand
         gi_status s = split_build_y_digits(c, u.I->blk->d_vecs.p, u.I->blk->ld,
                                            c->w_ivec.p + 2 * u.off, u.nI, ndegI, bI,
                                            u.I->blk->gamma, u.ycol, R.ncolY);
@@ -986,9 +1081,18 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
       fl_half += 2.0 * 3.0 * N * (double)N * R.ncolY;
     }
 
-    for (const auto& grp : groups[r]) {
+    for (size_t gi = 0; gi < groups[r].size(); gi++) {
+      const auto& grp = groups[r][gi];
       // H of every final block of the group
-      for (size_t t = grp.first; t < grp.second; t++) {
+      if (batch_small) {
+        const GroupLists& gl = glists[r][gi];
+        if (gl.hn)
+          GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
+                    return launch_build_h_items(c->w_hitems.p + gl.h0, gl.hn, gl.hblocks,
+                                                c->stream);
+                  }));
+      }
+      for (size_t t = grp.first; t < grp.second && !batch_small; t++) {
         const Target& T = targets[r][t];
         const Block& fb = *T.F->blk;
         const Basis& bF = *c->bases[fb.J];
@@ -1015,11 +1119,20 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         const Target& T = targets[r][t];
         const Block& fb = *T.F->blk;
         hn_at[t - grp.first] = hn_off;
-        GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
-                  return launch_col_norms(c->w_h.p + T.hoff, fb.ld, fb.nsize, (int)T.ncolH,
-                                          c->w_hn.p + hn_off, c->stream);
-                }));
+        if (!batch_small)
+          GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+                    return launch_col_norms(c->w_h.p + T.hoff, fb.ld, fb.nsize, (int)T.ncolH,
+                                            c->w_hn.p + hn_off, c->stream);
+                  }));
         hn_off += T.ncolH;
+      }
+      if (batch_small) {
+        const GroupLists& gl = glists[r][gi];
+        if (gl.nn)
+          GI_CUDA(c, timed(c, GI_PHASE_EPILOGUE, [&] {
+                    return launch_col_norms_items(c->w_nitems.p + gl.n0, gl.nn, gl.ncols,
+                                                  c->stream);
+                  }));
       }
       // the final-state GEMMs: one persistent launch for the group, or one per block
       if (grouped_final) {

@@ -18,6 +18,7 @@
 
 #include "engine.h"
 #include "epilogue.cuh"
+#include "items.cuh"
 
 namespace gi {
 
@@ -68,17 +69,14 @@ cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int 
 // One thread per symmetrised final function s of one initial column (i, dI);
 // writes H for every final degenerate component dF.
 template <int NDEGF>
-__global__ void k_build_h(const double* __restrict__ Z, size_t zc, int ldz, int nslotI, int ndegI,
-                          const int32_t* __restrict__ s_case, const int32_t* __restrict__ case_ptr,
-                          const int32_t* __restrict__ case_roots,
-                          const int32_t* __restrict__ root_v, const int32_t* __restrict__ root_key,
-                          const int32_t* __restrict__ root_lam, const double* __restrict__ rep,
-                          int Ntot, const StencilTerm* __restrict__ st,
-                          const int32_t* __restrict__ st_n, int st_max, int nsizeF, int ldh,
-                          double* __restrict__ H) {
-  const int s = blockIdx.x * blockDim.x + threadIdx.x;
-  const int colI = blockIdx.y;  // i * ndegI + dI
-  if (s >= ldh) return;
+__device__ __forceinline__ void build_h_col(
+    const double* __restrict__ Z, size_t zc, int ldz, int nslotI, int colI,
+    const int32_t* __restrict__ s_case, const int32_t* __restrict__ case_ptr,
+    const int32_t* __restrict__ case_roots, const int32_t* __restrict__ root_v,
+    const int32_t* __restrict__ root_key, const int32_t* __restrict__ root_lam,
+    const double* __restrict__ rep, int Ntot, const StencilTerm* __restrict__ st,
+    const int32_t* __restrict__ st_n, int st_max, int nsizeF, int ldh, int s,
+    double* __restrict__ H) {
   double acc[NDEGF];
 #pragma unroll
   for (int d = 0; d < NDEGF; ++d) acc[d] = 0.0;
@@ -101,6 +99,88 @@ __global__ void k_build_h(const double* __restrict__ Z, size_t zc, int ldz, int 
   }
 #pragma unroll
   for (int d = 0; d < NDEGF; ++d) H[((size_t)colI * NDEGF + d) * ldh + s] = acc[d];
+}
+
+template <int NDEGF>
+__global__ void k_build_h(const double* __restrict__ Z, size_t zc, int ldz, int nslotI, int ndegI,
+                          const int32_t* __restrict__ s_case, const int32_t* __restrict__ case_ptr,
+                          const int32_t* __restrict__ case_roots,
+                          const int32_t* __restrict__ root_v, const int32_t* __restrict__ root_key,
+                          const int32_t* __restrict__ root_lam, const double* __restrict__ rep,
+                          int Ntot, const StencilTerm* __restrict__ st,
+                          const int32_t* __restrict__ st_n, int st_max, int nsizeF, int ldh,
+                          double* __restrict__ H) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  const int colI = blockIdx.y;  // i * ndegI + dI
+  if (s >= ldh) return;
+  build_h_col<NDEGF>(Z, zc, ldz, nslotI, colI, s_case, case_ptr, case_roots, root_v, root_key,
+                     root_lam, rep, Ntot, st, st_n, st_max, nsizeF, ldh, s, H);
+}
+
+// Every H build of a group of final blocks in one launch: item k covers
+// blocks [items[k].blk0, items[k].blk0 + items[k].nblk) of the 1-D grid, each
+// block 256 functions s of kHCols initial columns (the item lookup is paid
+// once per kHCols columns).
+__global__ void __launch_bounds__(256) k_build_h_items(const HItem* __restrict__ items,
+                                                        int nitems) {
+  const long long b = blockIdx.x;
+  const int lo = find_item(items, nitems, b, [](const HItem& x) { return x.blk0; });
+  const HItem& it = items[lo];
+  const long long rel = b - it.blk0;
+  const int nsb = (it.ldh + 255) >> 8;
+  const int cb = (int)(rel / nsb);
+  const int s = (int)(rel - (long long)cb * nsb) * 256 + threadIdx.x;
+  if (s >= it.ldh) return;
+  const int c1 = min(it.ncol, (cb + 1) * kHCols);
+  for (int colI = cb * kHCols; colI < c1; ++colI) {
+    if (it.ndegF == 2)
+      build_h_col<2>(it.Z, it.zc, it.ldz, it.nslotI, colI, it.s_case, it.case_ptr, it.case_roots,
+                     it.root_v, it.root_key, it.root_lam, it.rep, it.Ntot, it.st, it.st_n,
+                     it.st_max, it.nsizeF, it.ldh, s, it.H);
+    else
+      build_h_col<1>(it.Z, it.zc, it.ldz, it.nslotI, colI, it.s_case, it.case_ptr, it.case_roots,
+                     it.root_v, it.root_key, it.root_lam, it.rep, it.Ntot, it.st, it.st_n,
+                     it.st_max, it.nsizeF, it.ldh, s, it.H);
+  }
+}
+
+cudaError_t launch_build_h_items(const HItem* items, int nitems, long long nblocks,
+                                 cudaStream_t st) {
+  if (nitems <= 0 || nblocks <= 0) return cudaSuccess;
+  if (nblocks > 0x7FFFFFFFll) return cudaErrorInvalidValue;
+  k_build_h_items<<<(unsigned)nblocks, 256, 0, st>>>(items, nitems);
+  return cudaGetLastError();
+}
+
+// The item of an H build (one per (initial unit, final block) of a group).
+HItem make_h_item(const double* Z, size_t zstride_c, int ldz, int nslotI, int ndegI, int nI,
+                  const Basis& bF, int gammaF, int degF, int nsizeF, int ldh,
+                  const StencilTerm* st, const int32_t* st_n, int st_max, double* H,
+                  long long blk0) {
+  HItem it{};
+  it.Z = Z;
+  it.zc = zstride_c;
+  it.ldz = ldz;
+  it.nslotI = nslotI;
+  it.ndegF = degF;
+  it.nsizeF = nsizeF;
+  it.ldh = ldh;
+  it.Ntot = bF.Ntotal[gammaF];
+  it.st_max = st_max;
+  it.s_case = bF.d_s_case[gammaF].p;
+  it.case_ptr = bF.d_case_ptr.p;
+  it.case_roots = bF.d_case_roots.p;
+  it.root_v = bF.d_root_v.p;
+  it.root_key = bF.d_root_key.p;
+  it.root_lam = bF.d_root_lam.p;
+  it.rep = bF.d_rep[gammaF].p;
+  it.st = st;
+  it.st_n = st_n;
+  it.H = H;
+  it.blk0 = blk0;
+  it.ncol = nI * ndegI;
+  it.nblk = (long long)((it.ncol + kHCols - 1) / kHCols) * ((ldh + 255) / 256);
+  return it;
 }
 
 cudaError_t launch_build_h(const double* Z, size_t zstride_c, int ldz, int nslotI, int ndegI,
@@ -266,6 +346,34 @@ __global__ void k_col_norms(const double* __restrict__ H, int ldh, int n, double
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
     if (threadIdx.x == 0) out[blockIdx.x] = sqrt(acc);
   }
+}
+
+// The columns of every H of a group in one launch (item k: columns
+// [items[k].col0, items[k+1].col0) of the grid).
+__global__ void k_col_norms_items(const NormItem* __restrict__ items, int nitems) {
+  const long long b = blockIdx.x;
+  const int lo = find_item(items, nitems, b, [](const NormItem& x) { return x.col0; });
+  const NormItem& it = items[lo];
+  const double* h = it.H + (size_t)(b - it.col0) * it.ldh;
+  double acc = 0.0;
+  for (int s = threadIdx.x; s < it.n; s += blockDim.x) acc = fma(h[s], h[s], acc);
+  __shared__ double part[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    acc = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (threadIdx.x == 0) it.out[b - it.col0] = sqrt(acc);
+  }
+}
+
+cudaError_t launch_col_norms_items(const NormItem* items, int nitems, long long ncol,
+                                   cudaStream_t s) {
+  if (nitems <= 0 || ncol <= 0) return cudaSuccess;
+  if (ncol > 0x7FFFFFFFll) return cudaErrorInvalidValue;
+  k_col_norms_items<<<(unsigned)ncol, 256, 0, s>>>(items, nitems);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_col_norms(const double* H, int ldh, int n, int ncol, double* out,

@@ -47,6 +47,7 @@
 
 #include "split.h"
 #include "epilogue.cuh"
+#include "items.cuh"
 #include "../../include/gi_probe.h"
 
 namespace gi {
@@ -151,8 +152,12 @@ __device__ __forceinline__ double ld_acc(const double* p) {
 // v * 2^E for an integer |v| < 2^53 (so the double is exact), built from the
 // bits with integer instructions: FP64 throughput is low on this GPU and the
 // epilogues convert every output element.  Results outside the normal range
-// take ldexp.
-__device__ __forceinline__ double scaled_int(long long v, int E) {
+// take ldexp.  Not inlined: the epilogues' unrolled column loops call it twice
+// per element, and inlined copies made the pass-1 epilogue of the half-ls GEMM
+// a long stretch of straight-line code that ran out of the instruction cache
+// once per tile (39 us of a 265 us tile against 21 us called, measured with
+// per-tile clock stamps).
+__device__ __noinline__ double scaled_int(long long v, int E) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
   const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
@@ -1430,21 +1435,17 @@ __global__ void k_slice_rows(const double* __restrict__ X, int ldx, size_t xstri
 // compile time (the planes' row bases in registers, the digit loop unrolled):
 // rows as long as a final block's basis (~11k elements) keep enough loads in
 // flight, where one warp per row leaves the kernel latency-bound.
+// One row of k_slice_rows_b: row ro of a plane set of rset rows, x2 its K
+// values (valid: a row of X, else zeros).
 template <int S>
-__global__ void __launch_bounds__(256) k_slice_rows_b(const double* __restrict__ X, int ldx,
-                                                      size_t xstride, int rows, int K,
-                                                      int rows_pad, int w,
-                                                      uint32_t* __restrict__ out, int grouped,
-                                                      int32_t* __restrict__ e_out) {
+__device__ __forceinline__ void slice_row_b(const double2* __restrict__ x2, bool valid, int K,
+                                            int w, uint32_t* __restrict__ out, int grouped,
+                                            int32_t* __restrict__ e_out, size_t ro, size_t rset) {
   __shared__ unsigned long long wmax[8];
-  const int r = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const size_t rset = (size_t)gridDim.y * rows_pad;     // rows of the plane set
-  const size_t ro = (size_t)blockIdx.y * rows_pad + r;  // this row in the set
-  const double2* x2 =
-      reinterpret_cast<const double2*>(X + blockIdx.y * xstride + (size_t)r * ldx);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int K2 = K >> 1;
   unsigned long long mx = 0;
-  if (r < rows)
+  if (valid)
     for (int k = threadIdx.x; k < K2; k += 256) {
       const double2 v = x2[k];
       mx = max(mx, (unsigned long long)__double_as_longlong(v.x) & 0x7FFFFFFFFFFFFFFFull);
@@ -1471,7 +1472,7 @@ __global__ void __launch_bounds__(256) k_slice_rows_b(const double* __restrict__
   const long long half = 1ll << (w - 1), mask = (1ll << w) - 1;
   for (int k = threadIdx.x; k < K2; k += 256) {
     long long X0 = 0, X1 = 0;
-    if (r < rows) {
+    if (valid) {
       const double2 v = x2[k];
       X0 = fixed_point(v.x, e, ws);
       X1 = fixed_point(v.y, e, ws);
@@ -1491,24 +1492,62 @@ __global__ void __launch_bounds__(256) k_slice_rows_b(const double* __restrict__
   }
 }
 
+template <int S>
+__global__ void __launch_bounds__(256) k_slice_rows_b(const double* __restrict__ X, int ldx,
+                                                      size_t xstride, int rows, int K,
+                                                      int rows_pad, int w,
+                                                      uint32_t* __restrict__ out, int grouped,
+                                                      int32_t* __restrict__ e_out) {
+  const int r = blockIdx.x;
+  const size_t rset = (size_t)gridDim.y * rows_pad;     // rows of the plane set
+  const size_t ro = (size_t)blockIdx.y * rows_pad + r;  // this row in the set
+  const double2* x2 =
+      reinterpret_cast<const double2*>(X + blockIdx.y * xstride + (size_t)r * ldx);
+  slice_row_b<S>(x2, r < rows, K, w, out, grouped, e_out, ro, rset);
+}
+
+// The rows of several operands in one launch (each its own plane set, every
+// row valid): operand j has rows [row0[j], row0[j + 1]) of the grid.
+constexpr int kSliceMaxOps = 44;
+struct SliceOps {
+  int n;
+  int row0[kSliceMaxOps + 1];
+  int K[kSliceMaxOps];
+  int ldx[kSliceMaxOps];
+  const double* X[kSliceMaxOps];
+  uint32_t* out[kSliceMaxOps];
+  int32_t* e[kSliceMaxOps];
+};
+template <int S>
+__global__ void __launch_bounds__(256) k_slice_rows_ops(const __grid_constant__ SliceOps ops,
+                                                        int w, int grouped) {
+  const int b = blockIdx.x;
+  int j = 0;
+  while (j + 1 < ops.n && ops.row0[j + 1] <= b) ++j;
+  const int r = b - ops.row0[j];
+  const size_t rows = (size_t)(ops.row0[j + 1] - ops.row0[j]);
+  const double2* x2 = reinterpret_cast<const double2*>(ops.X[j] + (size_t)r * ops.ldx[j]);
+  slice_row_b<S>(x2, true, ops.K[j], w, ops.out[j], grouped, ops.e[j], (size_t)r, rows);
+}
+
 // Y built straight into its digit planes (split path): one 256-thread block per
 // row (i, d, slot) of the B operand computes the row's Kp values of Y with
 // k_build_y's arithmetic (the same order of operations, so the same doubles)
 // into shared memory, takes the row exponent and cuts the digits as
 // k_slice_rows_b does.  The FP64 Y never goes to HBM.
+// One row of Y (row = (i * ndeg + d) * nslot + slot within the unit) into its
+// digit planes: the row in shared memory, its exponent, its digits.
 template <int S>
-__global__ void __launch_bounds__(256)
-    k_build_y_digits(const double* __restrict__ vecs, int ld, const int32_t* __restrict__ ivec,
-                     int ndeg, const int32_t* __restrict__ yptr, const int32_t* __restrict__ yroot,
-                     const int32_t* __restrict__ root_case, const int32_t* __restrict__ root_lam,
-                     const int32_t* __restrict__ case_iterm,
-                     const int32_t* __restrict__ case_nelem, const double* __restrict__ rep,
-                     int Ntot, int degen, int nslot, int N, int Kp, int w,
-                     uint32_t* __restrict__ out, int grouped, int32_t* __restrict__ e_out,
-                     size_t row0, size_t rset) {
+__device__ __forceinline__ void build_y_digits_row(
+    const double* __restrict__ vecs, int ld, const int32_t* __restrict__ ivec, int ndeg,
+    const int32_t* __restrict__ yptr, const int32_t* __restrict__ yroot,
+    const int32_t* __restrict__ root_case, const int32_t* __restrict__ root_lam,
+    const int32_t* __restrict__ case_iterm, const int32_t* __restrict__ case_nelem,
+    const double* __restrict__ rep, int Ntot, int degen, int nslot, int N, int Kp, int w,
+    uint32_t* __restrict__ out, int grouped, int32_t* __restrict__ e_out, size_t row0,
+    size_t rset, int row) {
   extern __shared__ __align__(16) double ys[];  // the row's Kp values
   __shared__ unsigned long long wmax[8];
-  const int row = blockIdx.x;  // (i * ndeg + d) * nslot + slot within the unit
   const int col = row / nslot, slot = row - col * nslot;
   const int i = col / ndeg, d = col - i * ndeg;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -1569,7 +1608,38 @@ __global__ void __launch_bounds__(256)
     }
     out[base[0] + (4 * nq > 0 ? kg : (size_t)k)] =
         (uint32_t)bf16_of_int((int)X0) | ((uint32_t)bf16_of_int((int)X1) << 16);
-  }
+  }}
+
+template <int S>
+__global__ void __launch_bounds__(256)
+    k_build_y_digits(const double* __restrict__ vecs, int ld, const int32_t* __restrict__ ivec,
+                     int ndeg, const int32_t* __restrict__ yptr, const int32_t* __restrict__ yroot,
+                     const int32_t* __restrict__ root_case, const int32_t* __restrict__ root_lam,
+                     const int32_t* __restrict__ case_iterm,
+                     const int32_t* __restrict__ case_nelem, const double* __restrict__ rep,
+                     int Ntot, int degen, int nslot, int N, int Kp, int w,
+                     uint32_t* __restrict__ out, int grouped, int32_t* __restrict__ e_out,
+                     size_t row0, size_t rset) {
+  build_y_digits_row<S>(vecs, ld, ivec, ndeg, yptr, yroot, root_case, root_lam, case_iterm,
+                        case_nelem, rep, Ntot, degen, nslot, N, Kp, w, out, grouped, e_out, row0,
+                        rset, (int)blockIdx.x);
+}
+
+// The Y rows of every unit of a round in one launch: item k has rows
+// [items[k].row0, items[k].row0 + items[k].rows) of the grid and of Y.
+template <int S>
+__global__ void __launch_bounds__(256)
+    k_build_y_digits_items(const YItem* __restrict__ items, int nitems, int N, int Kp, int w,
+                           uint32_t* __restrict__ out, int grouped, int32_t* __restrict__ e_out,
+                           size_t rset) {
+  const long long b = blockIdx.x;
+  const int lo = find_item(items, nitems, b, [](const YItem& x) { return x.row0; });
+  const YItem& it = items[lo];
+  if (b - it.row0 >= it.rows) return;  // not a row of any unit (the whole block)
+  build_y_digits_row<S>(it.vecs, it.ld, it.ivec, it.ndeg, it.yptr, it.yroot, it.root_case,
+                        it.root_lam, it.case_iterm, it.case_nelem, it.rep, it.Ntot, it.ndeg,
+                        it.nslot, N, Kp, w, out, grouped, e_out, (size_t)it.row0, rset,
+                        (int)(b - it.row0));
 }
 constexpr int kFusedYMaxKp = 8192;  // 64 KB of shared memory per row
 
@@ -1730,6 +1800,10 @@ cudaError_t set_attributes() {
                             k_split_gemm_g<S, BN2, D1, true, false, true>);
         if (status == cudaSuccess)
           status = cudaFuncSetAttribute(k_build_y_digits<S>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(kFusedYMaxKp * sizeof(double)));
+        if (status == cudaSuccess)
+          status = cudaFuncSetAttribute(k_build_y_digits_items<S>,
                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         (int)(kFusedYMaxKp * sizeof(double)));
       }
@@ -2318,6 +2392,13 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs,
   }
   size_t eoff = 0, boff = 0;
   double flops = 0.0;
+  // the H rows of every problem are cut in one launch (GI_BATCH_SMALL=0: one
+  // launch per problem)
+  const char* bs_env = getenv("GI_BATCH_SMALL");
+  const bool batch = !(bs_env && bs_env[0] == '0');
+  SliceOps* ops = new SliceOps();
+  ops->n = 0;
+  ops->row0[0] = 0;
   for (int q = 0; q < (int)jobs.size() && g == GI_OK; ++q) {
     const FinalJob& j = jobs[order[q]];
     Block& fb = *j.fb;
@@ -2326,11 +2407,23 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs,
     if (g != GI_OK) break;
     uint16_t* bs = S->b_slices.p + boff;
     int32_t* be = S->b_exp.p + eoff;
-    g = check(c, timed(c, GI_PHASE_SLICE, [&] {
-                return slice(j.H, j.ldh, j.ncol, K, j.ncol, SS, S->w, true, bs, be, c->stream);
-              }),
-              "slice H");
-    if (g != GI_OK) break;
+    if (batch) {
+      if (j.ncol > 0) {
+        const int o = ops->n++;
+        ops->K[o] = K;
+        ops->ldx[o] = j.ldh;
+        ops->X[o] = j.H;
+        ops->out[o] = reinterpret_cast<uint32_t*>(bs);
+        ops->e[o] = be;
+        ops->row0[o + 1] = ops->row0[o] + j.ncol;
+      }
+    } else {
+      g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                  return slice(j.H, j.ldh, j.ncol, K, j.ncol, SS, S->w, true, bs, be, c->stream);
+                }),
+                "slice H");
+      if (g != GI_OK) break;
+    }
     GpProb& pr = P->p[q];
     const int nq = SS / 4, nt = SS % 4;
     if (!make_map_groups(&pr.aq, fb.d_digits.p, K, vpad, nq, kBM, K) ||
@@ -2365,6 +2458,17 @@ gi_status split_gemm_final_grouped(Ctx* c, const std::vector<FinalJob>& jobs,
     eoff += j.ncol;
     flops += (double)SS * (SS + 1) / 2 * 2.0 * fb.nvec * (double)j.ncol * fb.nsize;
   }
+  if (g == GI_OK && ops->n > 0) {
+    for (int o = 0; o < ops->n; ++o)  // the grouped layout cuts K in 16-element slices
+      if (ops->K[o] & 15) g = check(c, cudaErrorInvalidValue, "slice H");
+    if (g == GI_OK)
+      g = check(c, timed(c, GI_PHASE_SLICE, [&] {
+                  k_slice_rows_ops<SS><<<ops->row0[ops->n], 256, 0, c->stream>>>(*ops, S->w, 1);
+                  return cudaGetLastError();
+                }),
+                "slice H");
+  }
+  delete ops;
   if (g == GI_OK && P->nitems > 0) {
     c->stats.flops_tensor += flops;
     g = check(c, kernel_attributes(SS), "kernel attributes");
@@ -2456,6 +2560,25 @@ gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, d
 }
 
 bool split_fused_y(const Ctx* c) { return split_grouped_final(c) && c->Kp <= kFusedYMaxKp; }
+
+gi_status split_build_y_digits_items(Ctx* c, const YItem* items, int n, long long rows,
+                                     size_t rows_total) {
+  SplitState* S = state(c);
+  if (n <= 0 || rows <= 0) return GI_OK;
+  if (S->s != 9 || S->b_slices.n < (size_t)9 * rows_total * c->Kp || S->b_exp.n < rows_total ||
+      rows > 0x7FFFFFFFll) {
+    c->err = "split precision: Y digit workspace not prepared";
+    return GI_ERR_STATE;
+  }
+  return check(c, timed(c, GI_PHASE_CORRELATE, [&] {
+                 k_build_y_digits_items<9><<<(unsigned)rows, 256, (size_t)c->Kp * sizeof(double),
+                                             c->stream>>>(
+                     items, n, c->N, c->Kp, S->w, reinterpret_cast<uint32_t*>(S->b_slices.p),
+                     S->grouped ? 1 : 0, S->b_exp.p, rows_total);
+                 return cudaGetLastError();
+               }),
+               "Y digits");
+}
 
 gi_status split_build_y_digits(Ctx* c, const double* vecs, int ld, const int32_t* ivec, int nI,
                                int ndeg, const Basis& b, int gamma, size_t row0,

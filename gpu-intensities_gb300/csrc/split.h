@@ -18,6 +18,10 @@ gi_status split_gemm_dipole_narrow(Ctx* c, const double* Y, int ldy, int ncol, d
 // into rows [row0, row0 + nI * ndeg * nslot) of the Y digit set of a round of
 // rows_total rows; split_fused_y() says when this path applies.
 bool split_fused_y(const Ctx* c);
+// Every unit's Y rows of a round (a device table of n items, rows in all) in
+// one launch; rows_total as in split_build_y_digits.
+gi_status split_build_y_digits_items(Ctx* c, const YItem* items, int n, long long rows,
+                                     size_t rows_total);
 gi_status split_build_y_digits(Ctx* c, const double* vecs, int ld, const int32_t* ivec, int nI,
                                int ndeg, const Basis& b, int gamma, size_t row0,
                                size_t rows_total);
