@@ -112,6 +112,49 @@ class gi_deck(C.Structure):
                 ("params", gi_params)]
 
 
+class gi_line_text(C.Structure):
+    """The fields of one printed line (gi_format_line_text)."""
+    _fields_ = [("jF", C.c_int32), ("jI", C.c_int32), ("krotF", C.c_int32), ("krotI", C.c_int32),
+                ("ilevelF", C.c_int32), ("ilevelI", C.c_int32), ("nclasses", C.c_int32),
+                ("nmodes", C.c_int32), ("ndegF", C.c_int32), ("ndegI", C.c_int32),
+                ("symF", C.c_char_p), ("symI", C.c_char_p),
+                ("cgF", C.c_char_p * GI_TROVE_MAXQ), ("cgI", C.c_char_p * GI_TROVE_MAXQ),
+                ("quantaF", C.c_int32 * GI_TROVE_MAXQ), ("quantaI", C.c_int32 * GI_TROVE_MAXQ),
+                ("normalF", C.c_int32 * GI_TROVE_MAXQ), ("normalI", C.c_int32 * GI_TROVE_MAXQ),
+                ("eF", C.c_double), ("eI", C.c_double), ("nu", C.c_double), ("S", C.c_double),
+                ("A", C.c_double), ("I", C.c_double), ("t", C.c_double * 4)]
+
+
+def format_line_text(f: dict) -> str:
+    """One printed line from explicit fields (host code, no GPU): labels
+    cgF/cgI for classes 0..nclasses, quanta/normal with index 0 unused."""
+    x = gi_line_text()
+    for k in ("jF", "jI", "krotF", "krotI", "ilevelF", "ilevelI", "ndegF", "ndegI"):
+        setattr(x, k, int(f[k]))
+    x.nclasses, x.nmodes = len(f["cgF"]) - 1, len(f["quantaF"]) - 1
+    keep = [str(v).encode() for v in [f["symF"], f["symI"]] + list(f["cgF"]) + list(f["cgI"])]
+    x.symF, x.symI = keep[0], keep[1]
+    for i, v in enumerate(f["cgF"]):
+        x.cgF[i] = str(v).encode()
+    for i, v in enumerate(f["cgI"]):
+        x.cgI[i] = str(v).encode()
+    for k in ("quantaF", "quantaI", "normalF", "normalI"):
+        arr = getattr(x, k)
+        for i, v in enumerate(f[k]):
+            arr[i] = int(v)
+    for k in ("eF", "eI", "nu", "S", "A", "I"):
+        setattr(x, k, float(f[k]))
+    for i, v in enumerate(f["t"]):
+        x.t[i] = float(v)
+    L = lib()
+    used = C.c_size_t(0)
+    buf = C.create_string_buffer(4096)
+    st = L.gi_format_line_text(C.byref(x), buf, len(buf), C.byref(used))
+    if st != GI_OK:
+        raise GiError(st, "gi_format_line_text")
+    return buf.value.decode()
+
+
 class gi_trove_level(C.Structure):
     _fields_ = [("irec", C.c_int32 * 2), ("ilevel", C.c_int32), ("ndeg", C.c_int32),
                 ("krot", C.c_int32), ("taurot", C.c_int32), ("large_coef", C.c_int32),
@@ -185,6 +228,7 @@ def lib():
                                            C.c_int, i32p, i32p, C.POINTER(gi_trove_level),
                                            C.c_int32, C.c_char_p, C.c_size_t]
         L.gi_load_trove.argtypes = [C.c_void_p, C.c_char_p, C.POINTER(gi_deck), C.c_int]
+        L.gi_format_line_text.argtypes = [C.c_void_p, C.c_char_p, C.c_size_t, C.c_void_p]
         L.gi_format_lines.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_char_p, C.c_size_t,
                                       C.POINTER(C.c_size_t)]
         L.gi_partition_function.argtypes = [C.c_void_p, C.c_double, f64p]

@@ -783,6 +783,75 @@ gi_status gi_partition_function(gi_ctx* h, double temperature, double* q) {
   return GI_OK;
 }
 
+// The printed layout of one line (cuda_host.cu:1444-1473): the reference's
+// printf sequence, field by field, appended to s.
+static void format_line_text(const gi_line_text& f, std::string& s) {
+  char tmp[128];
+  const int dj = f.jF - f.jI;
+  const char* br = dj == 0 ? "Q" : (dj == 1 ? "R" : "P");
+  std::snprintf(tmp, sizeof(tmp), "%4i %4s   <-%4i %4s   %1s  %11.4f <- %11.4f %11.4f  ( %3s %3i ) ( ",
+                f.jF, f.symF, f.jI, f.symI, br, f.eF, f.eI, std::fabs(f.nu), f.cgF[0], f.krotF);
+  s += tmp;
+  for (int i = 1; i <= f.nclasses; i++) {
+    std::snprintf(tmp, sizeof(tmp), " %3s", f.cgF[i]);
+    s += tmp;
+  }
+  s += " ";
+  for (int i = 1; i <= f.nmodes; i++) {
+    std::snprintf(tmp, sizeof(tmp), " %3i", f.quantaF[i]);
+    s += tmp;
+  }
+  std::snprintf(tmp, sizeof(tmp), " ) <- ( %3s %3i ) ( ", f.cgI[0], f.krotI);
+  s += tmp;
+  for (int i = 1; i <= f.nclasses; i++) {
+    std::snprintf(tmp, sizeof(tmp), " %3s", f.cgI[i]);
+    s += tmp;
+  }
+  s += " ";
+  for (int i = 1; i <= f.nmodes; i++) {
+    std::snprintf(tmp, sizeof(tmp), " %3i", f.quantaI[i]);
+    s += tmp;
+  }
+  std::snprintf(tmp, sizeof(tmp), ")  %16.8e %16.8e %16.8e   %6i <- %6i %8i %8i ( ", f.S, f.A,
+                f.I, f.ilevelF + 1, f.ilevelI + 1, 0, 0);
+  s += tmp;
+  for (int i = 1; i <= f.nmodes; i++) {
+    std::snprintf(tmp, sizeof(tmp), " %3i", f.normalF[i]);
+    s += tmp;
+  }
+  s += " ) <-  ( ";
+  for (int i = 1; i <= f.nmodes; i++) {
+    std::snprintf(tmp, sizeof(tmp), " %3i", f.normalI[i]);
+    s += tmp;
+  }
+  s += " ) ";
+  for (int dF = 0; dF < f.ndegF; dF++)
+    for (int dI = 0; dI < f.ndegI; dI++) {
+      std::snprintf(tmp, sizeof(tmp), " %16.9e", f.t[dI + 2 * dF]);
+      s += tmp;
+    }
+  s += "\n";
+}
+
+gi_status gi_format_line_text(const gi_line_text* f, char* buf, size_t cap, size_t* used) {
+  if (!f || !used || f->nclasses < 0 || f->nclasses >= GI_TROVE_MAXQ || f->nmodes < 0 ||
+      f->nmodes >= GI_TROVE_MAXQ || f->ndegF < 1 || f->ndegF > 2 || f->ndegI < 1 || f->ndegI > 2 ||
+      !f->symF || !f->symI)
+    return GI_ERR_ARG;
+  for (int q = 0; q <= f->nclasses; q++)
+    if (!f->cgF[q] || !f->cgI[q]) return GI_ERR_ARG;
+  std::string s;
+  format_line_text(*f, s);
+  *used = s.size();
+  if (buf && cap) {
+    const size_t n = std::min(cap - 1, s.size());
+    std::memcpy(buf, s.data(), n);
+    buf[n] = 0;
+    if (s.size() >= cap) return GI_ERR_ARG;
+  }
+  return GI_OK;
+}
+
 // One line of the reference's list (cuda_host.cu:1444-1473) for each line of
 // the last gi_run, "\n"-terminated.  The level descriptors come from
 // gi_load_trove; levels loaded otherwise print their symmetry as the class
@@ -828,7 +897,6 @@ gi_status gi_format_lines(gi_ctx* h, int64_t offset, int64_t count, char* buf, s
   };
   std::string s;
   s.reserve((size_t)count * 256);
-  char tmp[128];
   for (const gi_line& ln : lines) {
     if (ln.level_i < 0 || ln.level_f < 0 || ln.level_i >= (int)c->levels.size() ||
         ln.level_f >= (int)c->levels.size())
@@ -838,51 +906,38 @@ gi_status gi_format_lines(gi_ctx* h, int64_t offset, int64_t count, char* buf, s
     gi_trove_level dI, dF;
     describe(LI, dI);
     describe(LF, dF);
-    const int dj = LF.J - LI.J;
-    const char* br = dj == 0 ? "Q" : (dj == 1 ? "R" : "P");
-    std::snprintf(tmp, sizeof(tmp), "%4i %4s   <-%4i %4s   %1s  %11.4f <- %11.4f %11.4f  ( %3s %3i ) ( ",
-                  LF.J, label(LF.gamma), LI.J, label(LI.gamma), br, LF.energy - zpe,
-                  LI.energy - zpe, std::fabs(ln.nu), label(dF.cgamma[0]), dF.krot);
-    s += tmp;
-    for (int i = 1; i <= nclasses; i++) {
-      std::snprintf(tmp, sizeof(tmp), " %3s", label(dF.cgamma[i]));
-      s += tmp;
+    gi_line_text f;
+    std::memset(&f, 0, sizeof(f));
+    f.jF = LF.J;
+    f.jI = LI.J;
+    f.krotF = dF.krot;
+    f.krotI = dI.krot;
+    f.ilevelF = dF.ilevel;
+    f.ilevelI = dI.ilevel;
+    f.nclasses = std::min(nclasses, GI_TROVE_MAXQ - 1);
+    f.nmodes = std::min(nmodes, GI_TROVE_MAXQ - 1);
+    f.ndegF = ln.ndeg_f;
+    f.ndegI = ln.ndeg_i;
+    f.symF = label(LF.gamma);
+    f.symI = label(LI.gamma);
+    for (int q = 0; q <= f.nclasses; q++) {
+      f.cgF[q] = label(dF.cgamma[q]);
+      f.cgI[q] = label(dI.cgamma[q]);
     }
-    s += " ";
-    for (int i = 1; i <= nmodes; i++) {
-      std::snprintf(tmp, sizeof(tmp), " %3i", dF.quanta[i]);
-      s += tmp;
+    for (int q = 0; q <= f.nmodes; q++) {
+      f.quantaF[q] = dF.quanta[q];
+      f.quantaI[q] = dI.quanta[q];
+      f.normalF[q] = dF.normal[q];
+      f.normalI[q] = dI.normal[q];
     }
-    std::snprintf(tmp, sizeof(tmp), " ) <- ( %3s %3i ) ( ", label(dI.cgamma[0]), dI.krot);
-    s += tmp;
-    for (int i = 1; i <= nclasses; i++) {
-      std::snprintf(tmp, sizeof(tmp), " %3s", label(dI.cgamma[i]));
-      s += tmp;
-    }
-    s += " ";
-    for (int i = 1; i <= nmodes; i++) {
-      std::snprintf(tmp, sizeof(tmp), " %3i", dI.quanta[i]);
-      s += tmp;
-    }
-    std::snprintf(tmp, sizeof(tmp), ")  %16.8e %16.8e %16.8e   %6i <- %6i %8i %8i ( ", ln.S, ln.A,
-                  ln.I, dF.ilevel + 1, dI.ilevel + 1, 0, 0);
-    s += tmp;
-    for (int i = 1; i <= nmodes; i++) {
-      std::snprintf(tmp, sizeof(tmp), " %3i", dF.normal[i]);
-      s += tmp;
-    }
-    s += " ) <-  ( ";
-    for (int i = 1; i <= nmodes; i++) {
-      std::snprintf(tmp, sizeof(tmp), " %3i", dI.normal[i]);
-      s += tmp;
-    }
-    s += " ) ";
-    for (int dF_ = 0; dF_ < ln.ndeg_f; dF_++)
-      for (int dI_ = 0; dI_ < ln.ndeg_i; dI_++) {
-        std::snprintf(tmp, sizeof(tmp), " %16.9e", ln.t[dI_ + 2 * dF_]);
-        s += tmp;
-      }
-    s += "\n";
+    f.eF = LF.energy - zpe;
+    f.eI = LI.energy - zpe;
+    f.nu = ln.nu;
+    f.S = ln.S;
+    f.A = ln.A;
+    f.I = ln.I;
+    for (int q = 0; q < 4; q++) f.t[q] = ln.t[q];
+    format_line_text(f, s);
   }
   *used = s.size();
   if (buf && cap) {

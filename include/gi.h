@@ -381,6 +381,27 @@ gi_status gi_load_trove(gi_ctx* ctx, const char* dir, const gi_deck* deck, int f
    line; *used receives the bytes needed (without the final NUL). */
 gi_status gi_format_lines(gi_ctx* ctx, int64_t offset, int64_t count, char* buf, size_t cap,
                           size_t* used);
+/* The fields of one printed line (cuda_host.cu:1444-1473) and the formatter
+   gi_format_lines applies to them, host code only (no context, no GPU).  The
+   branch letter follows from jF - jI; energies are relative to the ZPE;
+   labels hold the symmetry names of classes 0..nclasses, quanta and normal
+   indices 1..nmodes (index 0 unused, as in gi_trove_level); ilevel is
+   0-based (printed + 1); t holds ndeg_i * ndeg_f moments t[dI + 2 dF]. */
+typedef struct {
+  int32_t jF, jI, krotF, krotI, ilevelF, ilevelI;
+  int32_t nclasses, nmodes, ndegF, ndegI;
+  const char* symF;
+  const char* symI;
+  const char* cgF[GI_TROVE_MAXQ];
+  const char* cgI[GI_TROVE_MAXQ];
+  int32_t quantaF[GI_TROVE_MAXQ], quantaI[GI_TROVE_MAXQ];
+  int32_t normalF[GI_TROVE_MAXQ], normalI[GI_TROVE_MAXQ];
+  double eF, eI, nu, S, A, I;
+  double t[4];
+} gi_line_text;
+/* Appends the line's text ("\n"-terminated) to buf; *used receives its
+   length (also when cap is too small, then GI_ERR_ARG). */
+gi_status gi_format_line_text(const gi_line_text* f, char* buf, size_t cap, size_t* used);
 /* Partition function over the loaded levels: sum of g_ns(gamma) (2J+1) ndeg
    exp(-c2 (E - ZPE) / T); the reference takes it from the deck (QSTAT).  A run
    whose q_stat is <= 0 uses this value at its temperature. */

@@ -40,7 +40,7 @@ def test_struct_layouts_match_header(pkg, tmp_path):
     import numpy as np
     structs = {"gi_params": pkg.gi_params, "gi_stats": pkg.gi_stats,
                "gi_serve_config": pkg.gi_serve_config, "gi_job_info": pkg.gi_job_info,
-               "gi_serve_stats": pkg.gi_serve_stats}
+               "gi_serve_stats": pkg.gi_serve_stats, "gi_line_text": pkg.gi_line_text}
     dtypes = {"gi_line": pkg.LINE_DTYPE, "gi_level": pkg.LEVEL_DTYPE,
               "gi_line_compact": pkg.LINE_COMPACT_DTYPE}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gi.h"', "int main(void){"]
