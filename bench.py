@@ -63,9 +63,14 @@ SHARDS = {"c3v_batched": 10}
 # lowest initial levels
 CPU_SAMPLE = {"c3v_batched": ((20, 21), 2), "c2v_plain": ((9, 10), 8),
               "c2v_small": ((0, 1), 4), "c3v_small": ((1, 2), 4)}
-# DRAM bytes (read + write) per Y column of one half-line-strength split GEMM
-# launch, from ncu captures (profiles/): N = 3000 (c3v) and N = 2000 (c2v)
-SPLIT_HALFLS_DRAM_BYTES_PER_COL = {3000: None, 2000: (62.136866e9 + 6.543222e9) / 96000}
+# DRAM traffic of the half-line-strength split GEMM from one ncu capture of its
+# first K segment (K = 2048) on a small case of the same Nvib (profiles/):
+# bytes read per Y column per K element (the digit planes streamed past the
+# tiles) and bytes written per Y column (Z).  A job's K runs in segments of
+# 2048; each later segment re-reads Z to add to it.
+SPLIT_HALFLS_TRAFFIC = {3000: {"read_per_col_k": 43139425024 / (47904 * 2048),
+                               "write_per_col": 4181061888 / 47904,
+                               "capture": "c3v_batched J <= 8, 47904 Y columns, K = 2048"}}
 
 
 def parse(argv=None):
@@ -438,23 +443,6 @@ class Timer:
         return a.elapsed_time(b) * 1e-3, out
 
 
-def register_host(torch, arrays):
-    """Page-lock numpy arrays in place (cudaHostRegister), so that copies from
-    them run at pinned-memory speed without a second host copy."""
-    rt = torch.cuda.cudart()
-    done = []
-    for a in arrays:
-        if a.nbytes and int(rt.cudaHostRegister(a.ctypes.data, a.nbytes, 0)) == 0:
-            done.append(a)
-    return done
-
-
-def unregister_host(torch, arrays):
-    rt = torch.cuda.cudart()
-    for a in arrays:
-        rt.cudaHostUnregister(a.ctypes.data)
-
-
 def split_roofline(prob, ps, peaks):
     """The dominant kernel of the split path: the half-line-strength digit GEMM
     (k_split_gemm_g, one launch per round)."""
@@ -465,14 +453,27 @@ def split_roofline(prob, ps, peaks):
     ncol = ps["flops_halfls"] / (6.0 * prob.N * prob.N)
     peak = peaks.get("bf16_tflops", 1900.0)
     achieved = flops / sp[dom] / 1e12 if sp[dom] else 0.0
-    per_col = SPLIT_HALFLS_DRAM_BYTES_PER_COL.get(prob.N)
+    tr = SPLIT_HALFLS_TRAFFIC.get(prob.N)
+    traffic = None
+    if tr:
+        kp = -(-prob.N // 64) * 64
+        nseg = -(-kp // 2048)
+        step_bytes = ncol * (tr["read_per_col_k"] * kp + tr["write_per_col"] * (2 * nseg - 1))
+        traffic = step_bytes / max(lp[dom], 1)
+    algo = ncol * (9 * 2 * (-(-prob.N // 64) * 64) + 3 * prob.N * 8) / max(lp[dom], 1)
     return {"bound": "tensor", "kernel": "k_split_gemm_g (tcgen05 bf16 digit GEMM, grouped digit "
                                          "layout, half line strength)",
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
-            "traffic": per_col * ncol / max(lp[dom], 1) if per_col else None,
-            "traffic_source": "ncu dram__bytes_read+write of this kernel per Y column on a small "
-                              "case of the same Nvib, scaled by Y columns" if per_col else
-                              "not captured for this Nvib",
+            "traffic": traffic,
+            "traffic_source": (f"ncu dram__bytes_read+write of this kernel on {tr['capture']}, "
+                               "scaled to the launch by Y columns and K (reads) and by Y columns "
+                               "(writes, and the re-read of Z by later K segments)")
+            if tr else "not captured for this Nvib",
+            "algorithmic_bytes_per_launch": algo,
+            "algorithmic_bytes_meaning": "Y digit planes (9 x 2 B x Kp per column) read once and "
+                                         "Z (3 x N doubles per column) written once, per launch "
+                                         "averaged over the step's launches; the dipole's digit "
+                                         "planes (0.5 GB) are re-read per L2 raster group",
             "achieved_meaning": "bf16 tensor-pipe rate: digit-pair products x 2 x M x N x K",
             "tensor_tflop_per_launch": flops / max(lp[dom], 1) / 1e12,
             "digit_pair_products": pairs,
@@ -482,7 +483,10 @@ def split_roofline(prob, ps, peaks):
             "peak_source": "MEASURED_PEAKS.json bf16_tflops (of measured)"
             if "bf16_tflops" in peaks else "fallback 1.9 PFLOP/s",
             "phase_seconds": {k: round(v, 6) for k, v in sp.items()},
-            "phase_launches": lp, "launch_avg_ms": 1e3 * sp[dom] / max(lp[dom], 1)}
+            "phase_launches": lp, "launch_avg_ms": 1e3 * sp[dom] / max(lp[dom], 1),
+            "launch_unit": "one round's half-ls GEMM: its K segments (2048, then the rest) as "
+                           "consecutive kernel launches; achieved, traffic and launch_avg_ms "
+                           "are per such launch"}
 
 
 # ---------------------------------------------------------------- legs
@@ -718,20 +722,23 @@ def main_ours(args):
     # records while it computes), so the uploads are paid once per job
     e2e = None
     if not args.no_e2e:
-        arrays = [prob.mu] + [b.vecs for _, b in sorted(prob.blocks.items())]
-        pinned = register_host(torch, arrays)
-        h2d = sum(a.nbytes for a in arrays)
+        # the job's inputs in page-locked host memory (cudaHostAlloc through
+        # torch), as a caller that owns pinned buffers hands them over
+        host = {"mu": torch.from_numpy(prob.mu).pin_memory().numpy()}
+        for key, b in sorted(prob.blocks.items()):
+            host[key] = torch.from_numpy(b.vecs).pin_memory().numpy()
+        h2d = sum(a.nbytes for a in host.values())
         parts = {"upload_ms": 0.0, "run_ms": 0.0, "dipole_ms": 0.0}
         d2h = []
         slowest = []
 
         def e2e_step(i):
             ta = time.perf_counter()
-            eng.set_dipole(prob.N, prob.mu)
+            eng.set_dipole(prob.N, host["mu"])
             parts["dipole_ms"] += 1e3 * (time.perf_counter() - ta)
             for (J, g), b in sorted(prob.blocks.items()):
                 t = time.perf_counter()
-                eng.set_block(J, g, b.vecs, b.energies, b.quanta)
+                eng.set_block(J, g, host[(J, g)], b.energies, b.quanta)
                 slowest.append((time.perf_counter() - t, b.vecs.nbytes, J, g))
             tb = time.perf_counter()
             n_pre, nbytes = 0, 0
@@ -751,12 +758,12 @@ def main_ours(args):
         slowest.clear()
         ne = args.e2e_steps
         te, n = timer(ne, e2e_step)
-        unregister_host(torch, pinned)
+        del host
         e2e = {"value": world * sum(n) / te, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(np.mean(d2h)), "ms_per_step": 1e3 * te / ne,
                "steps": ne, "step": f"one whole job: uploads, then all {S} shards",
                "value_over_device_value": (sum(n) / te) / value_rate,
-               "host_pinned": bool(len(pinned) == len(arrays)),
+               "host_memory": "page-locked (cudaHostAlloc)",
                "host_wall_ms_per_step": {k: v / ne for k, v in parts.items()},
                "upload_gb_per_s": h2d / (parts["upload_ms"] / ne * 1e-3),
                "slowest_block_uploads": [{"s": round(t, 4), "bytes": int(nb), "J": J, "gamma": g}

@@ -331,6 +331,7 @@ struct Ctx {
   DevArray<double> w_BI;       // Boltzmann factors of the run's initial levels
   DevArray<EpiPart> w_epi;     // parts of the fused epilogue
   DevArray<HItem> w_hitems;    // the H builds of every group (one launch per group)
+  DevArray<long long> w_hfirst; // their first grid blocks, contiguous for the lookup
   DevArray<NormItem> w_nitems; // the H column norms of every group
   DevArray<YItem> w_yitems;    // the Y digit builds of every round (one launch per round)
   DevArray<RefineRec> w_rec;   // lines handed to the exact re-evaluation
@@ -428,8 +429,8 @@ HItem make_h_item(const double* Z, size_t zstride_c, int ldz, int nslotI, int nd
                   const StencilTerm* st, const int32_t* st_n, int st_max, double* H,
                   long long blk0);
 // Every item of a device table in one launch (nblocks = the items' blocks).
-cudaError_t launch_build_h_items(const HItem* items, int nitems, long long nblocks,
-                                 cudaStream_t st);
+cudaError_t launch_build_h_items(const HItem* items, const long long* firsts, int nitems,
+                                 long long nblocks, cudaStream_t st);
 cudaError_t launch_half_ls_prim(const double* Z, size_t zstride_c, int ldz, const Basis& bF,
                                 const StencilTerm* st, const int32_t* st_n, int st_max,
                                 double* h, cudaStream_t s);

@@ -1020,7 +1020,11 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         glists[r].push_back(gl);
       }
     }
+    std::vector<long long> hfirst(hitems.size());
+    for (size_t k = 0; k < hitems.size(); k++) hfirst[k] = hitems[k].blk0;
     GI_CUDA(c, c->w_hitems.assign(hitems));
+    GI_CUDA(c, c->w_hfirst.assign(hfirst));
+    mixv(c->w_hfirst.p);
     GI_CUDA(c, c->w_nitems.assign(nitems));
     GI_CUDA(c, c->w_yitems.assign(yitems));
     mixv(c->w_hitems.p);
@@ -1088,8 +1092,8 @@ gi_status run_job(Ctx* c, int flags, int64_t* nlines_out) {
         const GroupLists& gl = glists[r][gi];
         if (gl.hn)
           GI_CUDA(c, timed(c, GI_PHASE_STENCIL, [&] {
-                    return launch_build_h_items(c->w_hitems.p + gl.h0, gl.hn, gl.hblocks,
-                                                c->stream);
+                    return launch_build_h_items(c->w_hitems.p + gl.h0, c->w_hfirst.p + gl.h0,
+                                                gl.hn, gl.hblocks, c->stream);
                   }));
       }
       for (size_t t = grp.first; t < grp.second && !batch_small; t++) {

@@ -11,13 +11,13 @@ namespace gi {
 // loads and searches there (a search in global memory is a chain of
 // dependent loads, microseconds per block).
 constexpr int kItemsSmem = 1024;
-template <class T, class F>
-__device__ __forceinline__ int find_item(const T* __restrict__ items, int nitems, long long b,
-                                         F first) {
+// first(k): the first grid block of item k (first(0) = 0, non-decreasing).
+template <class F>
+__device__ __forceinline__ int find_item(int nitems, long long b, F first) {
   __shared__ long long s_first[kItemsSmem];
   __shared__ int s_item;
   if (nitems <= kItemsSmem) {
-    for (int k = threadIdx.x; k < nitems; k += blockDim.x) s_first[k] = first(items[k]);
+    for (int k = threadIdx.x; k < nitems; k += blockDim.x) s_first[k] = first(k);
     __syncthreads();
     if (threadIdx.x == 0) {
       int lo = 0, hi = nitems - 1;
@@ -32,7 +32,7 @@ __device__ __forceinline__ int find_item(const T* __restrict__ items, int nitems
     int lo = 0, hi = nitems - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
-      if (first(items[mid]) <= b) lo = mid;
+      if (first(mid) <= b) lo = mid;
       else hi = mid - 1;
     }
     s_item = lo;

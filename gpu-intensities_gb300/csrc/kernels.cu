@@ -122,9 +122,10 @@ __global__ void k_build_h(const double* __restrict__ Z, size_t zc, int ldz, int 
 // block 256 functions s of kHCols initial columns (the item lookup is paid
 // once per kHCols columns).
 __global__ void __launch_bounds__(256) k_build_h_items(const HItem* __restrict__ items,
+                                                        const long long* __restrict__ firsts,
                                                         int nitems) {
   const long long b = blockIdx.x;
-  const int lo = find_item(items, nitems, b, [](const HItem& x) { return x.blk0; });
+  const int lo = find_item(nitems, b, [&](int k) { return firsts[k]; });
   const HItem& it = items[lo];
   const long long rel = b - it.blk0;
   const int nsb = (it.ldh + 255) >> 8;
@@ -144,11 +145,11 @@ __global__ void __launch_bounds__(256) k_build_h_items(const HItem* __restrict__
   }
 }
 
-cudaError_t launch_build_h_items(const HItem* items, int nitems, long long nblocks,
-                                 cudaStream_t st) {
+cudaError_t launch_build_h_items(const HItem* items, const long long* firsts, int nitems,
+                                 long long nblocks, cudaStream_t st) {
   if (nitems <= 0 || nblocks <= 0) return cudaSuccess;
   if (nblocks > 0x7FFFFFFFll) return cudaErrorInvalidValue;
-  k_build_h_items<<<(unsigned)nblocks, 256, 0, st>>>(items, nitems);
+  k_build_h_items<<<(unsigned)nblocks, 256, 0, st>>>(items, firsts, nitems);
   return cudaGetLastError();
 }
 
@@ -352,7 +353,7 @@ __global__ void k_col_norms(const double* __restrict__ H, int ldh, int n, double
 // [items[k].col0, items[k+1].col0) of the grid).
 __global__ void k_col_norms_items(const NormItem* __restrict__ items, int nitems) {
   const long long b = blockIdx.x;
-  const int lo = find_item(items, nitems, b, [](const NormItem& x) { return x.col0; });
+  const int lo = find_item(nitems, b, [&](int k) { return items[k].col0; });
   const NormItem& it = items[lo];
   const double* h = it.H + (size_t)(b - it.col0) * it.ldh;
   double acc = 0.0;

@@ -1633,7 +1633,7 @@ __global__ void __launch_bounds__(256)
                            uint32_t* __restrict__ out, int grouped, int32_t* __restrict__ e_out,
                            size_t rset) {
   const long long b = blockIdx.x;
-  const int lo = find_item(items, nitems, b, [](const YItem& x) { return x.row0; });
+  const int lo = find_item(nitems, b, [&](int k) { return items[k].row0; });
   const YItem& it = items[lo];
   if (b - it.row0 >= it.rows) return;  // not a row of any unit (the whole block)
   build_y_digits_row<S>(it.vecs, it.ld, it.ivec, it.ndeg, it.yptr, it.yroot, it.root_case,
