@@ -910,6 +910,17 @@ __global__ void __launch_bounds__(kThreadsG, 1)
 #pragma unroll
       for (int ch = 0; ch < NCH; ++ch) {
         const int c0 = half * HALF + ch * kChunkG;
+        // the earlier K segments' sums of this chunk, loaded before the
+        // tensor-memory reads so that their latency overlaps them
+        double prev[kChunkG];
+        if constexpr (ACC) {
+#pragma unroll
+          for (int j = 0; j < kChunkG; ++j) {
+            const int n = n0 + c0 + j;
+            prev[j] = (pass == NPASS - 1 && m < M && n < Nc)
+                          ? ld_acc(Cz + (size_t)n * ldc + m) : 0.0;
+          }
+        }
         uint32_t f[(D1 > S - D1 ? D1 : S - D1)][kChunkG];
 #pragma unroll
         for (int d = 0; d < (D1 > S - D1 ? D1 : S - D1); ++d)
@@ -949,7 +960,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
               if (NPASS == 2) out = scaled_int(v0[ch][j], base - w * (D1 - 1)) + out;
               else out = scaled_int(hi[j], base - w * (SPLIT - 1)) + out;
               double* dst = Cz + (size_t)n * ldc + m;
-              if constexpr (ACC) out += ld_acc(dst);
+              if constexpr (ACC) out += prev[j];
               *dst = out;
             }
           }
@@ -1268,6 +1279,15 @@ __global__ void __launch_bounds__(kThreadsG, 1)
 #pragma unroll
           for (int ch = 0; ch < NCH; ++ch) {
             const int c0 = half * HALF + ch * kChunkG;
+            // the earlier segments' sums of this chunk, loaded before the
+            // tensor-memory reads so that their latency overlaps them
+            double prev[kChunkG];
+#pragma unroll
+            for (int j = 0; j < kChunkG; ++j) {
+              const int n = n0 + c0 + j;
+              prev[j] = (pass == 1 && k0 > 0 && m < pr.M && n < pr.Nc)
+                            ? ld_acc(pr.C + (size_t)n * pr.ldc + m) : 0.0;
+            }
             uint32_t f[MAXD][kChunkG];
 #pragma unroll
             for (int d = 0; d < MAXD; ++d)
@@ -1301,7 +1321,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
                   double out = scaled_int(v0[ch][j], base - w * (D1 - 1)) +
                                scaled_int(v[j], base - w * (S - 1));
                   double* dst = pr.C + (size_t)n * pr.ldc + m;
-                  if (k0 > 0) out += ld_acc(dst);  // the earlier segments' sum
+                  if (k0 > 0) out += prev[j];  // the earlier segments' sum
                   if (!lines) *dst = out;
                   outv[j] = out;
                 }
