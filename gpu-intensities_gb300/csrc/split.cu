@@ -913,6 +913,12 @@ __global__ void __launch_bounds__(kThreadsG, 1)
         // the earlier K segments' sums of this chunk, loaded before the
         // tensor-memory reads so that their latency overlaps them
         double prev[kChunkG];
+        int ebc[kChunkG];  // the chunk's column exponents (last pass)
+#pragma unroll
+        for (int j = 0; j < kChunkG; ++j) {
+          const int n = n0 + c0 + j;
+          ebc[j] = (pass == NPASS - 1 && n < Nc) ? eb[n] : 0;
+        }
         if constexpr (ACC) {
 #pragma unroll
           for (int j = 0; j < kChunkG; ++j) {
@@ -955,7 +961,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
           for (int j = 0; j < kChunkG; ++j) {
             const int n = n0 + c0 + j;
             if (n < Nc) {
-              const int base = emr + eb[n] - 2 * w;
+              const int base = emr + ebc[j] - 2 * w;
               double out = scaled_int(v[j], base - w * (d1 - 1));
               if (NPASS == 2) out = scaled_int(v0[ch][j], base - w * (D1 - 1)) + out;
               else out = scaled_int(hi[j], base - w * (SPLIT - 1)) + out;
@@ -1282,6 +1288,12 @@ __global__ void __launch_bounds__(kThreadsG, 1)
             // the earlier segments' sums of this chunk, loaded before the
             // tensor-memory reads so that their latency overlaps them
             double prev[kChunkG];
+            int ebc[kChunkG];  // the chunk's column exponents (pass 1)
+#pragma unroll
+            for (int j = 0; j < kChunkG; ++j) {
+              const int n = n0 + c0 + j;
+              ebc[j] = (pass == 1 && n < pr.Nc) ? pr.eb[n] : 0;
+            }
 #pragma unroll
             for (int j = 0; j < kChunkG; ++j) {
               const int n = n0 + c0 + j;
@@ -1317,7 +1329,7 @@ __global__ void __launch_bounds__(kThreadsG, 1)
                 const int n = n0 + c0 + j;
                 outv[j] = 0.0;
                 if (row_ok && n < pr.Nc) {
-                  const int base = emr + pr.eb[n] - 2 * w;
+                  const int base = emr + ebc[j] - 2 * w;
                   double out = scaled_int(v0[ch][j], base - w * (D1 - 1)) +
                                scaled_int(v[j], base - w * (S - 1));
                   double* dst = pr.C + (size_t)n * pr.ldc + m;
