@@ -419,7 +419,7 @@ int dipole_panel_rows(const Ctx* c);
 
 cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int nI, int ndeg,
                            const Basis& b, int gamma, int degen, int N, int Kp, double* Y,
-                           cudaStream_t s);
+                           cudaStream_t s, int d0 = 0);
 cudaError_t launch_build_h(const double* Z, size_t zstride_c, int ldz, int nslotI, int ndegI,
                            int nI, const Basis& bF, int gammaF, int degF, int nsizeF, int ldh,
                            const StencilTerm* st, const int32_t* st_n, int st_max, double* H,

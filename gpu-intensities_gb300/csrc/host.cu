@@ -1815,7 +1815,9 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
   const int32_t* dstn = bI.d_pair_stn[jF - jI + 1].p;
   if (!dst || !dstn) return fail(c, GI_ERR_STATE, "basis J=%d has no term tables", jI);
   const int nsize = bI.Ntotal[gammaI], ld = round_up(nsize, 64), ndeg = c->degen[gammaI];
-  const int ncol = ndeg * bI.nslot;
+  // the Y columns of component ideg alone (the other components' would be
+  // contracted for nothing)
+  const int ncol = bI.nslot;
   // grow-only workspaces of the context: repeated calls allocate nothing
   GI_CUDA(c, c->hls_v.reserve(ld));
   GI_CUDA(c, c->hls_iv.reserve(1));
@@ -1837,8 +1839,8 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
                              cudaMemcpyHostToDevice, c->stream));
   double* y = c->hls_y.p;
   double* hh = c->hls_h.p;
-  GI_CUDA(c, launch_build_y(c->hls_v.p, ld, c->hls_iv.p, 1, ndeg, bI, gammaI, ndeg, c->N, c->Kp,
-                            y, c->stream));
+  GI_CUDA(c, launch_build_y(c->hls_v.p, ld, c->hls_iv.p, 1, 1, bI, gammaI, ndeg, c->N, c->Kp,
+                            y, c->stream, ideg));
   if (c->have_params && c->params.precision == GI_PREC_SPLIT && !c->streamed()) {
     // split precision: the narrow digit GEMM, one pass over the dipole digits
     // with K split over the SMs, its partial products summed by the stencil
@@ -1851,7 +1853,7 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
     s = split_gemm_dipole_narrow(c, y, c->Kp, ncol, c->hls_z.p, (size_t)ncol * ldz_max,
                                  max_parts, &nparts, &ldz);
     if (s != GI_OK) return s;
-    GI_CUDA(c, launch_half_ls_prim_parts(c->hls_z.p + (size_t)ideg * bI.nslot * ldz, nparts,
+    GI_CUDA(c, launch_half_ls_prim_parts(c->hls_z.p, nparts,
                                          (size_t)ncol * ldz_max, ldz, ldz / 3, bF, dst, dstn, 6,
                                          hh, c->stream));
   } else {
@@ -1859,7 +1861,7 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
     const size_t zc = (size_t)ncol * c->Kp;
     s = dipole_gemm_fp64(c, y, c->Kp, c->hls_z.p, c->Kp, zc, ncol, c->stream);
     if (s != GI_OK) return s;
-    GI_CUDA(c, launch_half_ls_prim(c->hls_z.p + (size_t)ideg * bI.nslot * c->Kp, zc, c->Kp, bF,
+    GI_CUDA(c, launch_half_ls_prim(c->hls_z.p, zc, c->Kp, bF,
                                    dst, dstn, 6, hh, c->stream));
   }
   GI_CUDA(c, cudaMemcpyAsync(c->hls_pin, hh, sizeof(double) * bF.D, cudaMemcpyDeviceToHost,

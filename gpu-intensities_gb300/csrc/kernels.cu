@@ -55,12 +55,14 @@ __global__ void k_build_y(const double* __restrict__ vecs, int ld, const int32_t
 
 cudaError_t launch_build_y(const double* vecs, int ld, const int32_t* ivec, int nI, int ndeg,
                            const Basis& b, int gamma, int degen, int N, int Kp, double* Y,
-                           cudaStream_t s) {
+                           cudaStream_t s, int d0) {
   if (nI == 0) return cudaSuccess;
   dim3 grid((b.nslot * Kp + 255) / 256, nI * ndeg);
+  // d0: the first degenerate component (ndeg = 1, d0 = d: component d alone)
   k_build_y<<<grid, 256, 0, s>>>(vecs, ld, ivec, ndeg, b.d_yptr.p, b.d_yroot.p, b.d_root_case.p,
                                  b.d_root_lam.p, b.d_case_iterm[gamma].p,
-                                 b.d_case_nelem[gamma].p, b.d_rep[gamma].p, b.Ntotal[gamma],
+                                 b.d_case_nelem[gamma].p,
+                                 b.d_rep[gamma].p + (size_t)d0 * b.Ntotal[gamma], b.Ntotal[gamma],
                                  degen, b.nslot, N, Kp, Y);
   return cudaGetLastError();
 }
