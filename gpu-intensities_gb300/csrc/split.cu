@@ -157,7 +157,7 @@ __device__ __forceinline__ double ld_acc(const double* p) {
 // a long stretch of straight-line code that ran out of the instruction cache
 // once per tile (39 us of a 265 us tile against 21 us called, measured with
 // per-tile clock stamps).
-__device__ __noinline__ double scaled_int(long long v, int E) {
+__device__ __forceinline__ double scaled_int_body(long long v, int E) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
   const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
@@ -166,6 +166,12 @@ __device__ __noinline__ double scaled_int(long long v, int E) {
   if (msb > 52 || ex <= 0 || ex >= 2047) return ldexp((double)v, E);
   const unsigned long long mant = (a << (52 - msb)) & ((1ull << 52) - 1);
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | mant));
+}
+__device__ __noinline__ double scaled_int(long long v, int E) { return scaled_int_body(v, E); }
+// a * 2^ea + b * 2^eb: the two parts of a two-pass tile's exact sums, added
+// in FP64 (one call per output element)
+__device__ __noinline__ double scaled_pair(long long a, int ea, long long b, int eb) {
+  return scaled_int_body(a, ea) + scaled_int_body(b, eb);
 }
 // Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 32
 // bytes (16 elements) with the 32-byte swizzle: 8-row groups 256 bytes apart.
@@ -962,9 +968,11 @@ __global__ void __launch_bounds__(kThreadsG, 1)
             const int n = n0 + c0 + j;
             if (n < Nc) {
               const int base = emr + ebc[j] - 2 * w;
-              double out = scaled_int(v[j], base - w * (d1 - 1));
-              if (NPASS == 2) out = scaled_int(v0[ch][j], base - w * (D1 - 1)) + out;
-              else out = scaled_int(hi[j], base - w * (SPLIT - 1)) + out;
+              double out;
+              if (NPASS == 2)
+                out = scaled_pair(v0[ch][j], base - w * (D1 - 1), v[j], base - w * (d1 - 1));
+              else
+                out = scaled_pair(hi[j], base - w * (SPLIT - 1), v[j], base - w * (d1 - 1));
               double* dst = Cz + (size_t)n * ldc + m;
               if constexpr (ACC) out += prev[j];
               *dst = out;
@@ -1330,8 +1338,8 @@ __global__ void __launch_bounds__(kThreadsG, 1)
                 outv[j] = 0.0;
                 if (row_ok && n < pr.Nc) {
                   const int base = emr + ebc[j] - 2 * w;
-                  double out = scaled_int(v0[ch][j], base - w * (D1 - 1)) +
-                               scaled_int(v[j], base - w * (S - 1));
+                  double out = scaled_pair(v0[ch][j], base - w * (D1 - 1), v[j],
+                                           base - w * (S - 1));
                   double* dst = pr.C + (size_t)n * pr.ldc + m;
                   if (k0 > 0) out += prev[j];  // the earlier segments' sum
                   if (!lines) *dst = out;
