@@ -173,6 +173,14 @@ __device__ __noinline__ double scaled_int(long long v, int E) { return scaled_in
 __device__ __noinline__ double scaled_pair(long long a, int ea, long long b, int eb) {
   return scaled_int_body(a, ea) + scaled_int_body(b, eb);
 }
+// the same for two elements in one call (their conversions interleave)
+__device__ __noinline__ double2 scaled_pair2(long long a0, int ea0, long long b0, int eb0,
+                                             long long a1, int ea1, long long b1, int eb1) {
+  double2 r;
+  r.x = scaled_int_body(a0, ea0) + scaled_int_body(b0, eb0);
+  r.y = scaled_int_body(a1, ea1) + scaled_int_body(b1, eb1);
+  return r;
+}
 // Shared-memory matrix descriptor of a K-major bf16 tile whose rows are 32
 // bytes (16 elements) with the 32-byte swizzle: 8-row groups 256 bytes apart.
 __device__ __forceinline__ uint64_t sdesc_sw32(uint32_t addr) {
@@ -963,16 +971,24 @@ __global__ void __launch_bounds__(kThreadsG, 1)
 #pragma unroll
           for (int j = 0; j < kChunkG; ++j) v0[ch][j] = v[j];
         } else if (m < M) {
+          double outc[kChunkG];
+#pragma unroll
+          for (int j = 0; j < kChunkG; j += 2) {
+            const int b0 = emr + ebc[j] - 2 * w, b1 = emr + ebc[j + 1] - 2 * w;
+            const double2 o =
+                NPASS == 2
+                    ? scaled_pair2(v0[ch][j], b0 - w * (D1 - 1), v[j], b0 - w * (d1 - 1),
+                                   v0[ch][j + 1], b1 - w * (D1 - 1), v[j + 1], b1 - w * (d1 - 1))
+                    : scaled_pair2(hi[j], b0 - w * (SPLIT - 1), v[j], b0 - w * (d1 - 1),
+                                   hi[j + 1], b1 - w * (SPLIT - 1), v[j + 1], b1 - w * (d1 - 1));
+            outc[j] = o.x;
+            outc[j + 1] = o.y;
+          }
 #pragma unroll
           for (int j = 0; j < kChunkG; ++j) {
             const int n = n0 + c0 + j;
             if (n < Nc) {
-              const int base = emr + ebc[j] - 2 * w;
-              double out;
-              if (NPASS == 2)
-                out = scaled_pair(v0[ch][j], base - w * (D1 - 1), v[j], base - w * (d1 - 1));
-              else
-                out = scaled_pair(hi[j], base - w * (SPLIT - 1), v[j], base - w * (d1 - 1));
+              double out = outc[j];
               double* dst = Cz + (size_t)n * ldc + m;
               if constexpr (ACC) out += prev[j];
               *dst = out;
