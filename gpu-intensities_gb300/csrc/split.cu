@@ -1347,15 +1347,22 @@ __global__ void __launch_bounds__(kThreadsG, 1)
               // other segment stores its sum for the next one
               const bool row_ok = m < pr.M;
               const bool lines = P.fused && k0 + kKSeg >= pr.K;
-              double outv[kChunkG];
+              double outc[kChunkG], outv[kChunkG];
+#pragma unroll
+              for (int j = 0; j < kChunkG; j += 2) {
+                const int b0 = emr + ebc[j] - 2 * w, b1 = emr + ebc[j + 1] - 2 * w;
+                const double2 o = scaled_pair2(v0[ch][j], b0 - w * (D1 - 1), v[j],
+                                               b0 - w * (S - 1), v0[ch][j + 1],
+                                               b1 - w * (D1 - 1), v[j + 1], b1 - w * (S - 1));
+                outc[j] = o.x;
+                outc[j + 1] = o.y;
+              }
 #pragma unroll
               for (int j = 0; j < kChunkG; ++j) {
                 const int n = n0 + c0 + j;
                 outv[j] = 0.0;
                 if (row_ok && n < pr.Nc) {
-                  const int base = emr + ebc[j] - 2 * w;
-                  double out = scaled_pair(v0[ch][j], base - w * (D1 - 1), v[j],
-                                           base - w * (S - 1));
+                  double out = outc[j];
                   double* dst = pr.C + (size_t)n * pr.ldc + m;
                   if (k0 > 0) out += prev[j];  // the earlier segments' sum
                   if (!lines) *dst = out;
