@@ -68,8 +68,8 @@ CPU_SAMPLE = {"c3v_batched": ((20, 21), 2), "c2v_plain": ((9, 10), 8),
 # bytes read per Y column per K element (the digit planes streamed past the
 # tiles) and bytes written per Y column (Z).  A job's K runs in segments of
 # 2048; each later segment re-reads Z to add to it.
-SPLIT_HALFLS_TRAFFIC = {3000: {"read_per_col_k": 37208139776 / (47904 * 2048),
-                               "write_per_col": 4328358912 / 47904,
+SPLIT_HALFLS_TRAFFIC = {3000: {"read_per_col_k": 44108294656 / (47904 * 2048),
+                               "write_per_col": 4468934656 / 47904,
                                "capture": "c3v_batched J <= 8, 47904 Y columns, K = 2048"}}
 
 

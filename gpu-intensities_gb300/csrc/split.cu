@@ -152,11 +152,7 @@ __device__ __forceinline__ double ld_acc(const double* p) {
 // v * 2^E for an integer |v| < 2^53 (so the double is exact), built from the
 // bits with integer instructions: FP64 throughput is low on this GPU and the
 // epilogues convert every output element.  Results outside the normal range
-// take ldexp.  Not inlined: the epilogues' unrolled column loops call it twice
-// per element, and inlined copies made the pass-1 epilogue of the half-ls GEMM
-// a long stretch of straight-line code that ran out of the instruction cache
-// once per tile (39 us of a 265 us tile against 21 us called, measured with
-// per-tile clock stamps).
+// take ldexp.
 __device__ __forceinline__ double scaled_int_body(long long v, int E) {
   if (v == 0) return 0.0;
   const unsigned long long sgn = v < 0 ? (1ull << 63) : 0ull;
@@ -167,13 +163,15 @@ __device__ __forceinline__ double scaled_int_body(long long v, int E) {
   const unsigned long long mant = (a << (52 - msb)) & ((1ull << 52) - 1);
   return __longlong_as_double((long long)(sgn | ((unsigned long long)ex << 52) | mant));
 }
+// The epilogues call these instead of inlining the conversion: inlined into
+// the unrolled column chunks, it made the pass-1 epilogue of the half-ls GEMM
+// a long stretch of straight-line code that ran out of the instruction cache
+// once per tile (39 us of a 265 us tile, against 21 us called, measured with
+// per-tile clock stamps).
 __device__ __noinline__ double scaled_int(long long v, int E) { return scaled_int_body(v, E); }
-// a * 2^ea + b * 2^eb: the two parts of a two-pass tile's exact sums, added
-// in FP64 (one call per output element)
-__device__ __noinline__ double scaled_pair(long long a, int ea, long long b, int eb) {
-  return scaled_int_body(a, ea) + scaled_int_body(b, eb);
-}
-// the same for two elements in one call (their conversions interleave)
+// a0 * 2^ea0 + b0 * 2^eb0 and the same for a second element, in one call (the
+// two parts of a two-pass tile's exact sums, added in FP64; the conversions of
+// the two elements interleave)
 __device__ __noinline__ double2 scaled_pair2(long long a0, int ea0, long long b0, int eb0,
                                              long long a1, int ea1, long long b1, int eb1) {
   double2 r;

@@ -72,3 +72,39 @@ def test_noalloc_rejects_sizes_beyond_scratch(pkg, synth):
                           torch.cuda.current_stream().cuda_stream)
         assert st == pkg.GI_ERR_ARG
         assert b"beyond the fixed scratch" in pkg.lib().gi_last_error(eng._h)
+
+
+def test_noalloc_captured_in_a_graph(pkg, synth):
+    """The call issues only device work on the caller's stream (no host copy,
+    no synchronisation), so after a first call on the device it can be
+    captured into a CUDA graph: a replay after the input vector changed gives
+    that vector's half line strength, bit for bit the direct call's."""
+    torch = pytest.importorskip("torch")
+    prob = synth.make_c3v(4, 14, [1, 2], nvec_max=3)
+    with pkg.Engine(0) as eng:
+        eng.load(prob)
+        jI, gI = 1, 2  # E: the second degenerate component below
+        blk = prob.blocks[(jI, gI)]
+        jF = jI + 1
+        DF = prob.bases[jF].Maxcontracts
+        d = prob.degen[gI] - 1
+        s = torch.cuda.Stream()
+        vdev = torch.from_numpy(np.ascontiguousarray(blk.vecs[0])).to("cuda")
+        out = torch.zeros(DF, dtype=torch.float64, device="cuda")
+        direct = torch.zeros_like(out)
+        with torch.cuda.stream(s):
+            assert call_noalloc(pkg, eng, jI, gI, d, jF, vdev, out, s.cuda_stream) == pkg.GI_OK
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            st = call_noalloc(pkg, eng, jI, gI, d, jF, vdev, out, s.cuda_stream)
+        assert st == pkg.GI_OK, pkg.lib().gi_last_error(eng._h)
+        vdev.copy_(torch.from_numpy(np.ascontiguousarray(blk.vecs[1])))
+        g.replay()
+        torch.cuda.synchronize()
+        with torch.cuda.stream(s):
+            assert call_noalloc(pkg, eng, jI, gI, d, jF, vdev, direct, s.cuda_stream) == pkg.GI_OK
+        torch.cuda.synchronize()
+        assert torch.equal(out, direct)
+        want = eng.half_ls(jI, gI, d, jF, blk.vecs[1], DF)
+        assert np.abs(out.cpu().numpy() - want).max() <= 1e-13 * np.abs(want).max()
