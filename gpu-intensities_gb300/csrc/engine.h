@@ -321,6 +321,14 @@ struct Ctx {
   DevArray<double> hls_v, hls_y, hls_z, hls_h;  // gi_half_ls (grow-only)
   double* hls_pin = nullptr;                     // its pinned host staging
   size_t hls_pin_cap = 0;
+  // gi_half_ls: the launch sequence of a call shape, captured on its second
+  // call and replayed while the shape and every buffer it names are unchanged
+  struct HlsGraph {
+    uint64_t sig;
+    cudaGraphExec_t exec;
+  };
+  std::vector<HlsGraph> hls_graphs;  // most recently used first
+  uint64_t hls_last_sig = 0;         // the last call run eagerly
   DevArray<int32_t> hls_iv;
   DevArray<double> w_y, w_z, w_h, w_t, w_EI;
   DevArray<unsigned long long> w_counter;

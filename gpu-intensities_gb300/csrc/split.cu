@@ -2677,6 +2677,10 @@ uint64_t split_identity(Ctx* c) {
   return h;
 }
 
+const int* split_error_word(const Ctx* c) {
+  return c->split ? c->split->err.p : nullptr;
+}
+
 gi_status split_check(Ctx* c) {
   if (!c->split || !c->split->err.p) return GI_OK;
   int e = 0;

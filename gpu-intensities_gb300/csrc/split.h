@@ -82,5 +82,8 @@ int split_digits(const Ctx* c);
 void split_invalidate(Ctx* c);  // the dipole changed: drop its cached slices
 // After a run: reads the device error word the split kernels set on a timeout.
 gi_status split_check(Ctx* c);
+// The device error word of the context's split GEMMs (nullptr before the
+// first split-precision GEMM), for a read ordered on a stream.
+const int* split_error_word(const Ctx* c);
 void split_release(Ctx* c);
 }  // namespace gi

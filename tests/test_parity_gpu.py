@@ -212,3 +212,22 @@ def test_threshold_guard_band(pkg, synth, oracle, precision, which):
                     norm_tol=1e-12 if precision else 1e-13)
         prob.params.thresh_linestrength = 0.0
         with_threshold(prob)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_half_ls_repeated_calls_replay_a_graph(pkg, synth, precision):
+    """The second call of a gi_half_ls shape is captured into a CUDA graph and
+    later calls replay it: every call gives, bit for bit, what a first (eager)
+    call on the same vector gives, also after the shape changed in between."""
+    prob = synth.make_c3v(4, 14, [1, 2], nvec_max=4)
+    DF = prob.bases[2].Maxcontracts
+    blk = prob.blocks[(1, 2)]
+    order = [(0, 1), (1, 1), (2, 1), (3, 0), (0, 1), (3, 1), (1, 0), (2, 1)]
+    with pkg.Engine(0) as eng:
+        eng.load(prob, precision=precision)
+        got = [eng.half_ls(1, 2, d, 2, blk.vecs[i], DF) for i, d in order]
+    for (i, d), g in zip(order, got):
+        with pkg.Engine(0) as fresh:
+            fresh.load(prob, precision=precision)
+            want = fresh.half_ls(1, 2, d, 2, blk.vecs[i], DF)
+        assert np.array_equal(g, want), (i, d)
