@@ -1892,36 +1892,45 @@ gi_status gi_half_ls(gi_ctx* h, int jI, int gammaI, int ideg, int jF, const doub
   if (split_path) mixv(split_identity(c));
   std::memcpy(c->hls_pin, vsym, sizeof(double) * nsize);
   *err_word = 0;
-  // graphs need a capturable stream (not the legacy default stream)
-  const bool graphable = c->stream != nullptr && !c->streamed();
+  // graphs need a capturable stream (not the legacy or per-thread default
+  // stream); a streamed dipole's panel copies are not captured
+  const bool graphable = c->stream != nullptr && c->stream != cudaStreamLegacy &&
+                         c->stream != cudaStreamPerThread && !c->streamed();
   auto hit = std::find_if(c->hls_graphs.begin(), c->hls_graphs.end(),
                           [&](const Ctx::HlsGraph& g) { return g.sig == sig; });
+  bool done = false;
   if (graphable && hit != c->hls_graphs.end()) {
     GI_CUDA(c, cudaGraphLaunch(hit->exec, c->stream));
     std::rotate(c->hls_graphs.begin(), hit, hit + 1);
+    done = true;
   } else if (graphable && c->hls_last_sig == sig) {
     // the second call of this shape: capture it (the first ran eagerly and
     // made every allocation and kernel attribute the sequence needs)
-    GI_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-    const gi_status q = issue();
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
-    if (q != GI_OK) {
-      if (graph) cudaGraphDestroy(graph);
-      return q;
+    if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      const gi_status q = issue();
+      cudaGraph_t graph = nullptr;
+      const cudaError_t ee = cudaStreamEndCapture(c->stream, &graph);
+      if (q != GI_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return q;
+      }
+      GI_CUDA(c, ee);
+      cudaGraphExec_t exec = nullptr;
+      const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+      cudaGraphDestroy(graph);
+      GI_CUDA(c, ie);
+      if (c->hls_graphs.size() >= 8) {
+        cudaGraphExecDestroy(c->hls_graphs.back().exec);
+        c->hls_graphs.pop_back();
+      }
+      c->hls_graphs.insert(c->hls_graphs.begin(), Ctx::HlsGraph{sig, exec});
+      GI_CUDA(c, cudaGraphLaunch(exec, c->stream));
+      done = true;
+    } else {
+      cudaGetLastError();  // a stream that refuses the capture runs the call eagerly
     }
-    GI_CUDA(c, ee);
-    cudaGraphExec_t exec = nullptr;
-    const cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    GI_CUDA(c, ie);
-    if (c->hls_graphs.size() >= 8) {
-      cudaGraphExecDestroy(c->hls_graphs.back().exec);
-      c->hls_graphs.pop_back();
-    }
-    c->hls_graphs.insert(c->hls_graphs.begin(), Ctx::HlsGraph{sig, exec});
-    GI_CUDA(c, cudaGraphLaunch(exec, c->stream));
-  } else {
+  }
+  if (!done) {
     s = issue();
     if (s != GI_OK) return s;
     c->hls_last_sig = sig;
